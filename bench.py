@@ -1,0 +1,322 @@
+"""Benchmark: frequency-solves per second of the IBEM inverse pipeline.
+
+Workload (the configuration the headline metric is quoted on): a sphere of
+radius 0.10 m meshed as an icosphere (642 nodes, 1280 triangles), 120
+microphones on a hemisphere of radius 0.30 m, 64 frequencies 100-2000 Hz,
+7-point regular / Duffy singular quadrature, pulsating + oscillating sphere
+velocity with seeded complex amplitudes, 30 dB SNR.  One step = one batched
+pass over the 64 frequencies: assembly, H = A_hs A^-1 B - B_hs, Jacobi SVD,
+GCV, Tikhonov.  Seeded synthetic inputs (no dataset is involved).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0.  Under torchrun each rank solves its own 64
+frequencies (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "freq-solves/sec (assemble+SVD+GCV) mixed vs FP64 on 1 GB300 at 1e-6 rel err"
+UNIT = "freq-solves/s"
+N_FREQ = 64
+
+
+def _parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _workload():
+    from inverseacoustics_gb300 import geometry as g
+    import numpy as np
+    w = g.ibem_sphere(n_freq=N_FREQ)
+    mics = w.arrays["mics"]
+    amp = w.params["amp"]
+    rng = w.params["rng"]
+    p = np.stack([
+        g.add_noise(rng, amp[f, 0] * g.pulsating_sphere_pressure(mics, w.k[f], 0.1, 1.0) +
+                    amp[f, 1] * g.oscillating_sphere_pressure(mics, w.k[f], 0.1, 1.0), 30.0)[None, :]
+        for f in range(N_FREQ)])
+    return w, p
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) == 6:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def _cpu_baseline(freqs, threads=0, repeat=1):
+    cmd = [sys.executable, "-m", "oracle.cpu_pipeline", "--freqs", str(freqs), "--threads", str(threads),
+           "--repeat", str(repeat)]
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=ROOT, env=env, timeout=900)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build_oracle()
+    threads = os.cpu_count() or 1
+    sample = max(threads, 8)
+    for _ in range(args.warmup):
+        _cpu_baseline(sample, threads, 1)
+    res = _cpu_baseline(sample, threads, args.steps)
+    rates = res["rates"]
+    value = sum(rates) / len(rates)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies": N_FREQ,
+                       "parallelism": "host threads, frequency-parallel"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
+                             "sample": res["sample"], "cpu": res["cpu"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from inverseacoustics_gb300 import api
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    w, p_np = _workload()
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    stream = torch.cuda.current_stream(dev)
+    ctx = api.Context(local, stream)
+    mesh = api.Mesh(ctx, nodes, elems)
+    mics_d = torch.as_tensor(mics, device=dev)
+    k_d = torch.as_tensor(w.k, device=dev)
+    p_d = torch.as_tensor(p_np, device=dev)
+    p_h = torch.as_tensor(p_np).pin_memory()
+    cfg = api.default_config()
+    m, l = nodes.shape[1], mics.shape[1]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
+
+    def step():
+        return api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, cfg)
+
+    for _ in range(max(args.warmup, 3)):
+        x, lam, s, info = step()
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0, f"solver info flags {info.tolist()}"
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing
+    times = []
+    launches0 = ctx.launches()
+    barrier()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            x, lam, s, info = step()
+            e1.record(stream)
+            times.append((e0, e1))
+        barrier()
+    launches = ctx.launches() - launches0
+    ms = [a.elapsed_time(b) for a, b in times]
+    total_ms = sum(ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * N_FREQ * args.steps / (total_ms / 1000.0)
+
+    # ---- end to end through the public API, host buffers
+    x_h = torch.empty((N_FREQ, 1, m), dtype=torch.complex128).pin_memory()
+    lam_h = torch.empty((N_FREQ, 1), dtype=torch.float64).pin_memory()
+    e2e_times = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        p_d.copy_(p_h, non_blocking=True)
+        x, lam, s, info = step()
+        x_h.copy_(x, non_blocking=True)
+        lam_h.copy_(lam, non_blocking=True)
+        e1.record(stream)
+        e2e_times.append((e0, e1))
+    barrier()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * N_FREQ * args.steps / (e2e_ms / 1000.0)
+
+    # ---- per-stage timing (same stream, CUDA events) for the roofline
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        acc = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            acc += a.elapsed_time(b)
+        return acc / reps
+
+    t_asm = timed(lambda: api.ibem_assemble_batch(ctx, mesh, mics_d, k_d, cfg))
+    t_transfer = timed(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg))
+    H, _ = api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg)
+    t_solve = timed(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg))
+    hbm_peak, bf16_peak, peak_kind = _peaks()
+    # assembly: algorithmic bytes = rows written, (m + l) rows x m columns x (A, B) x 16 B per frequency
+    asm_bytes = N_FREQ * (m + l) * m * 2 * 16
+    # FP64 work of the dense stages (complex: 8 flops per multiply-add)
+    lu_flops = N_FREQ * (8.0 / 3.0 * m ** 3 + 8.0 * m * m * l + 8.0 * m * m * l)
+    fp64_tflops_dgemm = None
+    try:
+        a64 = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+        torch.mm(a64, a64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            torch.mm(a64, a64)
+        torch.cuda.synchronize()
+        fp64_tflops_dgemm = 3 * 2 * 4096 ** 3 / (time.perf_counter() - t0) / 1e12
+        del a64
+    except Exception:
+        pass
+    roofline = {"kernel": "ibem_rows_kernel (assembly)", "bound": "hbm",
+                "achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": None,
+                "peak_kind": peak_kind,
+                "note": "FP64-issue bound, not HBM bound; see compute",
+                "compute": {"stage": "LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
+                            "achieved": lu_flops / ((t_transfer - t_asm) / 1000.0) / 1e12,
+                            "peak_dgemm_measured": fp64_tflops_dgemm}}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            res = _cpu_baseline(16, 0, 1)
+            cpu = {"value": res["rates"][0], "unit": UNIT, "cores": res["threads"], "kind": "port",
+                   "sample": res["sample"], "cpu": res["cpu"]}
+        except Exception as e:  # a baseline failure must not hide the GPU line
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"[:200]}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "precision_path": "fp64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies_per_gpu": N_FREQ,
+                           "nodes": m, "triangles": int(elems.shape[1]), "mics": l,
+                           "rules": "7-point Radon regular, 4x4 Duffy singular", "parallelism": f"freq-shard x{world}",
+                           "l2": "flushed between timed steps (256 MB write)"},
+                "stages_ms": {"assembly": t_asm, "transfer_incl_assembly": t_transfer, "svd_gcv_tikhonov": t_solve},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(p_np.nbytes),
+                        "d2h_bytes_per_step": int(x_h.numel() * 16 + lam_h.numel() * 8)},
+                "gpu_launches": int(launches)}
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = _parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

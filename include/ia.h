@@ -1,0 +1,218 @@
+/* ia.h -- C ABI of the GB300-native inverse-acoustics library (libia.so).
+ *
+ * Two layers:
+ *
+ * 1. Reference-compatible entry points.  Same argument order and meaning as
+ *    the reference's CUDA headers' functions: host input arrays, outputs malloc'd
+ *    by the callee and released by the caller (here with ia_free or free()).
+ *    Where the reference throws or exit()s, these return a status code.
+ *
+ *      ia_esm   <- esm()   CUDA/esm.cuh:112   (and esmgpu() CUDA/esm.cuh:38)
+ *      ia_ibem  <- ibem()  CUDA/ibem.cuh:424  (and ibemgpu() CUDA/ibem.cuh:263)
+ *      ia_hels  <- hels()  CUDA/hels.cuh:222  (and helsgpu() CUDA/hels.cuh:185)
+ *      ia_csvd  <- csvd()  CUDA/tsvd.cuh:10
+ *      ia_tsvd  <- tsvd()  CUDA/tsvd.cuh:122
+ *      ia_to_pressure / ia_to_velocity / ia_sound_power
+ *               <- to_pressure / to_velocity / sound_power CUDA/utils.cuh:199,232,265
+ *
+ * 2. Device-resident batched entry points (the GB300 path).  All array
+ *    arguments named d_* are device pointers; one call processes F
+ *    frequencies, each an independent problem.  Calls are ordered on the
+ *    context's CUDA stream and do not synchronise the host unless stated.
+ *
+ * Conventions (as the reference): complex numbers are interleaved double
+ * pairs (the layout of cuDoubleComplex); matrices are column-major; point
+ * sets are structure-of-arrays x[0..n), y[0..n), z[0..n) (CUDA/esm.cuh:9);
+ * triangle connectivity is e_n[i + j*n], 0-based (CUDA/ibem.cuh:10).  The
+ * outgoing wave is exp(+ikr) (CUDA/esm.cuh:16).  A batch of F matrices of
+ * size r x c is stored as F consecutive column-major r x c blocks.
+ *
+ * Every function returns an ia_status; nothing throws across this ABI.
+ */
+#ifndef IA_H
+#define IA_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { double re, im; } ia_complex;
+
+typedef enum {
+    IA_OK = 0,
+    IA_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, k out of range) */
+    IA_ERR_CUDA = 2,         /* CUDA runtime error (see ia_last_cuda_error) */
+    IA_ERR_ALLOC = 3,        /* host or device allocation failed */
+    IA_ERR_NOCONV = 4,       /* a Jacobi iteration hit its sweep cap (per-frequency info says which) */
+    IA_ERR_SINGULAR = 5,     /* an exactly zero pivot in an LU factorisation */
+    IA_ERR_NONFINITE = 6,    /* NaN or Inf in an input or a result */
+    IA_ERR_RULE = 7,         /* invalid quadrature rule */
+    IA_ERR_TOO_LARGE = 8     /* size above a fixed limit of the called entry point */
+} ia_status;
+
+/* per-frequency info words written by the batched solvers (bit flags) */
+#define IA_INFO_NOCONV    1  /* Jacobi sweep cap reached */
+#define IA_INFO_SINGULAR  2  /* zero pivot */
+#define IA_INFO_NONFINITE 4  /* NaN/Inf met */
+
+enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
+enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };
+enum { IA_METHOD_TIKHONOV_GCV = 0, IA_METHOD_TSVD = 1, IA_METHOD_TIKHONOV_FIXED = 2 };
+
+typedef struct {
+    double c;              /* speed of sound [m/s]; reference C_AIR (CUDA/constants.cuh:2) */
+    double rho;            /* density [kg/m^3]; reference RHO_AIR (CUDA/constants.cuh:5) */
+    int method;            /* IA_METHOD_* */
+    int gcv_mode;          /* IA_GCV_STANDARD (Hansen's Tikhonov GCV) or IA_GCV_REFERENCE (gcvG.m as written) */
+    int gcv_points;        /* grid size, 200 in gcvG.m:20 */
+    double gcv_lo;         /* fixed log-spaced grid [gcv_lo, gcv_hi]; both 0 selects */
+    double gcv_hi;         /*   regtools' grid max(s_p, 16 eps s_1) .. s_1 (gcvG.m:28-30) */
+    double lambda_fixed;   /* lambda for IA_METHOD_TIKHONOV_FIXED */
+    int tsvd_k;            /* truncation index for IA_METHOD_TSVD, 1 <= k <= p */
+    int precision;         /* IA_PREC_FP64 or IA_PREC_MIXED */
+    int svd_max_sweeps;    /* Jacobi sweep cap (default 40) */
+    int refine_steps;      /* iterative-refinement steps of the mixed path (default 2) */
+} ia_config;
+
+/* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,
+ * weights summing to 1/2 as in the reference's IPF.txt / IPFs.txt
+ * (CUDA/ibem.cuh:276-311).  singular holds 3 pages (one per vertex of the
+ * element, the vertex with shape function 1 at the singular point), each
+ * 3*nqs doubles. */
+typedef struct {
+    int nq;
+    const double *regular;   /* 3*nq   : xi1[nq], xi2[nq], w[nq] */
+    int nqs;
+    const double *singular;  /* 9*nqs  : page0, page1, page2 */
+} ia_rules;
+
+void ia_config_default(ia_config *cfg);
+/* sizeof(ia_config), for bindings that mirror the struct */
+int ia_config_size(void);
+const char *ia_status_string(int status);
+const char *ia_version(void);
+int ia_last_cuda_error(void);
+void ia_free(void *p);
+
+/* ---------------------------------------------------------------- layer 1 */
+
+/* ESM: Me = M_sq D^-1 (m x m), He = M_hq D^-1 (l x m), sources at r_ms*r_i.
+ * Replaces esm() CUDA/esm.cuh:112 (correct for l != m, where the reference's
+ * M_hq leading dimension is wrong). */
+int ia_esm(int m, int l, const double *r_ms, const double *r_lh, ia_complex **m_e, ia_complex **h,
+           double k, double r_i, const ia_config *cfg);
+
+/* IBEM: Z = A \ (i rho c k B) (m x m) and H = A_hs Z - i rho c k B_hs (l x m).
+ * n triangles e_n, n_ch CHIEF points cp (least squares when n_ch > 0).
+ * rules == NULL selects the built-in 7-point regular / 4x4 Duffy singular rules.
+ * Replaces ibem() CUDA/ibem.cuh:424 (which reads IPF.txt/IPFs.txt from the cwd). */
+int ia_ibem(int m, int l, int n, const double *r_ms, const int *e_n, const double *r_lh, ia_complex **m_e,
+            ia_complex **h, double k, int n_ch, const double *cp, const ia_rules *rules, const ia_config *cfg);
+
+/* HELS: Me (m x nt), He (l x nt), Qe (m x nt), nt = (n_sh+1)^2, column
+ * i = n^2 + n + m.  Points in (az, el, r) structure-of-arrays.
+ * Replaces hels() CUDA/hels.cuh:222. */
+int ia_hels(int m, int l, const double *r_ms_s, const double *r_lh_s, ia_complex **m_e, ia_complex **h,
+            ia_complex **q_e, double k, int n_sh, const ia_config *cfg);
+
+/* Compact SVD a = u diag(s) v^H: u m x p, s p, v n x p, p = min(m, n),
+ * s descending.  Replaces csvd() CUDA/tsvd.cuh:10 (which returns v n x n
+ * when m >= n; the first p columns agree). */
+int ia_csvd(int m, int n, const ia_complex *a, ia_complex **u, double **s, ia_complex **v);
+
+/* x = V(:,1:k) diag(1/s(1:k)) U(:,1:p)^H b.  Returns IA_ERR_ARG for k
+ * outside [1, p] (the reference prints and leaves *x unset,
+ * CUDA/tsvd.cuh:124-126).  Replaces tsvd() CUDA/tsvd.cuh:122. */
+int ia_tsvd(int m, int n, int p, int k, const ia_complex *u, const double *s, const ia_complex *v,
+            const ia_complex *b, ia_complex **x);
+
+/* p = Me x, v = Qe x (m x n times n); W = 1/2 Re(v^H p) S/m.
+ * Replace CUDA/utils.cuh:199, :232, :265. */
+int ia_to_pressure(int m, int n, const ia_complex *me, const ia_complex *x, ia_complex **p);
+int ia_to_velocity(int m, int n, const ia_complex *qe, const ia_complex *x, ia_complex **v);
+int ia_sound_power(int m, const ia_complex *p, const ia_complex *v, double *w, double s);
+
+/* ---------------------------------------------------------------- layer 2 */
+
+typedef struct ia_context ia_context;
+typedef struct ia_mesh ia_mesh;
+
+/* stream: a cudaStream_t (NULL = legacy default stream). */
+int ia_create(ia_context **ctx, int device, void *stream);
+int ia_destroy(ia_context *ctx);
+int ia_set_stream(ia_context *ctx, void *stream);
+int ia_synchronize(ia_context *ctx);
+/* number of kernels this context has launched since creation */
+long long ia_launch_count(const ia_context *ctx);
+
+/* Upload a triangle mesh (host arrays) with its quadrature rules; builds the
+ * element geometry, the element colouring and the node-to-element adjacency
+ * used by the gather-form assembly. */
+int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int *elems, const ia_rules *rules,
+                   ia_mesh **mesh);
+int ia_mesh_destroy(ia_mesh *mesh);
+
+/* G_f(i,j) = exp(i k_f r_ij)/(4 pi r_ij), microphones d_mics (3 x l SoA) by
+ * sources d_src (3 x m SoA): the plain ESM transfer matrix, F x (l x m). */
+int ia_monopole_batch(ia_context *ctx, int l, int m, int F, const double *d_mics, const double *d_src,
+                      const double *d_k, ia_complex *d_G);
+
+/* IBEM system rows for F wavenumbers, row-major rows (each collocation row
+ * contiguous, i.e. the column-major transpose):
+ *   d_At, d_Bt : F x (m x mt)  columns = surface rows 0..m-1 then CHIEF rows
+ *   d_Ahs_t, d_Bhs_t : F x (m x l)  columns = field rows
+ * B terms scaled by i rho c k.  Any of the outputs may be NULL only together
+ * with its partner. */
+int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                           const double *d_cp, int F, const double *d_k, const ia_config *cfg, ia_complex *d_At,
+                           ia_complex *d_Bt, ia_complex *d_Ahs_t, ia_complex *d_Bhs_t);
+
+/* IBEM transfer matrices H_f = A_hs A^-1 B - B_hs (F x (l x m)), without
+ * forming Z (an l-right-hand-side solve); square systems only (n_ch = 0). */
+int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                           const double *d_k, const ia_config *cfg, ia_complex *d_H, int *d_info);
+
+/* HELS field matrix He (F x (l x nt)) at points (az, el, r) d_pts. */
+int ia_hels_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k,
+                  ia_complex *d_H);
+
+/* Batched compact SVD of F matrices m x n: d_U F x (m x p), d_s F x p,
+ * d_V F x (n x p), p = min(m, n); d_U / d_V may be NULL. */
+int ia_svd_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_A, ia_complex *d_U, double *d_s,
+                 ia_complex *d_V, int *d_info);
+
+/* Regularised solves from SVD factors: for each frequency f and right-hand
+ * side r, x = V diag(phi) U^H b with phi from cfg->method (Tikhonov with the
+ * GCV lambda, TSVD, or a fixed lambda).  d_b F x (m x nrhs), d_x F x (n x nrhs),
+ * d_lambda F x nrhs (lambda used; 0 for TSVD). */
+int ia_regularize_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_U, const double *d_s,
+                        const ia_complex *d_V, int nrhs, const ia_complex *d_b, const ia_config *cfg,
+                        ia_complex *d_x, double *d_lambda);
+
+/* One frequency-solve per frequency: SVD of d_H (F x (m x n)), regularised
+ * solution of H x = b.  d_s (F x p) and d_info (F) may be NULL. */
+int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_b,
+                   const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info);
+
+/* The whole IBEM pipeline for F frequencies: assembly, H, SVD, GCV/Tikhonov.
+ * d_p F x (l x nrhs) measured pressures, d_x F x (m x nrhs) surface velocity. */
+int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                        const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
+                        double *d_lambda, double *d_s, int *d_info);
+
+/* The ESM pipeline (plain monopole G, sources given) for F frequencies. */
+int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, const double *d_src, int F,
+                       const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
+                       double *d_lambda, double *d_s, int *d_info);
+
+/* The HELS pipeline (He of order n_sh at field points) for F frequencies. */
+int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, int nrhs,
+                        const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x, double *d_lambda,
+                        double *d_s, int *d_info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IA_H */

@@ -1,0 +1,112 @@
+"""ctypes binding of libia.so (the C ABI declared in include/ia.h).
+
+The shared library is built in-tree by ``inverseacoustics_gb300._build``.
+There is no fallback: if the library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libia.so")
+
+IA_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "allocation failed",
+          4: "Jacobi iteration did not converge", 5: "singular matrix", 6: "non-finite value",
+          7: "invalid quadrature rule", 8: "size above the entry point's limit"}
+IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE = 1, 2, 4
+IA_GCV_STANDARD, IA_GCV_REFERENCE = 0, 1
+IA_PREC_FP64, IA_PREC_MIXED = 0, 1
+IA_METHOD_TIKHONOV_GCV, IA_METHOD_TSVD, IA_METHOD_TIKHONOV_FIXED = 0, 1, 2
+
+
+class IAError(RuntimeError):
+    def __init__(self, code: int, where: str = ""):
+        self.code = code
+        super().__init__(f"{where}: {STATUS.get(code, 'unknown status')} (ia_status {code})")
+
+
+class Config(C.Structure):
+    _fields_ = [("c", C.c_double), ("rho", C.c_double), ("method", C.c_int), ("gcv_mode", C.c_int),
+                ("gcv_points", C.c_int), ("gcv_lo", C.c_double), ("gcv_hi", C.c_double),
+                ("lambda_fixed", C.c_double), ("tsvd_k", C.c_int), ("precision", C.c_int),
+                ("svd_max_sweeps", C.c_int), ("refine_steps", C.c_int)]
+
+
+class Rules(C.Structure):
+    _fields_ = [("nq", C.c_int), ("regular", C.c_void_p), ("nqs", C.c_int), ("singular", C.c_void_p)]
+
+
+_lib = None
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_PP = C.POINTER(C.c_void_p)
+
+_SIGS = {
+    "ia_config_default": (None, [_P]),
+    "ia_config_size": (_I, []),
+    "ia_status_string": (C.c_char_p, [_I]),
+    "ia_version": (C.c_char_p, []),
+    "ia_last_cuda_error": (_I, []),
+    "ia_free": (None, [_P]),
+    "ia_esm": (_I, [_I, _I, _P, _P, _PP, _PP, _D, _D, _P]),
+    "ia_ibem": (_I, [_I, _I, _I, _P, _P, _P, _PP, _PP, _D, _I, _P, _P, _P]),
+    "ia_hels": (_I, [_I, _I, _P, _P, _PP, _PP, _PP, _D, _I, _P]),
+    "ia_csvd": (_I, [_I, _I, _P, _PP, _PP, _PP]),
+    "ia_tsvd": (_I, [_I, _I, _I, _I, _P, _P, _P, _P, _PP]),
+    "ia_to_pressure": (_I, [_I, _I, _P, _P, _PP]),
+    "ia_to_velocity": (_I, [_I, _I, _P, _P, _PP]),
+    "ia_sound_power": (_I, [_I, _P, _P, C.POINTER(C.c_double), _D]),
+    "ia_create": (_I, [_PP, _I, _P]),
+    "ia_destroy": (_I, [_P]),
+    "ia_set_stream": (_I, [_P, _P]),
+    "ia_synchronize": (_I, [_P]),
+    "ia_launch_count": (C.c_longlong, [_P]),
+    "ia_mesh_create": (_I, [_P, _I, _I, _P, _P, _P, _PP]),
+    "ia_mesh_destroy": (_I, [_P]),
+    "ia_monopole_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P]),
+    "ia_ibem_assemble_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_ibem_transfer_batch": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _P]),
+    "ia_hels_batch": (_I, [_P, _I, _P, _I, _I, _P, _P]),
+    "ia_svd_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "ia_regularize_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _I, _P, _P, _P, _P]),
+    "ia_solve_batch": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_ibem_solve_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_esm_solve_batch": (_I, [_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_hels_solve_batch": (_I, [_P, _I, _P, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+}
+
+
+def declared_symbols():
+    return list(_SIGS)
+
+
+def lib():
+    """Load libia.so.  Raises OSError if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"libia.so not built at {LIB_PATH}; run inverseacoustics_gb300._build.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code: int, where: str):
+    if code != IA_OK:
+        raise IAError(code, where)
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    lib().ia_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg

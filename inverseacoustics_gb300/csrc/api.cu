@@ -1,0 +1,824 @@
+// C ABI of libia.so: contexts, workspace, meshes, the reference-compatible
+// host entry points and the batched device pipelines.  See include/ia.h.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <algorithm>
+#include <mutex>
+#include <vector>
+#include "ia_common.cuh"
+#include "ia_internal.h"
+
+static thread_local int g_last_cuda_error = 0;
+
+namespace ia {
+
+int cuda_status(cudaError_t e)
+{
+    g_last_cuda_error = (int)e;
+    if (e == cudaErrorMemoryAllocation) return IA_ERR_ALLOC;
+    return IA_ERR_CUDA;
+}
+
+int ws_reserve(ia_context *ctx, size_t bytes)
+{
+    if (bytes <= ctx->ws_bytes) return IA_OK;
+    if (ctx->ws) {
+        cudaError_t e = cudaFreeAsync(ctx->ws, ctx->stream);
+        ctx->ws = nullptr;
+        ctx->ws_bytes = 0;
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    size_t grow = bytes + bytes / 8;
+    cudaError_t e = cudaMallocAsync(&ctx->ws, grow, ctx->stream);
+    if (e != cudaSuccess) {
+        ctx->ws = nullptr;
+        return cuda_status(e);
+    }
+    ctx->ws_bytes = grow;
+    return IA_OK;
+}
+
+// ---- built-in quadrature rules ------------------------------------------
+// Gauss-Legendre nodes/weights on [0, 1] by Newton iteration on P_n.
+static void gauss_legendre01(int n, std::vector<double> &x, std::vector<double> &w)
+{
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+        double dp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0; }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        x[n - 1 - i] = 0.5 * (1.0 + z);      // ascending
+        w[n - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// Radon's 7-point degree-5 triangle rule (weights scaled to sum 1/2).
+static void radon7(std::vector<double> &rule)
+{
+    const double s15 = sqrt(15.0);
+    const double a1 = (6.0 - s15) / 21.0, b1 = (9.0 + 2.0 * s15) / 21.0, w1 = (155.0 - s15) / 1200.0;
+    const double a2 = (6.0 + s15) / 21.0, b2 = (9.0 - 2.0 * s15) / 21.0, w2 = (155.0 + s15) / 1200.0;
+    const double pts[7][3] = {{1.0 / 3.0, 1.0 / 3.0, 9.0 / 40.0}, {a1, a1, w1}, {b1, a1, w1}, {a1, b1, w1},
+                              {a2, a2, w2}, {b2, a2, w2}, {a2, b2, w2}};
+    rule.assign(21, 0.0);
+    for (int q = 0; q < 7; ++q) {
+        rule[q] = pts[q][0];
+        rule[q + 7] = pts[q][1];
+        rule[q + 14] = 0.5 * pts[q][2];
+    }
+}
+
+// Duffy rule for a singularity at vertex `page` (shape function of that vertex
+// = 1): collapse the unit square onto the triangle at that vertex,
+//   N_page = 1 - u, N_next = u (1 - v), N_prev = u v,  weight w_u w_v u.
+static void duffy_rule(int nu, int nv, std::vector<double> &rule)
+{
+    std::vector<double> xu, wu, xv, wv;
+    gauss_legendre01(nu, xu, wu);
+    gauss_legendre01(nv, xv, wv);
+    const int nq = nu * nv;
+    rule.assign(9 * (size_t)nq, 0.0);
+    for (int page = 0; page < 3; ++page) {
+        double *P = rule.data() + (size_t)3 * nq * page;
+        for (int a = 0; a < nu; ++a)
+            for (int b = 0; b < nv; ++b) {
+                int q = a * nv + b;
+                double u = xu[a], v = xv[b];
+                double N[3];
+                N[page] = 1.0 - u;
+                N[(page + 1) % 3] = u * (1.0 - v);
+                N[(page + 2) % 3] = u * v;
+                P[q] = N[0];
+                P[q + nq] = N[1];
+                P[q + 2 * nq] = wu[a] * wv[b] * u;
+            }
+    }
+}
+
+static int check_rule(int nq, const double *r)
+{
+    if (nq < 1 || !r) return IA_ERR_RULE;
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) {
+        if (!isfinite(r[q]) || !isfinite(r[q + nq]) || !isfinite(r[q + 2 * nq])) return IA_ERR_RULE;
+        s += r[q + 2 * nq];
+    }
+    return fabs(s - 0.5) < 1e-9 ? IA_OK : IA_ERR_RULE;
+}
+
+// ---- default context for the reference-compatible entry points ---------
+static std::mutex g_compat_mu;
+static ia_context *g_compat_ctx[64];
+
+static ia_context *compat_context(int *st)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { *st = cuda_status(e); return nullptr; }
+    if (dev < 0 || dev >= 64) { *st = IA_ERR_ARG; return nullptr; }
+    if (!g_compat_ctx[dev]) {
+        cudaStream_t s;
+        e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { *st = cuda_status(e); return nullptr; }
+        int r = ia_create(&g_compat_ctx[dev], dev, (void *)s);
+        if (r) { *st = r; return nullptr; }
+    }
+    *st = IA_OK;
+    return g_compat_ctx[dev];
+}
+
+template <class T>
+static int to_host_malloc(ia_context *ctx, const T *d, size_t count, T **out)
+{
+    T *h = (T *)malloc(sizeof(T) * (count ? count : 1));
+    if (!h) return IA_ERR_ALLOC;
+    cudaError_t e = cudaMemcpyAsync(h, d, sizeof(T) * count, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { free(h); return cuda_status(e); }
+    *out = h;
+    return IA_OK;
+}
+
+static bool all_finite(const double *p, size_t n)
+{
+    for (size_t i = 0; i < n; ++i)
+        if (!isfinite(p[i])) return false;
+    return true;
+}
+
+}  // namespace ia
+
+using namespace ia;
+
+// =========================================================================
+extern "C" {
+
+void ia_config_default(ia_config *cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->c = 343.0;
+    cfg->rho = 1.21;
+    cfg->method = IA_METHOD_TIKHONOV_GCV;
+    cfg->gcv_mode = IA_GCV_STANDARD;
+    cfg->gcv_points = 200;
+    cfg->gcv_lo = 0.0;
+    cfg->gcv_hi = 0.0;
+    cfg->lambda_fixed = 0.0;
+    cfg->tsvd_k = 1;
+    cfg->precision = IA_PREC_FP64;
+    cfg->svd_max_sweeps = 40;
+    cfg->refine_steps = 2;
+}
+
+const char *ia_status_string(int status)
+{
+    switch (status) {
+    case IA_OK: return "ok";
+    case IA_ERR_ARG: return "invalid argument";
+    case IA_ERR_CUDA: return "CUDA runtime error";
+    case IA_ERR_ALLOC: return "allocation failed";
+    case IA_ERR_NOCONV: return "Jacobi iteration did not converge";
+    case IA_ERR_SINGULAR: return "singular matrix";
+    case IA_ERR_NONFINITE: return "non-finite value";
+    case IA_ERR_RULE: return "invalid quadrature rule";
+    case IA_ERR_TOO_LARGE: return "size above the entry point's limit";
+    default: return "unknown status";
+    }
+}
+
+const char *ia_version(void) { return "ia-gb300 0.1 (sm_103a)"; }
+int ia_config_size(void) { return (int)sizeof(ia_config); }
+int ia_last_cuda_error(void) { return g_last_cuda_error; }
+void ia_free(void *p) { free(p); }
+
+int ia_create(ia_context **out, int device, void *stream)
+{
+    if (!out) return IA_ERR_ARG;
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_status(e);
+    ia_context *c = (ia_context *)calloc(1, sizeof(ia_context));
+    if (!c) return IA_ERR_ALLOC;
+    c->device = device;
+    c->stream = (cudaStream_t)stream;
+    int sm = 0;
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+    c->sm_count = sm;
+    *out = c;
+    return IA_OK;
+}
+
+int ia_destroy(ia_context *ctx)
+{
+    if (!ctx) return IA_OK;
+    if (ctx->ws) {
+        cudaFreeAsync(ctx->ws, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    free(ctx);
+    return IA_OK;
+}
+
+int ia_set_stream(ia_context *ctx, void *stream)
+{
+    if (!ctx) return IA_ERR_ARG;
+    if (ctx->ws) {
+        // the workspace was allocated on the old stream: release it there
+        cudaFreeAsync(ctx->ws, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        ctx->ws = nullptr;
+        ctx->ws_bytes = 0;
+    }
+    ctx->stream = (cudaStream_t)stream;
+    return IA_OK;
+}
+
+int ia_synchronize(ia_context *ctx)
+{
+    if (!ctx) return IA_ERR_ARG;
+    IA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return IA_OK;
+}
+
+long long ia_launch_count(const ia_context *ctx) { return ctx ? ctx->launches : 0; }
+
+// ---- mesh -----------------------------------------------------------------
+int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int *elems, const ia_rules *rules,
+                   ia_mesh **out)
+{
+    if (!ctx || !out || !nodes || !elems || m < 3 || n < 1) return IA_ERR_ARG;
+    *out = nullptr;
+    if (!all_finite(nodes, (size_t)3 * m)) return IA_ERR_NONFINITE;
+    for (int i = 0; i < n; ++i) {
+        int a = elems[i], b = elems[i + n], c = elems[i + 2 * n];
+        if (a < 0 || b < 0 || c < 0 || a >= m || b >= m || c >= m) return IA_ERR_ARG;
+        if (a == b || b == c || a == c) return IA_ERR_ARG;
+    }
+    std::vector<double> reg, sing;
+    int nq, nqs;
+    if (rules) {
+        nq = rules->nq;
+        nqs = rules->nqs;
+        if (check_rule(nq, rules->regular)) return IA_ERR_RULE;
+        for (int p = 0; p < 3; ++p)
+            if (!rules->singular || check_rule(nqs, rules->singular + (size_t)3 * nqs * p)) return IA_ERR_RULE;
+        reg.assign(rules->regular, rules->regular + 3 * (size_t)nq);
+        sing.assign(rules->singular, rules->singular + 9 * (size_t)nqs);
+    } else {
+        radon7(reg);
+        nq = 7;
+        duffy_rule(4, 4, sing);
+        nqs = 16;
+    }
+    // node -> elements
+    std::vector<std::vector<int>> node_elems(m);
+    for (int i = 0; i < n; ++i)
+        for (int s = 0; s < 3; ++s) node_elems[elems[i + s * n]].push_back(i);
+    // greedy colouring: no two elements of one colour share a vertex
+    std::vector<int> color(n, -1);
+    int ncolors = 0;
+    std::vector<char> used;
+    for (int i = 0; i < n; ++i) {
+        used.assign(ncolors + 1, 0);
+        for (int s = 0; s < 3; ++s)
+            for (int o : node_elems[elems[i + s * n]])
+                if (color[o] >= 0) used[color[o]] = 1;
+        int c = 0;
+        while (c < ncolors && used[c]) ++c;
+        color[i] = c;
+        if (c == ncolors) ++ncolors;
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return color[a] < color[b]; });
+    std::vector<int> newidx(n);
+    for (int t = 0; t < n; ++t) newidx[order[t]] = t;
+    std::vector<int> cptr(ncolors + 1, 0);
+    for (int i = 0; i < n; ++i) cptr[color[i] + 1]++;
+    for (int c = 0; c < ncolors; ++c) cptr[c + 1] += cptr[c];
+    std::vector<double> egeo((size_t)16 * n, 0.0);
+    std::vector<int> evert((size_t)4 * n, 0);
+    for (int t = 0; t < n; ++t) {
+        int i = order[t];
+        double v[3][3];
+        for (int s = 0; s < 3; ++s) {
+            int node = elems[i + s * n];
+            evert[4 * t + s] = node;
+            for (int d = 0; d < 3; ++d) v[s][d] = nodes[node + d * m];
+        }
+        evert[4 * t + 3] = color[i];
+        double a0 = v[0][0] - v[2][0], a1 = v[0][1] - v[2][1], a2 = v[0][2] - v[2][2];
+        double b0 = v[1][0] - v[2][0], b1 = v[1][1] - v[2][1], b2 = v[1][2] - v[2][2];
+        double nx = a1 * b2 - a2 * b1, ny = a2 * b0 - a0 * b2, nz = a0 * b1 - a1 * b0;
+        double *g = &egeo[(size_t)16 * t];
+        for (int s = 0; s < 3; ++s)
+            for (int d = 0; d < 3; ++d) g[3 * s + d] = v[s][d];
+        g[9] = nx;
+        g[10] = ny;
+        g[11] = nz;
+        g[12] = sqrt(nx * nx + ny * ny + nz * nz);
+    }
+    std::vector<int> aptr(m + 1, 0), adj;
+    adj.reserve((size_t)3 * n);
+    for (int o = 0; o < m; ++o) {
+        std::vector<int> inc;
+        for (int i : node_elems[o]) {
+            int slot = elems[i] == o ? 0 : (elems[i + n] == o ? 1 : 2);
+            inc.push_back(newidx[i] * 4 + slot);
+        }
+        std::sort(inc.begin(), inc.end());
+        for (int v : inc) adj.push_back(v);
+        aptr[o + 1] = (int)adj.size();
+    }
+    ia_mesh *M = (ia_mesh *)calloc(1, sizeof(ia_mesh));
+    if (!M) return IA_ERR_ALLOC;
+    M->ctx = ctx;
+    M->m = m;
+    M->n = n;
+    M->ncolors = ncolors;
+    M->nq = nq;
+    M->nqs = nqs;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void **dst, const void *src, size_t bytes) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(dst, bytes ? bytes : 16);
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up((void **)&M->d_nodes, nodes, sizeof(double) * 3 * (size_t)m);
+    up((void **)&M->d_egeo, egeo.data(), sizeof(double) * egeo.size());
+    up((void **)&M->d_evert, evert.data(), sizeof(int) * evert.size());
+    up((void **)&M->d_color_ptr, cptr.data(), sizeof(int) * cptr.size());
+    up((void **)&M->d_adj_ptr, aptr.data(), sizeof(int) * aptr.size());
+    up((void **)&M->d_adj, adj.data(), sizeof(int) * adj.size());
+    up((void **)&M->d_reg, reg.data(), sizeof(double) * reg.size());
+    up((void **)&M->d_sing, sing.data(), sizeof(double) * sing.size());
+    if (e != cudaSuccess) {
+        ia_mesh_destroy(M);
+        return cuda_status(e);
+    }
+    *out = M;
+    return IA_OK;
+}
+
+int ia_mesh_destroy(ia_mesh *M)
+{
+    if (!M) return IA_OK;
+    cudaFree(M->d_nodes);
+    cudaFree(M->d_egeo);
+    cudaFree(M->d_evert);
+    cudaFree(M->d_color_ptr);
+    cudaFree(M->d_adj_ptr);
+    cudaFree(M->d_adj);
+    cudaFree(M->d_reg);
+    cudaFree(M->d_sing);
+    free(M);
+    return IA_OK;
+}
+
+// ---- batched device entry points ------------------------------------------
+static int check_info(ia_context *ctx, const int *d_info, int F)
+{
+    (void)ctx; (void)d_info; (void)F;
+    return IA_OK;
+}
+
+int ia_monopole_batch(ia_context *ctx, int l, int m, int F, const double *d_mics, const double *d_src,
+                      const double *d_k, ia_complex *d_G)
+{
+    if (!ctx || l < 1 || m < 1 || F < 1 || !d_mics || !d_src || !d_k || !d_G) return IA_ERR_ARG;
+    return monopole_batched(ctx, l, m, F, d_mics, d_src, d_k, (double2 *)d_G);
+}
+
+int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                           const double *d_cp, int F, const double *d_k, const ia_config *cfg, ia_complex *d_At,
+                           ia_complex *d_Bt, ia_complex *d_Ahs_t, ia_complex *d_Bhs_t)
+{
+    if (!ctx || !mesh || !cfg || F < 1 || l < 0 || n_ch < 0 || !d_k) return IA_ERR_ARG;
+    if ((l > 0 && !d_mics) || (n_ch > 0 && !d_cp)) return IA_ERR_ARG;
+    return ibem_rows(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, cfg->c, cfg->rho, (double2 *)d_At, (double2 *)d_Bt,
+                     (double2 *)d_Ahs_t, (double2 *)d_Bhs_t);
+}
+
+// H^T (m x l per frequency) into Ht, given workspace for A^T, B^T, pivots.
+static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                           const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
+                           double2 *Ahs_t, double2 *Ht, int *d_info)
+{
+    const int m = mesh->m;
+    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
+    if (st) return st;
+    const long long sMM = (long long)m * m, sML = (long long)m * l;
+    // LU of M = A^T; solve M Y = A_hs^T  ->  Y = W^T, W = A_hs A^-1
+    st = zgetrf_batched(ctx, m, At, m, sMM, ipiv, d_info, F);
+    if (st) return st;
+    st = zgetrs_batched(ctx, m, l, At, m, sMM, ipiv, Ahs_t, m, sML, F);
+    if (st) return st;
+    // H^T = B^T Y - B_hs^T  (in place over B_hs^T)
+    return zgemm_batched(ctx, OP_N, OP_N, m, l, m, make_double2(1.0, 0.0), Bt, m, sMM, Ahs_t, m, sML,
+                         make_double2(-1.0, 0.0), Ht, m, sML, F);
+}
+
+int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                           const double *d_k, const ia_config *cfg, ia_complex *d_H, int *d_info)
+{
+    if (!ctx || !mesh || !cfg || F < 1 || l < 1 || !d_mics || !d_k || !d_H || !d_info) return IA_ERR_ARG;
+    const int m = mesh->m;
+    size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2;
+    int st = ws_reserve(ctx, need);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    double2 *At = cur.take<double2>((size_t)m * m * F);
+    double2 *Bt = cur.take<double2>((size_t)m * m * F);
+    int *ipiv = cur.take<int>((size_t)m * F);
+    double2 *Ahs = cur.take<double2>((size_t)m * l * F);
+    double2 *Ht = cur.take<double2>((size_t)m * l * F);
+    st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
+    if (st) return st;
+    return ztranspose_batched(ctx, m, l, Ht, m, (long long)m * l, (double2 *)d_H, l, (long long)m * l, false, F);
+}
+
+int ia_hels_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, ia_complex *d_H)
+{
+    if (!ctx || l < 1 || !d_pts || n_sh < 0 || F < 1 || !d_k || !d_H) return IA_ERR_ARG;
+    return hels_batched(ctx, l, d_pts, n_sh, F, d_k, 343.0, 1.21, (double2 *)d_H, nullptr);
+}
+
+int ia_svd_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_A, ia_complex *d_U, double *d_s,
+                 ia_complex *d_V, int *d_info)
+{
+    if (!ctx || m < 1 || n < 1 || F < 1 || !d_A || !d_s || !d_info) return IA_ERR_ARG;
+    int st = ws_reserve(ctx, svd_workspace_bytes(m, n, F));
+    if (st) return st;
+    const int M = m >= n ? m : n, N = m >= n ? n : m;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    double2 *Y = cur.take<double2>((size_t)M * N * F);
+    double2 *Vacc = cur.take<double2>((size_t)N * N * F);
+    return svd_batched(ctx, m, n, (const double2 *)d_A, false, (double2 *)d_U, d_s, (double2 *)d_V, F, 40, d_info,
+                       Y, Vacc);
+}
+
+int ia_regularize_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_U, const double *d_s,
+                        const ia_complex *d_V, int nrhs, const ia_complex *d_b, const ia_config *cfg,
+                        ia_complex *d_x, double *d_lambda)
+{
+    if (!ctx || !cfg || m < 1 || n < 1 || F < 1 || nrhs < 1 || !d_U || !d_s || !d_V || !d_b || !d_x) return IA_ERR_ARG;
+    const int p = m < n ? m : n;
+    return regularize_batched(ctx, m, n, p, F, (const double2 *)d_U, d_s, (const double2 *)d_V, nrhs,
+                              (const double2 *)d_b, cfg, (double2 *)d_x, d_lambda);
+}
+
+// SVD + regularisation on an operator given as A (m x n) or its transpose.
+static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bool transposed, int nrhs,
+                      const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
+                      WsCursor &cur)
+{
+    const int p = m < n ? m : n;
+    const int M = m >= n ? m : n;
+    double2 *Y = cur.take<double2>((size_t)M * p * F);
+    double2 *Vacc = cur.take<double2>((size_t)p * p * F);
+    double2 *U = cur.take<double2>((size_t)m * p * F);
+    double2 *V = cur.take<double2>((size_t)n * p * F);
+    double *s = s_out ? s_out : cur.take<double>((size_t)p * F);
+    int st = svd_batched(ctx, m, n, A, transposed, U, s, V, F, cfg->svd_max_sweeps, info, Y, Vacc);
+    if (st) return st;
+    return regularize_batched(ctx, m, n, p, F, U, s, V, nrhs, b, cfg, x, lambda);
+}
+
+static size_t solve_ws_bytes(int m, int n, int F)
+{
+    const int p = m < n ? m : n;
+    const int M = m >= n ? m : n;
+    return ws_round(sizeof(double2) * (size_t)M * p * F) + ws_round(sizeof(double2) * (size_t)p * p * F) +
+           ws_round(sizeof(double2) * (size_t)m * p * F) + ws_round(sizeof(double2) * (size_t)n * p * F) +
+           ws_round(sizeof(double) * (size_t)p * F) + 1024;
+}
+
+int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_b,
+                   const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info)
+{
+    if (!ctx || !cfg || m < 1 || n < 1 || F < 1 || nrhs < 1 || !d_H || !d_b || !d_x || !d_info) return IA_ERR_ARG;
+    int st = ws_reserve(ctx, solve_ws_bytes(m, n, F));
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return solve_core(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg, (double2 *)d_x,
+                      d_lambda, d_s, d_info, cur);
+}
+
+int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                        const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
+                        double *d_lambda, double *d_s, int *d_info)
+{
+    if (!ctx || !mesh || !cfg || l < 1 || F < 1 || nrhs < 1 || !d_mics || !d_k || !d_p || !d_x || !d_info)
+        return IA_ERR_ARG;
+    const int m = mesh->m;
+    size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F);
+    int st = ws_reserve(ctx, need);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    double2 *At = cur.take<double2>((size_t)m * m * F);
+    double2 *Bt = cur.take<double2>((size_t)m * m * F);
+    int *ipiv = cur.take<int>((size_t)m * F);
+    double2 *Ahs = cur.take<double2>((size_t)m * l * F);
+    double2 *Ht = cur.take<double2>((size_t)m * l * F);
+    st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
+    if (st) return st;
+    return solve_core(ctx, l, m, F, Ht, true, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
+                      cur);
+}
+
+int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, const double *d_src, int F,
+                       const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
+                       double *d_lambda, double *d_s, int *d_info)
+{
+    if (!ctx || !cfg || l < 1 || m < 1 || F < 1 || nrhs < 1 || !d_mics || !d_src || !d_k || !d_p || !d_x || !d_info)
+        return IA_ERR_ARG;
+    size_t need = ws_round(sizeof(double2) * (size_t)l * m * F) + solve_ws_bytes(l, m, F);
+    int st = ws_reserve(ctx, need);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    double2 *G = cur.take<double2>((size_t)l * m * F);
+    st = monopole_batched(ctx, l, m, F, d_mics, d_src, d_k, G);
+    if (st) return st;
+    return solve_core(ctx, l, m, F, G, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
+                      cur);
+}
+
+int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, int nrhs,
+                        const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x, double *d_lambda,
+                        double *d_s, int *d_info)
+{
+    if (!ctx || !cfg || l < 1 || n_sh < 0 || F < 1 || nrhs < 1 || !d_pts || !d_k || !d_p || !d_x || !d_info)
+        return IA_ERR_ARG;
+    const int nt = (n_sh + 1) * (n_sh + 1);
+    size_t need = ws_round(sizeof(double2) * (size_t)l * nt * F) + solve_ws_bytes(l, nt, F);
+    int st = ws_reserve(ctx, need);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    double2 *H = cur.take<double2>((size_t)l * nt * F);
+    st = hels_batched(ctx, l, d_pts, n_sh, F, d_k, cfg->c, cfg->rho, H, nullptr);
+    if (st) return st;
+    return solve_core(ctx, l, nt, F, H, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
+                      cur);
+}
+
+}  // extern "C"
+
+// ---- reference-compatible host entry points -------------------------------
+// Device scratch for one compat call: a single cudaMallocAsync block on the
+// compat context's stream, released at the end of the call.
+struct CompatScratch {
+    ia_context *ctx;
+    char *base = nullptr;
+    size_t off = 0, cap = 0;
+    int alloc(size_t bytes)
+    {
+        cap = bytes;
+        cudaError_t e = cudaMallocAsync((void **)&base, bytes, ctx->stream);
+        return e == cudaSuccess ? IA_OK : cuda_status(e);
+    }
+    template <class T>
+    T *take(size_t count)
+    {
+        size_t a = (off + 255) & ~size_t(255);
+        off = a + count * sizeof(T);
+        return reinterpret_cast<T *>(base + a);
+    }
+    ~CompatScratch()
+    {
+        if (base) {
+            cudaFreeAsync(base, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        }
+    }
+};
+
+#define IA_TRY(x)                \
+    do {                         \
+        int r__ = (x);           \
+        if (r__) return r__;     \
+    } while (0)
+#define IA_CTRY(x) IA_CUDA_TRY(x)
+
+extern "C" {
+
+int ia_esm(int m, int l, const double *r_ms, const double *r_lh, ia_complex **m_e, ia_complex **h, double k,
+           double r_i, const ia_config *cfg)
+{
+    if (m < 1 || l < 1 || !r_ms || !r_lh || !m_e || !h || !(k > 0.0)) return IA_ERR_ARG;
+    if (!all_finite(r_ms, 3 * (size_t)m) || !all_finite(r_lh, 3 * (size_t)l) || !isfinite(r_i)) return IA_ERR_NONFINITE;
+    ia_config dc;
+    if (!cfg) { ia_config_default(&dc); cfg = &dc; }
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    CompatScratch sc{ctx};
+    size_t need = ws_round(24 * (size_t)(m + l)) + ws_round(16 * (size_t)m * m) + ws_round(16 * (size_t)m * (m + l)) +
+                  ws_round(16 * (size_t)m * (m + l)) + ws_round(4 * (size_t)m) + ws_round(4) + 4096;
+    IA_TRY(sc.alloc(need));
+    double *dr = sc.take<double>(3 * (size_t)m);
+    double *dl = sc.take<double>(3 * (size_t)l);
+    double2 *DT = sc.take<double2>((size_t)m * m);
+    double2 *RHS = sc.take<double2>((size_t)m * (m + l));
+    double2 *OUT = sc.take<double2>((size_t)m * (m + l));
+    int *ipiv = sc.take<int>(m);
+    int *info = sc.take<int>(1);
+    IA_CTRY(cudaMemcpyAsync(dr, r_ms, 24 * (size_t)m, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(dl, r_lh, 24 * (size_t)l, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemsetAsync(info, 0, 4, ctx->stream));
+    IA_TRY(esm_system(ctx, m, l, dr, dl, r_i, k, cfg->c, cfg->rho, DT, RHS));
+    IA_TRY(zgetrf_batched(ctx, m, DT, m, 0, ipiv, info, 1));
+    IA_TRY(zgetrs_batched(ctx, m, m + l, DT, m, 0, ipiv, RHS, m, 0, 1));
+    // Me = X[:, :m]^T, He = X[:, m:]^T
+    IA_TRY(ztranspose_batched(ctx, m, m, RHS, m, 0, OUT, m, 0, false, 1));
+    IA_TRY(ztranspose_batched(ctx, m, l, RHS + (size_t)m * m, m, 0, OUT + (size_t)m * m, l, 0, false, 1));
+    int hinfo = 0;
+    IA_CTRY(cudaMemcpyAsync(&hinfo, info, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ia_complex *me = nullptr, *he = nullptr;
+    IA_TRY(to_host_malloc(ctx, (const ia_complex *)OUT, (size_t)m * m, &me));
+    int r = to_host_malloc(ctx, (const ia_complex *)(OUT + (size_t)m * m), (size_t)l * m, &he);
+    if (r) { free(me); return r; }
+    *m_e = me;
+    *h = he;
+    if (hinfo & IA_INFO_NONFINITE) return IA_ERR_NONFINITE;
+    if (hinfo & IA_INFO_SINGULAR) return IA_ERR_SINGULAR;
+    return IA_OK;
+}
+
+int ia_hels(int m, int l, const double *r_ms_s, const double *r_lh_s, ia_complex **m_e, ia_complex **h,
+            ia_complex **q_e, double k, int n_sh, const ia_config *cfg)
+{
+    if (m < 1 || l < 1 || !r_ms_s || !r_lh_s || !m_e || !h || !q_e || !(k > 0.0) || n_sh < 0) return IA_ERR_ARG;
+    if (!all_finite(r_ms_s, 3 * (size_t)m) || !all_finite(r_lh_s, 3 * (size_t)l)) return IA_ERR_NONFINITE;
+    ia_config dc;
+    if (!cfg) { ia_config_default(&dc); cfg = &dc; }
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    const int nt = (n_sh + 1) * (n_sh + 1);
+    CompatScratch sc{ctx};
+    IA_TRY(sc.alloc(ws_round(24 * (size_t)(m + l)) + ws_round(8) + 3 * ws_round(16 * (size_t)nt * (m > l ? m : l)) +
+                    4096));
+    double *dr = sc.take<double>(3 * (size_t)m);
+    double *dl = sc.take<double>(3 * (size_t)l);
+    double *dk = sc.take<double>(1);
+    double2 *Me = sc.take<double2>((size_t)m * nt);
+    double2 *Qe = sc.take<double2>((size_t)m * nt);
+    double2 *He = sc.take<double2>((size_t)l * nt);
+    IA_CTRY(cudaMemcpyAsync(dr, r_ms_s, 24 * (size_t)m, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(dl, r_lh_s, 24 * (size_t)l, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(dk, &k, 8, cudaMemcpyHostToDevice, ctx->stream));
+    IA_TRY(hels_batched(ctx, m, dr, n_sh, 1, dk, cfg->c, cfg->rho, Me, Qe));
+    IA_TRY(hels_batched(ctx, l, dl, n_sh, 1, dk, cfg->c, cfg->rho, He, nullptr));
+    ia_complex *a = nullptr, *b = nullptr, *c = nullptr;
+    IA_TRY(to_host_malloc(ctx, (const ia_complex *)Me, (size_t)m * nt, &a));
+    int r = to_host_malloc(ctx, (const ia_complex *)He, (size_t)l * nt, &b);
+    if (!r) r = to_host_malloc(ctx, (const ia_complex *)Qe, (size_t)m * nt, &c);
+    if (r) { free(a); free(b); return r; }
+    *m_e = a;
+    *h = b;
+    *q_e = c;
+    return IA_OK;
+}
+
+int ia_csvd(int m, int n, const ia_complex *a, ia_complex **u, double **s, ia_complex **v)
+{
+    if (m < 1 || n < 1 || !a || !u || !s || !v) return IA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    const int p = m < n ? m : n, M = m > n ? m : n;
+    CompatScratch sc{ctx};
+    IA_TRY(sc.alloc(ws_round(16 * (size_t)m * n) + ws_round(16 * (size_t)M * p) + ws_round(16 * (size_t)p * p) +
+                    ws_round(16 * (size_t)m * p) + ws_round(16 * (size_t)n * p) + ws_round(8 * (size_t)p) + 4096));
+    double2 *A = sc.take<double2>((size_t)m * n);
+    double2 *Y = sc.take<double2>((size_t)M * p);
+    double2 *Vacc = sc.take<double2>((size_t)p * p);
+    double2 *U = sc.take<double2>((size_t)m * p);
+    double2 *V = sc.take<double2>((size_t)n * p);
+    double *S = sc.take<double>(p);
+    int *info = sc.take<int>(1);
+    IA_CTRY(cudaMemcpyAsync(A, a, 16 * (size_t)m * n, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemsetAsync(info, 0, 4, ctx->stream));
+    IA_TRY(svd_batched(ctx, m, n, A, false, U, S, V, 1, 60, info, Y, Vacc));
+    int hinfo = 0;
+    IA_CTRY(cudaMemcpyAsync(&hinfo, info, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ia_complex *hu = nullptr, *hv = nullptr;
+    double *hs = nullptr;
+    IA_TRY(to_host_malloc(ctx, (const ia_complex *)U, (size_t)m * p, &hu));
+    int r = to_host_malloc(ctx, (const ia_complex *)V, (size_t)n * p, &hv);
+    if (!r) r = to_host_malloc(ctx, S, (size_t)p, &hs);
+    if (r) { free(hu); free(hv); return r; }
+    *u = hu;
+    *v = hv;
+    *s = hs;
+    if (hinfo & IA_INFO_NONFINITE) return IA_ERR_NONFINITE;
+    if (hinfo & IA_INFO_NOCONV) return IA_ERR_NOCONV;
+    return IA_OK;
+}
+
+int ia_tsvd(int m, int n, int p, int k, const ia_complex *u, const double *s, const ia_complex *v,
+            const ia_complex *b, ia_complex **x)
+{
+    if (m < 1 || n < 1 || p < 1 || !u || !s || !v || !b || !x) return IA_ERR_ARG;
+    if (k < 1 || k > p) return IA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    CompatScratch sc{ctx};
+    IA_TRY(sc.alloc(ws_round(16 * (size_t)m * p) + ws_round(8 * (size_t)p) + ws_round(16 * (size_t)n * p) +
+                    ws_round(16 * (size_t)m) + ws_round(16 * (size_t)n) + 4096));
+    double2 *U = sc.take<double2>((size_t)m * p);
+    double *S = sc.take<double>(p);
+    double2 *V = sc.take<double2>((size_t)n * p);
+    double2 *B = sc.take<double2>(m);
+    double2 *X = sc.take<double2>(n);
+    IA_CTRY(cudaMemcpyAsync(U, u, 16 * (size_t)m * p, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(S, s, 8 * (size_t)p, cudaMemcpyHostToDevice, ctx->stream));
+    // the reference copies only the first k columns of V (CUDA/tsvd.cuh:143-144)
+    IA_CTRY(cudaMemsetAsync(V, 0, 16 * (size_t)n * p, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(V, v, 16 * (size_t)n * k, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(B, b, 16 * (size_t)m, cudaMemcpyHostToDevice, ctx->stream));
+    ia_config cfg;
+    ia_config_default(&cfg);
+    cfg.method = IA_METHOD_TSVD;
+    cfg.tsvd_k = k;
+    IA_TRY(regularize_batched(ctx, m, n, p, 1, U, S, V, 1, B, &cfg, X, nullptr));
+    return to_host_malloc(ctx, (const ia_complex *)X, (size_t)n, x);
+}
+
+static int matvec_compat(int m, int n, const ia_complex *a, const ia_complex *x, ia_complex **y)
+{
+    if (m < 1 || n < 1 || !a || !x || !y) return IA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    CompatScratch sc{ctx};
+    IA_TRY(sc.alloc(ws_round(16 * (size_t)m * n) + ws_round(16 * (size_t)n) + ws_round(16 * (size_t)m) + 1024));
+    double2 *A = sc.take<double2>((size_t)m * n);
+    double2 *X = sc.take<double2>(n);
+    double2 *Y = sc.take<double2>(m);
+    IA_CTRY(cudaMemcpyAsync(A, a, 16 * (size_t)m * n, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(X, x, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    IA_TRY(zgemm_batched(ctx, OP_N, OP_N, m, 1, n, make_double2(1.0, 0.0), A, m, 0, X, n, 0, make_double2(0.0, 0.0), Y,
+                         m, 0, 1));
+    return to_host_malloc(ctx, (const ia_complex *)Y, (size_t)m, y);
+}
+
+int ia_to_pressure(int m, int n, const ia_complex *me, const ia_complex *x, ia_complex **p)
+{
+    return matvec_compat(m, n, me, x, p);
+}
+
+int ia_to_velocity(int m, int n, const ia_complex *qe, const ia_complex *x, ia_complex **v)
+{
+    return matvec_compat(m, n, qe, x, v);
+}
+
+int ia_sound_power(int m, const ia_complex *p, const ia_complex *v, double *w, double s)
+{
+    if (m < 1 || !p || !v || !w) return IA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    int st;
+    ia_context *ctx = compat_context(&st);
+    if (!ctx) return st;
+    CompatScratch sc{ctx};
+    IA_TRY(sc.alloc(ws_round(16 * (size_t)m) * 2 + ws_round(16) + 1024));
+    double2 *P = sc.take<double2>(m);
+    double2 *Vv = sc.take<double2>(m);
+    double2 *D = sc.take<double2>(1);
+    IA_CTRY(cudaMemcpyAsync(P, p, 16 * (size_t)m, cudaMemcpyHostToDevice, ctx->stream));
+    IA_CTRY(cudaMemcpyAsync(Vv, v, 16 * (size_t)m, cudaMemcpyHostToDevice, ctx->stream));
+    // v^H p as a 1 x 1 product
+    IA_TRY(zgemm_batched(ctx, OP_C, OP_N, 1, 1, m, make_double2(1.0, 0.0), Vv, m, 0, P, m, 0, make_double2(0.0, 0.0), D,
+                         1, 0, 1));
+    double2 hd;
+    IA_CTRY(cudaMemcpyAsync(&hd, D, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    IA_CTRY(cudaStreamSynchronize(ctx->stream));
+    *w = 0.5 * hd.x * (s / m);
+    return IA_OK;
+}
+
+}  // extern "C"

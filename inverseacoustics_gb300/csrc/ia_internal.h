@@ -1,0 +1,111 @@
+// Internal declarations shared by the libia.so translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "../../include/ia.h"
+
+struct ia_context {
+    int device;
+    cudaStream_t stream;
+    void *ws;              // stream-ordered workspace (grow-only)
+    size_t ws_bytes;
+    long long launches;    // kernels launched through this context
+    int sm_count;
+};
+
+struct ia_mesh {
+    ia_context *ctx;
+    int m, n;              // nodes, triangles
+    int ncolors;
+    int nq, nqs;           // regular / singular rule sizes
+    double *d_nodes;       // 3 x m SoA
+    double *d_egeo;        // n x 16 per element (colour order): v0 v1 v2 (9), normal (3), |n|, pad
+    int *d_evert;          // n x 4 per element (colour order): 3 vertex indices, pad
+    int *d_color_ptr;      // ncolors + 1
+    int *d_adj_ptr;        // m + 1: incident (element, slot) list per node
+    int *d_adj;            // 3n: element index (colour order) * 4 + slot
+    double *d_reg;         // 3 x nq
+    double *d_sing;        // 9 x nqs
+};
+
+namespace ia {
+
+// ---- error plumbing
+int cuda_status(cudaError_t e);
+#define IA_CUDA_TRY(expr)                                  \
+    do {                                                   \
+        cudaError_t e__ = (expr);                          \
+        if (e__ != cudaSuccess) return ia::cuda_status(e__); \
+    } while (0)
+#define IA_LAUNCH_CHECK(ctx)                               \
+    do {                                                   \
+        (ctx)->launches++;                                 \
+        cudaError_t e__ = cudaGetLastError();              \
+        if (e__ != cudaSuccess) return ia::cuda_status(e__); \
+    } while (0)
+
+// workspace carving: returns IA_OK / IA_ERR_ALLOC
+int ws_reserve(ia_context *ctx, size_t bytes);
+struct WsCursor {
+    char *base;
+    size_t off, cap;
+    template <class T>
+    T *take(size_t count)
+    {
+        size_t a = (off + 255) & ~size_t(255);
+        off = a + count * sizeof(T);
+        return reinterpret_cast<T *>(base + a);
+    }
+};
+inline size_t ws_round(size_t b) { return (b + 255) & ~size_t(255); }
+
+// ---- dense kernels (dense.cu)
+enum Op { OP_N = 0, OP_T = 1, OP_C = 2 };
+int zgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
+                  long long sA, const double2 *B, int ldb, long long sB, double2 beta, double2 *C, int ldc,
+                  long long sC, int batch);
+int zgetrf_batched(ia_context *ctx, int n, double2 *A, int lda, long long sA, int *ipiv, int *info, int batch);
+int zgetrs_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, const int *ipiv,
+                   double2 *B, int ldb, long long sB, int batch);
+// X = U^-1 X for the upper triangle of LU (n x n), X n x nrhs
+int zbacksolve_upper_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, double2 *B,
+                             int ldb, long long sB, int batch);
+// Householder QR of A (rows x cols, rows >= cols) applied to [A | B] in place:
+// on exit the upper triangle of A is R and B holds Q^H B.
+int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
+                   int ldb, long long sB, int batch);
+// out[f] (cols x rows) = op(in[f]) (rows x cols), op in {T, C}; or copy/conj when transpose=false
+int ztranspose_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
+                       int ldo, long long so, bool conj, int batch);
+int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
+                    int ldo, long long so, bool conj, int batch);
+
+// ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
+int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);
+// sigma, normalised sorted outputs: Uy (M x N) <- Y/sigma, Vs (N x N) <- V, both column-permuted to
+// descending sigma.  Either output may be null.
+int svd_finalize_batched(ia_context *ctx, int M, int N, const double2 *Y, const double2 *V, double *s,
+                         double2 *Uy, double2 *Vs, int batch, int *info);
+// full batched compact SVD of A (m x n) -> U (m x p), s, V (n x p); transposed_input: A given as A^T (n x m).
+// Y (max(m,n) x p per matrix) and Vacc (p x p per matrix) are caller-provided workspace.
+int svd_batched(ia_context *ctx, int m, int n, const double2 *A, bool transposed_input, double2 *U, double *s,
+                double2 *V, int batch, int max_sweeps, int *info, double2 *Y, double2 *Vacc);
+size_t svd_workspace_bytes(int m, int n, int batch);
+
+// ---- regularisation (regularize.cu)
+int regularize_batched(ia_context *ctx, int m, int n, int p, int batch, const double2 *U, const double *s,
+                       const double2 *V, int nrhs, const double2 *b, const ia_config *cfg, double2 *x,
+                       double *lambda);
+
+// ---- assembly (assemble.cu)
+int monopole_batched(ia_context *ctx, int l, int m, int F, const double *mics, const double *src, const double *k,
+                     double2 *G);
+int esm_system(ia_context *ctx, int m, int l, const double *src, const double *mics, double r_i, double k, double c,
+               double rho, double2 *DT, double2 *RHS);
+int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
+              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t);
+int hels_batched(ia_context *ctx, int npts, const double *pts, int order, int F, const double *k, double c,
+                 double rho, double2 *Me, double2 *Qe);
+
+}  // namespace ia

@@ -1,0 +1,464 @@
+"""FP64 CPU restatement of the reference's inverse pipeline (the oracle).
+
+ORACLE / TEST INFRASTRUCTURE ONLY.  Imported by tests/, by
+__graft_entry__.smoke() as the checker, and by bench.py's CPU-baseline and
+reference legs.  The product path (inverseacoustics_gb300) never imports it.
+
+Each function cites the reference code it restates.  Parity pins:
+  * esm / ibem against the reference's own compiled CPU code
+    (oracle/_ref/libiaref.so), frozen as golden fixtures in tests/golden/
+    by tests/golden/make_golden.py;
+  * hels against scipy's spherical Bessel and Legendre functions (the
+    reference's CPU hels() needs GSL, which is absent);
+  * gcv / tikhonov / tsvd / csvd restate MATLAB/regtools/*G.m (MATLAB is
+    absent); sinc-R has no reference code and is unpinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+C_LIB_PATH = os.path.join(HERE, "_build", "libiaoracle.so")
+INV4PI = 1.0 / (4.0 * math.pi)
+EPS = np.finfo(np.float64).eps
+
+_clib = None
+
+
+def clib():
+    """The C restatement (oracle/ibem_oracle.c), built by oracle/build.py."""
+    global _clib
+    if _clib is None:
+        if not os.path.exists(C_LIB_PATH):
+            from oracle import build as _b
+            _b.build_oracle()
+        _clib = C.CDLL(C_LIB_PATH)
+        P = C.c_void_p
+        _clib.ora_ibem_assemble.argtypes = [C.c_int, C.c_int, C.c_int, P, P, P, C.c_double, C.c_int, P, C.c_int, P,
+                                            C.c_int, P, C.c_double, C.c_double, P, P, P, P]
+        _clib.ora_sinc_resistance.argtypes = [C.c_int, P, C.c_double, C.c_double, C.c_double, C.c_double, P]
+    return _clib
+
+
+def _soa(P):
+    return np.ascontiguousarray(np.asarray(P, dtype=np.float64))
+
+
+# ---------------------------------------------------------------------------
+# ESM  (MATLAB/esmV.m:20-30; CUDA/esm.cuh:112-174)
+# ---------------------------------------------------------------------------
+def esm_matrices(r_ms, r_lh, k, r_i, c, rho):
+    """D, M_sq (m x m; rows = surface points, cols = sources) and M_hq
+    (l x m) of the equivalent source method, sources at r_ms * r_i."""
+    S = _soa(r_ms).T            # (m, 3)
+    Hp = _soa(r_lh).T           # (l, 3)
+    Q = S * r_i
+    dsq = S[:, None, :] - Q[None, :, :]
+    R_sq = np.sqrt((dsq ** 2).sum(-1))
+    vr_s = np.sqrt((S ** 2).sum(-1))
+    cos_t = (S[:, None, :] * dsq).sum(-1) / (vr_s[:, None] * R_sq)
+    ek = np.exp(1j * k * R_sq)
+    D = ((1j * k * R_sq - 1.0) / (4 * np.pi * R_sq ** 2)) * ek * cos_t
+    M_sq = (1j * rho * k * c) * (ek / (4 * np.pi * R_sq))
+    R_hq = np.sqrt(((Hp[:, None, :] - Q[None, :, :]) ** 2).sum(-1))
+    M_hq = (1j * rho * k * c) * (np.exp(1j * k * R_hq) / (4 * np.pi * R_hq))
+    return D, M_sq, M_hq
+
+
+def esm(r_ms, r_lh, k, r_i, c, rho):
+    """Me = M_sq D^-1 and He = M_hq D^-1 (esmV.m:30; esm.cuh:153-170)."""
+    D, M_sq, M_hq = esm_matrices(r_ms, r_lh, k, r_i, c, rho)
+    DT = D.T
+    Me = np.linalg.solve(DT, M_sq.T).T
+    He = np.linalg.solve(DT, M_hq.T).T
+    return Me, He
+
+
+def monopole_matrix(mics, sources, k):
+    """Plain ESM transfer matrix G_ij = exp(ik r_ij) / (4 pi r_ij) between
+    microphones (rows) and equivalent sources (cols); equals M_hq/(i rho c k)
+    of esmV.m:29-30 with the sources given directly."""
+    Mi = _soa(mics).T
+    Sj = _soa(sources).T
+    R = np.sqrt(((Mi[:, None, :] - Sj[None, :, :]) ** 2).sum(-1))
+    return np.exp(1j * k * R) / (4 * np.pi * R)
+
+
+def retreat_sources(surface, retreat):
+    """Surface points moved radially toward the origin by ``retreat``."""
+    S = _soa(surface)
+    rn = np.linalg.norm(S, axis=0)
+    return S * (1.0 - retreat / rn)
+
+
+# ---------------------------------------------------------------------------
+# IBEM  (CUDA/ibem.cuh:424-770; OpenBEM collocation)
+# ---------------------------------------------------------------------------
+def _rule_soa(rule):
+    rule = np.asarray(rule, dtype=np.float64)
+    return np.ascontiguousarray(rule.T).ravel(), rule.shape[0]
+
+
+def ibem_assemble(nodes, elems, mics, k, regular, singular, c, rho, chief=None):
+    """A, B (scaled by i rho c k) of size (m+n_ch) x m and A_hs, B_hs (l x m),
+    exactly the matrices the reference builds before its zgels
+    (CUDA/ibem.cuh:479-746)."""
+    r_ms = _soa(nodes).ravel()
+    r_lh = _soa(mics).ravel()
+    e_n = np.ascontiguousarray(np.asarray(elems, dtype=np.int32)).ravel()
+    m, l, n = r_ms.size // 3, r_lh.size // 3, e_n.size // 3
+    n_ch = 0 if chief is None else np.asarray(chief).shape[1]
+    cp = _soa(chief).ravel() if n_ch else np.zeros(3)
+    reg, nq = _rule_soa(regular)
+    sing = np.asarray(singular, dtype=np.float64)
+    nqs = sing.shape[1]
+    sg = np.ascontiguousarray(np.concatenate([_rule_soa(sing[p])[0] for p in range(3)]))
+    mt = m + n_ch
+    A = np.zeros((mt, m), np.complex128, order="F")
+    B = np.zeros((mt, m), np.complex128, order="F")
+    Ahs = np.zeros((l, m), np.complex128, order="F")
+    Bhs = np.zeros((l, m), np.complex128, order="F")
+    clib().ora_ibem_assemble(m, l, n, r_ms.ctypes.data, e_n.ctypes.data, r_lh.ctypes.data, float(k), nq,
+                             reg.ctypes.data, nqs, sg.ctypes.data, n_ch, cp.ctypes.data, float(c), float(rho),
+                             A.ctypes.data, B.ctypes.data, Ahs.ctypes.data, Bhs.ctypes.data)
+    return A, B, Ahs, Bhs
+
+
+def ibem(nodes, elems, mics, k, regular, singular, c, rho, chief=None):
+    """Z = A \\ B (least squares when CHIEF rows are present) and
+    H = A_hs Z - B_hs (CUDA/ibem.cuh:748-769)."""
+    A, B, Ahs, Bhs = ibem_assemble(nodes, elems, mics, k, regular, singular, c, rho, chief)
+    if A.shape[0] == A.shape[1]:
+        Z = np.linalg.solve(A, B)
+    else:
+        Z = np.linalg.lstsq(A, B, rcond=None)[0]
+    return Z, Ahs @ Z - Bhs
+
+
+def ibem_transfer(nodes, elems, mics, k, regular, singular, c, rho, chief=None):
+    """Only H, computed as W B - B_hs with W = A_hs A^-1 (the same matrix as
+    ibem()'s H, through an l-right-hand-side solve)."""
+    A, B, Ahs, Bhs = ibem_assemble(nodes, elems, mics, k, regular, singular, c, rho, chief)
+    if A.shape[0] != A.shape[1]:
+        return ibem(nodes, elems, mics, k, regular, singular, c, rho, chief)[1]
+    W = np.linalg.solve(A.T, Ahs.T).T
+    return W @ B - Bhs
+
+
+# ---------------------------------------------------------------------------
+# HELS  (CUDA/hels.cuh:222-323; MATLAB/helsV.m)
+# ---------------------------------------------------------------------------
+def _assoc_legendre(nmax, x):
+    """P_n^m(x) for 0 <= m <= n <= nmax with the Condon-Shortley phase, built
+    as the reference does: (-1)^m (1-x^2)^{m/2} (2m)!/(2^m m!) C^{m+1/2}_{n-m}(x)
+    (CUDA/hels.cuh:239-245), the Gegenbauer polynomial by its three-term
+    recurrence (MATLAB/gegenbauer.m:5-27)."""
+    x = np.asarray(x, dtype=np.float64)
+    P = np.zeros((nmax + 1, nmax + 1) + x.shape)
+    for mm in range(nmax + 1):
+        lam = mm + 0.5
+        pref = (-1.0) ** mm * (1 - x * x) ** (mm / 2.0) * math.factorial(2 * mm) / (2.0 ** mm * math.factorial(mm))
+        g_prev2 = np.ones_like(x)
+        g_prev1 = 2 * lam * x
+        for d in range(nmax - mm + 1):
+            if d == 0:
+                gd = g_prev2
+            elif d == 1:
+                gd = g_prev1
+            else:
+                gd = (2 * (d - 1 + lam) * x * g_prev1 - (d - 1 + 2 * lam - 1) * g_prev2) / d
+                g_prev2, g_prev1 = g_prev1, gd
+            P[mm + d, mm] = pref * gd
+    return P
+
+
+def _ynm_columns(order, az, el):
+    """Y_n^m at points (az, el) for every column i = n^2 + n + m, m = -n..n
+    (CUDA/hels.cuh:235, 246-247, 271)."""
+    nt = (order + 1) ** 2
+    P = _assoc_legendre(order, np.cos(el))
+    Y = np.zeros((az.size, nt), np.complex128)
+    for i in range(nt):
+        nn = int(math.floor(math.sqrt(i)))
+        mm = i - nn - nn * nn
+        a = abs(mm)
+        norm = math.sqrt((2 * nn + 1) * math.factorial(nn - a) / (4 * math.pi * math.factorial(nn + a)))
+        y = norm * P[nn, a] * np.exp(1j * a * az)
+        if mm < 0:
+            y = (-1.0) ** a * np.conj(y)
+        Y[:, i] = y
+    return Y
+
+
+def _sph_h(order, x):
+    from scipy.special import spherical_jn, spherical_yn
+    ns = np.arange(order + 1)[:, None]
+    h = spherical_jn(ns, x[None, :]) + 1j * spherical_yn(ns, x[None, :])
+    dh = spherical_jn(ns, x[None, :], derivative=True) + 1j * spherical_yn(ns, x[None, :], derivative=True)
+    return h, dh
+
+
+def hels(r_ms_s, r_lh_s, k, order, c, rho):
+    """Me (m x nt), He (l x nt), Qe (m x nt): h_n(kr) Y_n^m, h_n(kr) Y_n^m,
+    h_n'(kr) k Y_n^m / (i rho c k), h_n = j_n + i y_n (CUDA/hels.cuh:248-257,
+    298-302).  Points are (az, el, r) rows (CUDA/utils.cuh:414)."""
+    S = _soa(r_ms_s)
+    Hp = _soa(r_lh_s)
+    ns = np.array([int(math.floor(math.sqrt(i))) for i in range((order + 1) ** 2)])
+    Ys = _ynm_columns(order, S[0], S[1])
+    Yh = _ynm_columns(order, Hp[0], Hp[1])
+    hs, dhs = _sph_h(order, k * S[2])
+    hh, _ = _sph_h(order, k * Hp[2])
+    Me = hs[ns].T * Ys
+    Qe = (1.0 / (1j * rho * c * k)) * (k * dhs[ns].T) * Ys
+    He = hh[ns].T * Yh
+    return Me, He, Qe
+
+
+# ---------------------------------------------------------------------------
+# radiation resistance (sinc form; no reference code -- unpinned)
+# ---------------------------------------------------------------------------
+def sinc_resistance(centres, k, c, rho, area):
+    x = _soa(centres).ravel()
+    n = x.size // 3
+    R = np.zeros((n, n), order="F")
+    clib().ora_sinc_resistance(n, x.ctypes.data, float(k), float(c), float(rho), float(area), R.ctypes.data)
+    return R
+
+
+def radiation_modes(centres, k, c, rho, area):
+    """Eigenpairs of R (descending eigenvalues)."""
+    R = sinc_resistance(centres, k, c, rho, area)
+    w, V = np.linalg.eigh(R)
+    return w[::-1].copy(), V[:, ::-1].copy()
+
+
+def sound_power_R(R, v):
+    """W = 1/2 v^H R v (real R)."""
+    return 0.5 * float(np.real(np.vdot(v, R @ v)))
+
+
+# ---------------------------------------------------------------------------
+# products and sound power (CUDA/utils.cuh:199-289)
+# ---------------------------------------------------------------------------
+def to_pressure(Me, x):
+    return Me @ x
+
+
+def to_velocity(Qe, x):
+    return Qe @ x
+
+
+def sound_power(p, v, s):
+    """W = 1/2 Re(v^H p) S/m (CUDA/utils.cuh:279-280)."""
+    return 0.5 * float(np.real(np.vdot(v, p))) * (s / p.size)
+
+
+# ---------------------------------------------------------------------------
+# regularisation  (CUDA/tsvd.cuh; MATLAB/regtools)
+# ---------------------------------------------------------------------------
+def csvd(A):
+    """Compact SVD A = U diag(s) V^H, descending s (csvdG.m:17-24)."""
+    A = np.asarray(A)
+    m, n = A.shape
+    if m >= n:
+        U, s, Vh = np.linalg.svd(A, full_matrices=False)
+        return U, s, Vh.conj().T
+    V, s, Uh = np.linalg.svd(A.conj().T, full_matrices=False)
+    return Uh.conj().T, s, V
+
+
+def tsvd(U, s, V, b, k):
+    """x_k = V(:,1:k) diag(1/s(1:k)) U(:,1:p)^H b (tsvdG.m:20-23,
+    tsvd.cuh:151-154).  Raises for k outside [1, p] (tsvd.cuh:124)."""
+    p = s.size
+    if k < 1 or k > p:
+        raise ValueError("k out of range")
+    beta = U[:, :p].conj().T @ b
+    return V[:, :k] @ (beta[:k] / s[:k])
+
+
+def tikhonov(U, s, V, b, lam):
+    """x = V (s beta / (s^2 + lam^2)) (tikhonovG.m:26-30)."""
+    if lam < 0:
+        raise ValueError("lambda must be >= 0")
+    beta = U[:, :s.size].conj().T @ b
+    return V[:, :s.size] @ (s * beta / (s * s + lam * lam))
+
+
+def gcv_grid(s, npoints=200, grid=None):
+    """Descending lambda grid: regtools' from s_1 down to max(s_p, 16 eps s_1)
+    (gcvG.m:28-30), or a fixed (lo, hi) log-spaced grid."""
+    if grid is None:
+        rpm = max(s[-1], s[0] * 16 * EPS)
+        ratio = (s[0] / rpm) ** (1.0 / (npoints - 1))
+        return ratio ** np.arange(npoints - 1, -1, -1) * rpm
+    lo, hi = grid
+    t = np.arange(npoints) / (npoints - 1)
+    return np.exp(math.log(hi) + t * (math.log(lo) - math.log(hi)))
+
+
+def _gcv_terms(s, b2, delta0, dof, lam, mode):
+    if mode == "reference":
+        f = lam * lam / (s + lam * lam)            # gcvG.m:47
+    else:
+        f = lam * lam / (s * s + lam * lam)        # Hansen's Tikhonov filter
+    num = float(np.sum(f * f * b2) + delta0)
+    den = dof + float(np.sum(f))
+    return num, den, f
+
+
+def gcv_function(s, beta, lam, m, delta0=0.0, mode="standard"):
+    b2 = np.abs(beta) ** 2
+    num, den, _ = _gcv_terms(s, b2, delta0, m - s.size, lam, mode)
+    return num / (den * den)
+
+
+def gcv_delta0(b, beta, m, p):
+    """Intrinsic residual ||b||^2 - ||beta||^2 when m > p (gcvG.m:26,32-35)."""
+    d = float(np.vdot(b, b).real - np.vdot(beta, beta).real)
+    return d if (m > p and d > 0) else 0.0
+
+
+GCV_BISECT_ITERS = 64
+
+
+def gcv(U, s, b, npoints=200, grid=None, mode="standard"):
+    """lambda minimising GCV.  Grid search as gcvG.m:28-42, then on the
+    bracket [lam_{i+1}, lam_{i-1}] around the grid minimum:
+      standard  -- the zero of dG/dlog(lam) by 64 bisection steps in log(lam)
+                   (G = (sum f^2|beta|^2 + delta0) / ((m-p) + sum f)^2,
+                   f = lam^2/(s^2+lam^2)); the endpoint if G is monotone there;
+      reference -- gcvG.m exactly: grid filter lam/(s+lam) (:38), objective
+                   filter lam^2/(s+lam^2) (:47), Brent's fminbnd (:51)."""
+    m = U.shape[0]
+    p = s.size
+    beta = U[:, :p].conj().T @ b
+    delta0 = gcv_delta0(b, beta, m, p)
+    return gcv_from_beta(s, beta, m, delta0, npoints, grid, mode)
+
+
+def gcv_from_beta(s, beta, m, delta0, npoints=200, grid=None, mode="standard"):
+    p = s.size
+    b2 = np.abs(beta) ** 2
+    lam = gcv_grid(s, npoints, grid)
+    dof = m - p
+    G = np.empty(npoints)
+    for j in range(npoints):
+        if mode == "reference":
+            f = lam[j] / (s + lam[j])                  # gcvG.m:38
+            num = float(np.sum(f * f * b2) + delta0)
+            den = dof + float(np.sum(f))
+        else:
+            num, den, _ = _gcv_terms(s, b2, delta0, dof, lam[j], mode)
+        G[j] = num / (den * den)
+    jmin = int(np.argmin(G))
+    lo = lam[min(jmin + 1, npoints - 1)]
+    hi = lam[max(jmin - 1, 0)]
+    if mode == "reference":
+        fun = lambda la: gcv_function(s, beta, la, m, delta0, "reference")  # noqa: E731
+        return fminbnd(fun, lo, hi)
+    return _gcv_bisect(s, b2, delta0, dof, lo, hi)
+
+
+def _gcv_slope_sign_term(s, b2, delta0, dof, t):
+    lam = math.exp(t)
+    num, den, f = _gcv_terms(s, b2, delta0, dof, lam, "standard")
+    dnum = 4.0 * float(np.sum(f * f * (1.0 - f) * b2))
+    dden = 2.0 * float(np.sum(f * (1.0 - f)))
+    return dnum * den - 2.0 * num * dden
+
+
+def _gcv_bisect(s, b2, delta0, dof, lo, hi):
+    a, b = math.log(lo), math.log(hi)
+    if lo == hi:
+        return lo
+    if _gcv_slope_sign_term(s, b2, delta0, dof, a) >= 0.0:
+        return lo
+    if _gcv_slope_sign_term(s, b2, delta0, dof, b) <= 0.0:
+        return hi
+    for _ in range(GCV_BISECT_ITERS):
+        mid = 0.5 * (a + b)
+        if _gcv_slope_sign_term(s, b2, delta0, dof, mid) < 0.0:
+            a = mid
+        else:
+            b = mid
+    return math.exp(0.5 * (a + b))
+
+
+def fminbnd(fun, ax, bx, tolx=1e-4, maxiter=500):
+    """Brent's bounded minimiser (golden section + parabolic steps), with
+    MATLAB fminbnd's tolerances: tol1 = sqrt(eps)|x| + tolx/3."""
+    seps = math.sqrt(EPS)
+    c = 0.5 * (3.0 - math.sqrt(5.0))
+    a, b = ax, bx
+    v = a + c * (b - a)
+    w = xf = v
+    d = e = 0.0
+    fx = fun(xf)
+    fv = fw = fx
+    xm = 0.5 * (a + b)
+    tol1 = seps * abs(xf) + tolx / 3.0
+    tol2 = 2.0 * tol1
+    it = 0
+    while abs(xf - xm) > (tol2 - 0.5 * (b - a)) and it < maxiter:
+        golden = True
+        if abs(e) > tol1:
+            golden = False
+            r = (xf - w) * (fx - fv)
+            q = (xf - v) * (fx - fw)
+            p = (xf - v) * q - (xf - w) * r
+            q = 2.0 * (q - r)
+            if q > 0.0:
+                p = -p
+            q = abs(q)
+            r = e
+            e = d
+            if abs(p) < abs(0.5 * q * r) and p > q * (a - xf) and p < q * (b - xf):
+                d = p / q
+                x = xf + d
+                if (x - a) < tol2 or (b - x) < tol2:
+                    si = 1.0 if (xm - xf) >= 0 else -1.0
+                    d = tol1 * si
+            else:
+                golden = True
+        if golden:
+            e = (a - xf) if xf >= xm else (b - xf)
+            d = c * e
+        si = 1.0 if d >= 0 else -1.0
+        x = xf + si * max(abs(d), tol1)
+        fu = fun(x)
+        it += 1
+        if fu <= fx:
+            if x >= xf:
+                a = xf
+            else:
+                b = xf
+            v, fv = w, fw
+            w, fw = xf, fx
+            xf, fx = x, fu
+        else:
+            if x < xf:
+                a = x
+            else:
+                b = x
+            if fu <= fw or w == xf:
+                v, fv = w, fw
+                w, fw = x, fu
+            elif fu <= fv or v == xf or v == w:
+                v, fv = x, fu
+        xm = 0.5 * (a + b)
+        tol1 = seps * abs(xf) + tolx / 3.0
+        tol2 = 2.0 * tol1
+    return xf
+
+
+def solve_tikhonov_gcv(H, b, npoints=200, grid=None, mode="standard"):
+    """The per-frequency inverse step: csvd, GCV lambda, Tikhonov x."""
+    U, s, V = csvd(H)
+    lam = gcv(U, s, b, npoints, grid, mode)
+    return tikhonov(U, s, V, b, lam), lam, s

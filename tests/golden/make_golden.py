@@ -1,0 +1,69 @@
+"""Generate tests/golden/ref_vectors.npz from the reference's own CPU code.
+
+Run here, where the reference tree is mounted (it is read, never modified):
+
+    python oracle/build.py            # builds oracle/_ref/libiaref.so
+    python tests/golden/make_golden.py
+
+Contents (all produced by the reference's compiled esm()/ibem()/sphere()/
+cartesian_2_spherical(), built with C_AIR=343, RHO_AIR=1.21):
+  rule_regular (13, 3), rule_singular (3, 1600, 3)  the reference's quadrature
+      tables (CUDA/IPF.txt, CUDA/IPFs.txt), read as golden inputs
+  mesh_nodes (3, 42), mesh_elems (3, 80)  icosphere subdiv 1, radius 0.1
+  mics (3, 30), chief (3, 2), ks (2,)
+  ibem_Z_{0,1}, ibem_H_{0,1}        ibem() at ks[0], ks[1], no CHIEF points
+  ibem_chief_Z, ibem_chief_H        ibem() at ks[0] with the 2 CHIEF points
+  esm_src (3, 42), esm_fld (3, 42), esm_k, esm_ri, esm_Me, esm_He   esm(), l == m
+  kat_ps, kat_ph, kat_u, kat_a     sphere() analytic pressures at mesh nodes / mics
+  sph_in (3, 12), sph_out (3, 12)  cartesian_2_spherical()
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from inverseacoustics_gb300 import geometry as g  # noqa: E402
+from oracle import build, ref  # noqa: E402
+
+REF_CUDA = "/root/reference/CUDA"
+
+
+def main():
+    build.build_ref()
+    c, rho = ref.constants()
+    assert (c, rho) == (343.0, 1.21)
+    reg, sing = ref.read_reference_rules(REF_CUDA)
+    rng = np.random.default_rng(1234)
+    nodes, elems = g.icosphere(1, 0.10)
+    mics = g.hemisphere_array(rng, 30, 0.30)
+    chief = np.array([[0.01, 0.02, -0.03], [-0.02, 0.0, 0.015]]).T.copy()
+    ks = np.array([2 * np.pi * 400.0 / c, 2 * np.pi * 1500.0 / c])
+    out = dict(rule_regular=reg, rule_singular=sing, mesh_nodes=nodes, mesh_elems=elems, mics=mics, chief=chief,
+               ks=ks, c=np.array(c), rho=np.array(rho))
+    for i, k in enumerate(ks):
+        Z, H = ref.ibem(nodes, elems, mics, k, reg, sing)
+        out[f"ibem_Z_{i}"], out[f"ibem_H_{i}"] = Z, H
+    Z, H = ref.ibem(nodes, elems, mics, ks[0], reg, sing, chief)
+    out["ibem_chief_Z"], out["ibem_chief_H"] = Z, H
+    src = nodes.copy()
+    fld = nodes * 1.8
+    esm_k = 2 * np.pi * 800.0 / c
+    Me, He = ref.esm(src, fld, esm_k, 0.7)
+    out.update(esm_src=src, esm_fld=fld, esm_k=np.array(esm_k), esm_ri=np.array(0.7), esm_Me=Me, esm_He=He)
+    ps, ph, _ = ref.sphere(nodes, mics, ks[1], 0.02, 0.10)
+    out.update(kat_ps=ps, kat_ph=ph, kat_u=np.array(0.02), kat_a=np.array(0.10))
+    P = rng.normal(size=(3, 12))
+    out.update(sph_in=P, sph_out=ref.cart2sph(P))
+    path = os.path.join(HERE, "ref_vectors.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+"""CPU suite: the C ABI library loads and exports every symbol include/ia.h
+declares; argument checks that fire before any device work."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from inverseacoustics_gb300 import _lib
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "ia.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ia_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    names = header_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_ctypes_table_covers_header():
+    assert set(header_functions()) == set(_lib.declared_symbols())
+
+
+def test_config_defaults():
+    cfg = _lib.default_config()
+    assert (cfg.c, cfg.rho, cfg.gcv_points, cfg.gcv_mode, cfg.method) == (343.0, 1.21, 200, 0, 0)
+    assert C.sizeof(_lib.Config) == _lib.lib().ia_config_size()
+
+
+def test_status_strings():
+    L = _lib.lib()
+    assert L.ia_status_string(0) == b"ok"
+    assert L.ia_status_string(7) == b"invalid quadrature rule"
+
+
+def test_tsvd_k_out_of_range_is_an_error():
+    """The reference prints and leaves x unset (CUDA/tsvd.cuh:124-126); here it
+    is IA_ERR_ARG, raised before any device work."""
+    from inverseacoustics_gb300 import api
+    U = np.eye(4, dtype=np.complex128)
+    s = np.ones(4)
+    for k in (0, 5):
+        with pytest.raises(_lib.IAError) as e:
+            api.tsvd(U, s, U, np.ones(4), k)
+        assert e.value.code == 1
+
+
+def test_bad_arguments_rejected_before_device_work():
+    from inverseacoustics_gb300 import api
+    with pytest.raises(_lib.IAError) as e:
+        api.esm(np.zeros((3, 4)), np.zeros((3, 4)), -1.0, 0.5)
+    assert e.value.code == 1
+    bad = np.zeros((3, 4))
+    bad[0, 0] = np.nan
+    with pytest.raises(_lib.IAError) as e:
+        api.esm(bad, np.ones((3, 4)), 1.0, 0.5)
+    assert e.value.code == 6

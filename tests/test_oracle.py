@@ -1,0 +1,162 @@
+"""CPU suite: the oracle pinned against the reference's own outputs (golden
+vectors from its compiled CPU code), analytic known answers and
+independent scipy implementations."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import relerr
+from inverseacoustics_gb300 import geometry as g
+from oracle import ia_oracle as O
+
+
+def test_rules_weights(golden):
+    assert golden["rule_regular"].shape == (13, 3)
+    assert abs(golden["rule_regular"][:, 2].sum() - 0.5) < 1e-14
+    for p in range(3):
+        assert abs(golden["rule_singular"][p, :, 2].sum() - 0.5) < 1e-13
+
+
+def test_oracle_ibem_matches_reference(golden):
+    c, rho = float(golden["c"]), float(golden["rho"])
+    for i in range(2):
+        Z, H = O.ibem(golden["mesh_nodes"], golden["mesh_elems"], golden["mics"], golden["ks"][i],
+                      golden["rule_regular"], golden["rule_singular"], c, rho)
+        assert relerr(Z, golden[f"ibem_Z_{i}"]) < 1e-12
+        assert relerr(H, golden[f"ibem_H_{i}"]) < 1e-12
+
+
+def test_oracle_ibem_chief_matches_reference(golden):
+    c, rho = float(golden["c"]), float(golden["rho"])
+    Z, H = O.ibem(golden["mesh_nodes"], golden["mesh_elems"], golden["mics"], golden["ks"][0],
+                  golden["rule_regular"], golden["rule_singular"], c, rho, golden["chief"])
+    assert relerr(Z, golden["ibem_chief_Z"]) < 1e-12
+    assert relerr(H, golden["ibem_chief_H"]) < 1e-12
+
+
+def test_oracle_transfer_equals_ibem_H(golden):
+    c, rho = float(golden["c"]), float(golden["rho"])
+    H = O.ibem_transfer(golden["mesh_nodes"], golden["mesh_elems"], golden["mics"], golden["ks"][1],
+                        golden["rule_regular"], golden["rule_singular"], c, rho)
+    assert relerr(H, golden["ibem_H_1"]) < 1e-12
+
+
+def test_oracle_esm_matches_reference(golden):
+    Me, He = O.esm(golden["esm_src"], golden["esm_fld"], float(golden["esm_k"]), float(golden["esm_ri"]),
+                   float(golden["c"]), float(golden["rho"]))
+    assert relerr(Me, golden["esm_Me"]) < 1e-12
+    assert relerr(He, golden["esm_He"]) < 1e-12
+
+
+def test_analytic_sphere_matches_reference(golden):
+    k = golden["ks"][1]
+    ps = g.pulsating_sphere_pressure(golden["mesh_nodes"], k, float(golden["kat_a"]), float(golden["kat_u"]))
+    ph = g.pulsating_sphere_pressure(golden["mics"], k, float(golden["kat_a"]), float(golden["kat_u"]))
+    assert relerr(ps, golden["kat_ps"]) < 1e-14
+    assert relerr(ph, golden["kat_ph"]) < 1e-14
+
+
+def test_cart2sph_matches_reference(golden):
+    assert np.allclose(g.cartesian_to_spherical(golden["sph_in"]), golden["sph_out"], rtol=0, atol=1e-14)
+
+
+def test_ibem_sphere_kat_reference_rules(golden):
+    """IBEM of a pulsating sphere against the analytic field (the reference's
+    own KAT, CUDA/utils.cuh:384): discretisation error only."""
+    nodes, elems = g.icosphere(2, 0.1)
+    mics = golden["mics"]
+    k = 2 * np.pi * 700 / 343.0
+    Z, H = O.ibem(nodes, elems, mics, k, golden["rule_regular"], golden["rule_singular"], 343.0, 1.21)
+    ph = g.pulsating_sphere_pressure(mics, k, 0.1, 1.0)
+    assert relerr(H @ np.ones(nodes.shape[1]), ph) < 3e-2
+
+
+def test_hels_legendre_against_scipy():
+    sp = pytest.importorskip("scipy.special")
+    x = np.linspace(-0.99, 0.99, 7)
+    P = O._assoc_legendre(12, x)
+    for n in range(13):
+        for m in range(n + 1):
+            assert np.allclose(P[n, m], sp.lpmv(m, n, x), rtol=1e-10, atol=1e-12)
+
+
+def test_hels_ynm_orthonormal():
+    """Y_n^m columns are orthonormal under a product Gauss quadrature on the sphere."""
+    order = 6
+    xg, wg = np.polynomial.legendre.leggauss(16)
+    nphi = 32
+    phi = 2 * np.pi * np.arange(nphi) / nphi
+    el = np.arccos(xg)
+    AZ, EL = np.meshgrid(phi, el, indexing="ij")
+    W = np.outer(np.full(nphi, 2 * np.pi / nphi), wg).ravel()
+    Y = O._ynm_columns(order, AZ.ravel(), EL.ravel())
+    G = (Y.conj().T * W) @ Y
+    assert np.abs(G - np.eye(G.shape[0])).max() < 1e-12
+
+
+def test_hels_monopole_expansion():
+    """A monopole at the origin is exactly h_0 Y_0^0: He column 0 times
+    ik sqrt(4 pi)/(4 pi) equals exp(ikr)/(4 pi r)."""
+    P = g.cartesian_to_spherical(g.planar_array(4, 4, 0.05, 0.2))
+    k = 2 * np.pi * 1000 / 343.0
+    _, He, _ = O.hels(P, P, k, 3, 343.0, 1.21)
+    r = P[2]
+    coef = 1j * k * math.sqrt(4 * math.pi) / (4 * math.pi)
+    assert relerr(He[:, 0] * coef, np.exp(1j * k * r) / (4 * np.pi * r)) < 1e-13
+
+
+def test_gcv_standard_is_grid_minimum():
+    rng = np.random.default_rng(5)
+    A = g.complex_normal(rng, (40, 25)) @ np.diag(np.logspace(0, -6, 25))
+    b = A @ g.complex_normal(rng, 25) + 1e-3 * g.complex_normal(rng, 40)
+    U, s, V = O.csvd(A)
+    lam = O.gcv(U, s, b)
+    beta = U.conj().T @ b
+    d0 = O.gcv_delta0(b, beta, 40, 25)
+    fine = np.exp(np.linspace(math.log(lam) - 0.05, math.log(lam) + 0.05, 2001))
+    G = [O.gcv_function(s, beta, la, 40, d0) for la in fine]
+    assert abs(math.log(fine[int(np.argmin(G))]) - math.log(lam)) < 1e-4
+
+
+def test_fminbnd_matches_scipy_bounded():
+    opt = pytest.importorskip("scipy.optimize")
+    f = lambda x: (x - 0.3) ** 2 + 0.1 * math.sin(5 * x)  # noqa: E731
+    ours = O.fminbnd(f, 0.0, 1.0, tolx=1e-10)
+    theirs = opt.minimize_scalar(f, bounds=(0.0, 1.0), method="bounded", options={"xatol": 1e-10}).x
+    assert abs(ours - theirs) < 1e-8
+
+
+def test_tikhonov_normal_equations():
+    rng = np.random.default_rng(7)
+    A = g.complex_normal(rng, (30, 50))
+    b = g.complex_normal(rng, 30)
+    U, s, V = O.csvd(A)
+    lam = 0.37
+    x = O.tikhonov(U, s, V, b, lam)
+    lhs = A.conj().T @ A @ x + lam ** 2 * x
+    assert relerr(lhs, A.conj().T @ b) < 1e-12
+
+
+def test_tsvd_and_range():
+    rng = np.random.default_rng(8)
+    A = g.complex_normal(rng, (20, 12))
+    b = g.complex_normal(rng, 20)
+    U, s, V = O.csvd(A)
+    x = O.tsvd(U, s, V, b, 12)
+    assert relerr(x, np.linalg.lstsq(A, b, rcond=None)[0]) < 1e-12
+    with pytest.raises(ValueError):
+        O.tsvd(U, s, V, b, 0)
+    with pytest.raises(ValueError):
+        O.tsvd(U, s, V, b, 13)
+
+
+def test_sinc_resistance_properties():
+    P, area = g.plate_grid(0.5, 0.4, 8, 6)
+    k = 2 * np.pi * 500 / 343.0
+    R = O.sinc_resistance(P, k, 343.0, 1.21, area)
+    assert np.allclose(R, R.T)
+    w, _ = O.radiation_modes(P, k, 343.0, 1.21, area)
+    assert w.min() > -1e-10 * w.max()          # positive semidefinite
+    om = k * 343.0
+    assert abs(R[0, 0] - om * om * 1.21 * area * area / (4 * np.pi * 343.0)) < 1e-12 * R[0, 0]
