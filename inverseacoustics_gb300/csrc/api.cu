@@ -392,9 +392,11 @@ int ia_mesh_destroy(ia_mesh *M)
 }
 
 // ---- batched device entry points ------------------------------------------
-static int check_info(ia_context *ctx, const int *d_info, int F)
+// info words are bit sets OR-ed by the kernels: every batched call that takes
+// one starts from zero
+static int clear_info(ia_context *ctx, int *d_info, int F)
 {
-    (void)ctx; (void)d_info; (void)F;
+    if (d_info) IA_CUDA_TRY(cudaMemsetAsync(d_info, 0, sizeof(int) * (size_t)F, ctx->stream));
     return IA_OK;
 }
 
@@ -442,6 +444,7 @@ int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
                   ws_round(sizeof(double2) * (size_t)m * l * F) * 2;
     int st = ws_reserve(ctx, need);
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
     double2 *At = cur.take<double2>((size_t)m * m * F);
@@ -465,6 +468,7 @@ int ia_svd_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_A, ia
 {
     if (!ctx || m < 1 || n < 1 || F < 1 || !d_A || !d_s || !d_info) return IA_ERR_ARG;
     int st = ws_reserve(ctx, svd_workspace_bytes(m, n, F));
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     const int M = m >= n ? m : n, N = m >= n ? n : m;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
@@ -489,6 +493,7 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
                       const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                       WsCursor &cur)
 {
+    if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;
     double2 *Y = cur.take<double2>((size_t)M * p * F);
@@ -501,8 +506,9 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
     return regularize_batched(ctx, m, n, p, F, U, s, V, nrhs, b, cfg, x, lambda);
 }
 
-static size_t solve_ws_bytes(int m, int n, int F)
+static size_t solve_ws_bytes(int m, int n, int F, int nrhs)
 {
+    if (m <= n) return wide_solve_ws_bytes(m, n, nrhs, F);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;
     return ws_round(sizeof(double2) * (size_t)M * p * F) + ws_round(sizeof(double2) * (size_t)p * p * F) +
@@ -514,7 +520,8 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
                    const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info)
 {
     if (!ctx || !cfg || m < 1 || n < 1 || F < 1 || nrhs < 1 || !d_H || !d_b || !d_x || !d_info) return IA_ERR_ARG;
-    int st = ws_reserve(ctx, solve_ws_bytes(m, n, F));
+    int st = ws_reserve(ctx, solve_ws_bytes(m, n, F, nrhs));
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
     return solve_core(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg, (double2 *)d_x,
@@ -529,8 +536,9 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         return IA_ERR_ARG;
     const int m = mesh->m;
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F);
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs);
     int st = ws_reserve(ctx, need);
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
     double2 *At = cur.take<double2>((size_t)m * m * F);
@@ -550,8 +558,9 @@ int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, cons
 {
     if (!ctx || !cfg || l < 1 || m < 1 || F < 1 || nrhs < 1 || !d_mics || !d_src || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
-    size_t need = ws_round(sizeof(double2) * (size_t)l * m * F) + solve_ws_bytes(l, m, F);
+    size_t need = ws_round(sizeof(double2) * (size_t)l * m * F) + solve_ws_bytes(l, m, F, nrhs);
     int st = ws_reserve(ctx, need);
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
     double2 *G = cur.take<double2>((size_t)l * m * F);
@@ -568,8 +577,9 @@ int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, i
     if (!ctx || !cfg || l < 1 || n_sh < 0 || F < 1 || nrhs < 1 || !d_pts || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
     const int nt = (n_sh + 1) * (n_sh + 1);
-    size_t need = ws_round(sizeof(double2) * (size_t)l * nt * F) + solve_ws_bytes(l, nt, F);
+    size_t need = ws_round(sizeof(double2) * (size_t)l * nt * F) + solve_ws_bytes(l, nt, F, nrhs);
     int st = ws_reserve(ctx, need);
+    if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
     double2 *H = cur.take<double2>((size_t)l * nt * F);

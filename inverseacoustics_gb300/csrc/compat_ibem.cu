@@ -1,84 +1,12 @@
-// ia_ibem: the reference-compatible IBEM entry point (ibem() CUDA/ibem.cuh:424),
-// plus the Householder least-squares kernel it needs when CHIEF rows make the
-// system overdetermined (the reference's zgels / ZZgels, CUDA/ibem.cuh:752-755,
-// :389-391).
+// ia_ibem: the reference-compatible IBEM entry point (ibem() CUDA/ibem.cuh:424).
+// Square systems use LU; CHIEF rows make the system overdetermined and it is
+// solved in the least-squares sense by Householder QR, as the reference's
+// zgels / ZZgels do (CUDA/ibem.cuh:752-755, :389-391).
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
-#include <mutex>
 #include "ia_common.cuh"
 #include "ia_internal.h"
-
-namespace ia {
-
-// One CTA per matrix.  Column j: reflector H_j = I - tau v v^H with v(0) = 1
-// (LAPACK zlarfg convention, beta = -sign(Re alpha) ||x||), then H_j^H
-// applied to the trailing columns of A and to all columns of B.
-constexpr int QR_THREADS = 512;
-
-__global__ void __launch_bounds__(QR_THREADS) geqrs_kernel(int rows, int cols, double2 *A, int lda, long long sA,
-                                                           int nrhs, double2 *B, int ldb, long long sB)
-{
-    __shared__ double red[QR_THREADS / 32];
-    __shared__ double2 s_tau;
-    __shared__ double2 s_scale;   // 1/(alpha - beta)
-    const int f = blockIdx.x;
-    A += f * sA;
-    B += f * sB;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = QR_THREADS / 32;
-    for (int j = 0; j < cols; ++j) {
-        double2 *x = A + j + (size_t)j * lda;
-        const int len = rows - j;
-        double sg = 0.0;
-        for (int i = 1 + tid; i < len; i += QR_THREADS) sg += zabs2(x[i]);
-        sg = warp_sum(sg);
-        if (lane == 0) red[wid] = sg;
-        __syncthreads();
-        if (tid == 0) {
-            double sigma = 0.0;
-            for (int w = 0; w < nw; ++w) sigma += red[w];
-            double2 alpha = x[0];
-            if (sigma == 0.0 && alpha.y == 0.0) {
-                s_tau = make_double2(0.0, 0.0);
-                s_scale = make_double2(0.0, 0.0);
-            } else {
-                double nrm = sqrt(zabs2(alpha) + sigma);
-                double beta = alpha.x >= 0.0 ? -nrm : nrm;
-                s_tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-                s_scale = zdiv(make_double2(1.0, 0.0), make_double2(alpha.x - beta, alpha.y));
-                x[0] = make_double2(beta, 0.0);
-            }
-        }
-        __syncthreads();
-        const double2 tau = s_tau, sc = s_scale;
-        if (tau.x == 0.0 && tau.y == 0.0) continue;
-        for (int i = 1 + tid; i < len; i += QR_THREADS) x[i] = zmul(x[i], sc);
-        __syncthreads();
-        // apply H^H = I - conj(tau) v v^H to trailing columns of A and to B
-        const double2 ctau = zconj(tau);
-        const int ntot = (cols - j - 1) + nrhs;
-        for (int c = wid; c < ntot; c += nw) {
-            double2 *col = c < cols - j - 1 ? A + j + (size_t)(j + 1 + c) * lda : B + j + (size_t)(c - (cols - j - 1)) * ldb;
-            double2 w = lane == 0 ? col[0] : make_double2(0.0, 0.0);   // v(0) = 1
-            for (int i = 1 + lane; i < len; i += 32) zcfma(w, x[i], col[i]);
-            w = warp_sum2(w);
-            w = zmul(ctau, w);
-            if (lane == 0) col[0] = zsub(col[0], w);
-            for (int i = 1 + lane; i < len; i += 32) zfms(col[i], x[i], w);
-        }
-        __syncthreads();
-    }
-}
-
-int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
-                   int ldb, long long sB, int batch)
-{
-    geqrs_kernel<<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, nrhs, B, ldb, sB);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
-}
-
-}  // namespace ia
 
 using namespace ia;
 

@@ -83,6 +83,9 @@ int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *in, int 
 
 // ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);
+// Jacobi on Y (M x N) with only the first Mdot rows in the dot products
+int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, double2 *Y, double2 *V, int batch, int max_sweeps,
+                        int *info);
 // sigma, normalised sorted outputs: Uy (M x N) <- Y/sigma, Vs (N x N) <- V, both column-permuted to
 // descending sigma.  Either output may be null.
 int svd_finalize_batched(ia_context *ctx, int M, int N, const double2 *Y, const double2 *V, double *s,
@@ -97,6 +100,20 @@ size_t svd_workspace_bytes(int m, int n, int batch);
 int regularize_batched(ia_context *ctx, int m, int n, int p, int batch, const double2 *U, const double *s,
                        const double2 *V, int nrhs, const double2 *b, const ia_config *cfg, double2 *x,
                        double *lambda);
+
+// from projected beta (F x nrhs x p): z = phi .* beta, lambda per (f, rhs);
+// bnorm2 (||b||^2 per (f, rhs)) may be null when m <= p (delta0 = 0)
+int gcv_beta_batched(ia_context *ctx, int m, int p, int batch, const double *s, int nrhs, const double2 *beta,
+                     const double *bnorm2, const ia_config *cfg, double2 *z, double *lambda);
+
+// ---- regularised solve of wide / square operators (wide_solve.cu)
+// A (m x n, m <= n) given as A or as A^T; x F x (n x nrhs).  Householder QR
+// of A^H when n > m, one-sided Jacobi on R with U^H b carried as extra rows,
+// GCV / Tikhonov, x = Q [U_R (phi .* beta); 0].
+size_t wide_solve_ws_bytes(int m, int n, int nrhs, int batch);
+int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
+                       const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
+                       WsCursor &cur);
 
 // ---- assembly (assemble.cu)
 int monopole_batched(ia_context *ctx, int l, int m, int F, const double *mics, const double *src, const double *k,

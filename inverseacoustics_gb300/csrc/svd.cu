@@ -7,8 +7,12 @@
 // warp rotates one pair with no synchronisation inside a round.  Column dot
 // products are warp-shuffle reductions in a fixed order, so repeated runs
 // give identical results.  A pair is rotated while
-// |y_i^H y_j| > sqrt(M) eps ||y_i|| ||y_j||; the sweep loop ends after a sweep
-// without rotations or at the sweep cap (IA_INFO_NOCONV).
+// |y_i^H y_j| > sqrt(Mdot) eps ||y_i|| ||y_j||; the sweep loop ends after a
+// sweep without rotations or at the sweep cap (IA_INFO_NOCONV).
+//
+// Only the first Mdot rows enter the dot products; rows Mdot..M-1 are rotated
+// along (the pipeline keeps conj(b)^T there, so U^H b falls out of the
+// rotations without forming U).
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -28,7 +32,24 @@ __device__ __forceinline__ void rr_pair(int N2, int round, int k, int &i, int &j
     if (i > j) { int t = i; i = j; j = t; }
 }
 
-__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int N, double2 *Y, long long sY,
+// Rotation that zeroes y_i^H y_j for column norms a, b and product g.
+__device__ __forceinline__ bool jacobi_rotation(double a, double b, double2 g, double tol, double &c, double2 &sp)
+{
+    double gm = sqrt(g.x * g.x + g.y * g.y);
+    if (!(gm > tol * sqrt(a) * sqrt(b)) || gm == 0.0) return false;
+    double zeta = (b - a) / (2.0 * gm);
+    double t;
+    if (fabs(zeta) > 1e150) t = 0.5 / zeta;
+    else t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+    c = 1.0 / sqrt(1.0 + t * t);
+    double s = t * c;
+    sp = make_double2(s * g.x / gm, s * g.y / gm);   // s' = s e^{i arg gamma}
+    return true;
+}
+
+// KPL > 0: rows cached in registers (M <= 32*KPL); KPL == 0: streamed.
+template <int KPL>
+__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int Mdot, int N, double2 *Y, long long sY,
                                                                       double2 *V, long long sV, int max_sweeps,
                                                                       double tol, int *info)
 {
@@ -49,44 +70,68 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int N
                 rr_pair(N2, round, k, i, j);
                 if (j >= N) continue;
                 double2 *yi = Y + (size_t)i * M, *yj = Y + (size_t)j * M;
-                double a = 0.0, b = 0.0;
-                double2 g = make_double2(0.0, 0.0);
-                for (int r = lane; r < M; r += 32) {
-                    double2 u = yi[r], v = yj[r];
-                    a = fma(u.x, u.x, fma(u.y, u.y, a));
-                    b = fma(v.x, v.x, fma(v.y, v.y, b));
-                    zcfma(g, u, v);
-                }
-                a = warp_sum(a);
-                b = warp_sum(b);
-                g = warp_sum2(g);
-                double gm = sqrt(g.x * g.x + g.y * g.y);
-                if (!(gm > tol * sqrt(a) * sqrt(b)) || gm == 0.0) continue;
-                double zeta = (b - a) / (2.0 * gm);
-                double t;
-                if (fabs(zeta) > 1e150) t = 0.5 / zeta;
-                else t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                double c = 1.0 / sqrt(1.0 + t * t);
-                double s = t * c;
-                double2 sp = make_double2(s * g.x / gm, s * g.y / gm);   // s' = s e^{i arg gamma}
-                double2 spc = zconj(sp);
-                for (int r = lane; r < M; r += 32) {
-                    double2 u = yi[r], v = yj[r];
-                    double2 nu = zscale(u, c), nv = zscale(v, c);
-                    zfms(nu, spc, v);
-                    zfma(nv, sp, u);
-                    yi[r] = nu;
-                    yj[r] = nv;
+                double a = 0.0, b = 0.0, c;
+                double2 g = make_double2(0.0, 0.0), sp;
+                if (KPL > 0) {
+                    double2 ui[KPL > 0 ? KPL : 1], vj[KPL > 0 ? KPL : 1];
+#pragma unroll
+                    for (int t = 0; t < KPL; ++t) {
+                        int r = lane + 32 * t;
+                        ui[t] = r < M ? yi[r] : make_double2(0.0, 0.0);
+                        vj[t] = r < M ? yj[r] : make_double2(0.0, 0.0);
+                        if (r < Mdot) {
+                            a = fma(ui[t].x, ui[t].x, fma(ui[t].y, ui[t].y, a));
+                            b = fma(vj[t].x, vj[t].x, fma(vj[t].y, vj[t].y, b));
+                            zcfma(g, ui[t], vj[t]);
+                        }
+                    }
+                    a = warp_sum(a);
+                    b = warp_sum(b);
+                    g = warp_sum2(g);
+                    if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
+                    const double2 spc = zconj(sp);
+#pragma unroll
+                    for (int t = 0; t < KPL; ++t) {
+                        int r = lane + 32 * t;
+                        if (r < M) {
+                            double2 nu = zscale(ui[t], c), nv = zscale(vj[t], c);
+                            zfms(nu, spc, vj[t]);
+                            zfma(nv, sp, ui[t]);
+                            yi[r] = nu;
+                            yj[r] = nv;
+                        }
+                    }
+                } else {
+                    for (int r = lane; r < Mdot; r += 32) {
+                        double2 u = yi[r], v = yj[r];
+                        a = fma(u.x, u.x, fma(u.y, u.y, a));
+                        b = fma(v.x, v.x, fma(v.y, v.y, b));
+                        zcfma(g, u, v);
+                    }
+                    a = warp_sum(a);
+                    b = warp_sum(b);
+                    g = warp_sum2(g);
+                    if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
+                    const double2 spc = zconj(sp);
+                    for (int r = lane; r < M; r += 32) {
+                        double2 u = yi[r], v = yj[r];
+                        double2 nu = zscale(u, c), nv = zscale(v, c);
+                        zfms(nu, spc, v);
+                        zfma(nv, sp, u);
+                        yi[r] = nu;
+                        yj[r] = nv;
+                    }
                 }
                 if (V) {
-                    double2 *vi = V + (size_t)i * N, *vj = V + (size_t)j * N;
+                    const double2 spc = zconj(sp);
+                    double2 *vi = V + (size_t)i * N, *vjp = V + (size_t)j * N;
                     for (int r = lane; r < N; r += 32) {
-                        double2 u = vi[r], v = vj[r];
+                        double2 u = vi[r], v = vjp[r];
                         double2 nu = zscale(u, c), nv = zscale(v, c);
                         zfms(nu, spc, v);
                         zfma(nv, sp, u);
                         vi[r] = nu;
-                        vj[r] = nv;
+                        vjp[r] = nv;
                     }
                 }
                 rot_local++;
@@ -111,7 +156,8 @@ __global__ void identity_kernel(int N, double2 *V, long long sV)
     }
 }
 
-int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info)
+int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, double2 *Y, double2 *V, int batch, int max_sweeps,
+                        int *info)
 {
     if (V) {
         dim3 g((N * N + 255) / 256 < 256 ? (N * N + 255) / 256 : 256, batch);
@@ -121,11 +167,21 @@ int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, in
     int nw = (N + 1) / 2;
     if (nw > SVD_MAX_WARPS) nw = SVD_MAX_WARPS;
     if (nw < 1) nw = 1;
-    double tol = sqrt((double)M) * 2.220446049250313e-16;
-    jacobi_kernel<<<batch, nw * 32, 0, ctx->stream>>>(M, N, Y, (long long)M * N, V, (long long)N * N, max_sweeps,
-                                                      tol, info);
+    const double tol = sqrt((double)Mdot) * 2.220446049250313e-16;
+    const long long sY = (long long)M * N, sV = (long long)N * N;
+    if (M <= 128)
+        jacobi_kernel<4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+    else if (M <= 256)
+        jacobi_kernel<8><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+    else
+        jacobi_kernel<0><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
+}
+
+int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info)
+{
+    return jacobi_rows_batched(ctx, M, M, N, Y, V, batch, max_sweeps, info);
 }
 
 // sigma_j = ||y_j||, descending order (ties by index), U = Y/sigma, V permuted.
@@ -133,7 +189,7 @@ __global__ void svd_finalize_kernel(int M, int N, const double2 *Y, const double
                                     double2 *Vs, int *info)
 {
     extern __shared__ double sm[];
-    double *sig = sm;                          // N
+    double *sig = sm;                              // N
     int *rank = reinterpret_cast<int *>(sm + N);   // N
     const int f = blockIdx.x;
     Y += (size_t)f * M * N;

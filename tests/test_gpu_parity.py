@@ -252,22 +252,25 @@ def test_hels_pipeline_matches_oracle(cuda, ctx):
     src = rng.normal(size=(3, 5)) * 0.03
     p = []
     for k in ks:
-        p.append((O.monopole_matrix(mics, src, k) @ g.complex_normal(rng, 5))[None, :])
+        p.append(g.add_noise(rng, O.monopole_matrix(mics, src, k) @ g.complex_normal(rng, 5), 25.0)[None, :])
     p = np.stack(p)
     x, lam, s, info = api.hels_solve_batch(ctx, T(pts, cuda), 6, T(ks, cuda), T(p, cuda))
     torch.cuda.synchronize()
     for f, k in enumerate(ks):
         _, He, _ = O.hels(pts, pts, k, 6, 343.0, 1.21)
         xo, lo, so = O.solve_tikhonov_gcv(He, p[f, 0])
-        assert abs(lam[f, 0].item() - lo) < 1e-9 * lo
+        # lambda sits at a zero of dG/dlog(lambda); summation-order noise moves it
+        # by ~ eps / G'' -- the solution is flat there, so x carries the 1e-9 bar.
+        assert abs(lam[f, 0].item() - lo) < 1e-7 * lo
         assert relerr(x[f, 0].cpu().numpy(), xo) < 1e-9
 
 
 def test_ibem_full_size_transfer(cuda, ctx):
     """Full config size (642 nodes, 1280 triangles, 120 mics): H at two of the
     64 frequencies against the oracle; the rest through size-independent
-    properties (finite, reciprocity-free: H v for the pulsating sphere close to
-    the analytic field)."""
+    properties (finite; H v for the pulsating sphere close to the analytic
+    field, away from the interior Dirichlet resonance ka = pi of the sphere,
+    where collocation BEM without CHIEF points is ill-posed)."""
     from inverseacoustics_gb300 import api
     import torch
     w = g.ibem_sphere(n_freq=8)
@@ -284,6 +287,8 @@ def test_ibem_full_size_transfer(cuda, ctx):
     for f in range(8):
         Hf = H[f].cpu().numpy().T
         assert np.isfinite(Hf).all()
+        if abs(w.k[f] * 0.1 - np.pi) < 0.05 * np.pi:
+            continue
         ph = g.pulsating_sphere_pressure(mics, w.k[f], 0.1, 1.0)
         assert relerr(Hf @ v, ph) < 5e-2
 
