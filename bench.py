@@ -172,17 +172,13 @@ def run_ours(args):
     k_d = torch.as_tensor(w.k, device=dev)
     p_d = torch.as_tensor(p_np, device=dev)
     p_h = torch.as_tensor(p_np).pin_memory()
-    cfg = api.default_config()
+    cfg64 = api.default_config()
+    cfg = api.default_config(precision=1)          # the mixed path: the headline
     m, l = nodes.shape[1], mics.shape[1]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
 
-    def step():
-        return api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, cfg)
-
-    for _ in range(max(args.warmup, 3)):
-        x, lam, s, info = step()
-    torch.cuda.synchronize()
-    assert int(info.abs().sum()) == 0, f"solver info flags {info.tolist()}"
+    def step(c=cfg):
+        return api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, c)
 
     def barrier():
         if world > 1:
@@ -190,28 +186,46 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident timing
-    times = []
-    launches0 = ctx.launches()
-    barrier()
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+    def max_over_ranks(v):
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([v], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    def timed_steps(c, steps):
+        """W warm-up steps, then `steps` steps each bracketed by CUDA events on
+        the launching stream, L2 flushed between them."""
+        for _ in range(max(args.warmup, 3)):
+            out = step(c)
+        torch.cuda.synchronize()
+        assert int(out[3].abs().sum()) == 0, f"solver info flags {out[3].tolist()}"
+        times = []
+        l0 = ctx.launches()
+        barrier()
+        for _ in range(steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            x, lam, s, info = step()
+            out = step(c)
             e1.record(stream)
             times.append((e0, e1))
         barrier()
-    launches = ctx.launches() - launches0
-    ms = [a.elapsed_time(b) for a, b in times]
-    total_ms = sum(ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total = max_over_ranks(sum(a.elapsed_time(b) for a, b in times))
+        return total, ctx.launches() - l0, out
+
+    # ---- FP64 path (the comparison point of the mixed path)
+    fp64_ms, _, out64 = timed_steps(cfg64, max(1, min(args.steps, 3)))
+    fp64_value = world * N_FREQ * max(1, min(args.steps, 3)) / (fp64_ms / 1000.0)
+    # ---- mixed path, device-resident
+    with ClockSampler(local) as clk:
+        total_ms, launches, out = timed_steps(cfg, args.steps)
+    x, lam, s, info = out
     value = world * N_FREQ * args.steps / (total_ms / 1000.0)
+    x64, lam64 = out64[0], out64[1]
+    err_x = float(((x - x64).abs().pow(2).sum(dim=(1, 2)).sqrt() / x64.abs().pow(2).sum(dim=(1, 2)).sqrt()).max())
+    err_lam = float(((lam - lam64).abs() / lam64.abs()).max())
 
     # ---- end to end through the public API, host buffers
     x_h = torch.empty((N_FREQ, 1, m), dtype=torch.complex128).pin_memory()
@@ -229,12 +243,7 @@ def run_ours(args):
         e1.record(stream)
         e2e_times.append((e0, e1))
     barrier()
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_times)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in e2e_times))
     e2e_value = world * N_FREQ * args.steps / (e2e_ms / 1000.0)
 
     # ---- per-stage timing (same stream, CUDA events) for the roofline
@@ -256,6 +265,8 @@ def run_ours(args):
     t_transfer = timed(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg))
     H, _ = api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg)
     t_solve = timed(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg))
+    t_transfer64 = timed(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg64), reps=1)
+    t_solve64 = timed(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg64), reps=1)
     hbm_peak, bf16_peak, peak_kind = _peaks()
     # assembly: algorithmic bytes = rows written, (m + l) rows x m columns x (A, B) x 16 B per frequency
     asm_bytes = N_FREQ * (m + l) * m * 2 * 16
@@ -279,8 +290,8 @@ def run_ours(args):
                 "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": None,
                 "peak_kind": peak_kind,
                 "note": "FP64-issue bound, not HBM bound; see compute",
-                "compute": {"stage": "LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
-                            "achieved": lu_flops / ((t_transfer - t_asm) / 1000.0) / 1e12,
+                "compute": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
+                            "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
                             "peak_dgemm_measured": fp64_tflops_dgemm}}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -293,13 +304,20 @@ def run_ours(args):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "precision_path": "fp64",
-                "data": "synthetic (seeded)",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "mixed: f64 assembly, f32 LU/QR/Jacobi, double-float (f32 pair) refinement GEMMs, "
+                         "f64 GCV and Tikhonov refinement",
+                "precision_path": "mixed", "data": "synthetic (seeded)",
                 "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies_per_gpu": N_FREQ,
                            "nodes": m, "triangles": int(elems.shape[1]), "mics": l,
                            "rules": "7-point Radon regular, 4x4 Duffy singular", "parallelism": f"freq-shard x{world}",
                            "l2": "flushed between timed steps (256 MB write)"},
-                "stages_ms": {"assembly": t_asm, "transfer_incl_assembly": t_transfer, "svd_gcv_tikhonov": t_solve},
+                "fp64_path": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms / max(1, min(args.steps, 3)),
+                              "mixed_speedup": value / fp64_value},
+                "accuracy": {"max_rel_err_x_vs_fp64": err_x, "max_rel_err_lambda_vs_fp64": err_lam,
+                             "bound": 1e-6, "note": "FP64 path parity-tested against the oracle at 1e-10"},
+                "stages_ms": {"assembly": t_asm, "transfer_incl_assembly": t_transfer, "svd_gcv_tikhonov": t_solve,
+                              "fp64_transfer_incl_assembly": t_transfer64, "fp64_svd_gcv_tikhonov": t_solve64},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(p_np.nbytes),
                         "d2h_bytes_per_step": int(x_h.numel() * 16 + lam_h.numel() * 8)},

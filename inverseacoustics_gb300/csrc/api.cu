@@ -436,13 +436,49 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
                          make_double2(-1.0, 0.0), Ht, m, sML, F);
 }
 
+static size_t transfer_mixed_ws_bytes(int m, int l, int F)
+{
+    return ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 2 * ws_round(16 * (size_t)m * l * F);
+}
+
+// Mixed transfer: FP32 LU of M = A^T; Y = M^-1 A_hs^T by FP32 solves refined
+// with double-float residuals R = A_hs^T - M Y (cfg->refine_steps times);
+// H^T = B^T Y - B_hs^T by the double-float GEMM.  Matrices in, H^T out in FP64.
+static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                                 const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
+                                 double2 *Ahs_t, double2 *Ht, int *d_info, WsCursor &cur)
+{
+    const int m = mesh->m;
+    float2 *M32 = cur.take<float2>((size_t)m * m * F);
+    float2 *Y32 = cur.take<float2>((size_t)m * l * F);
+    double2 *Y = cur.take<double2>((size_t)m * l * F);
+    double2 *R = cur.take<double2>((size_t)m * l * F);
+    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
+    if (st) return st;
+    const long long sMM = (long long)m * m, sML = (long long)m * l;
+    if ((st = copy2d_batched<double2, float2>(ctx, m, m, At, m, sMM, M32, m, sMM, false, F))) return st;
+    if ((st = getrf_batched<float2>(ctx, m, M32, m, sMM, ipiv, d_info, F))) return st;
+    if ((st = copy2d_batched<double2, float2>(ctx, m, l, Ahs_t, m, sML, Y32, m, sML, false, F))) return st;
+    if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
+    if ((st = copy2d_batched<float2, double2>(ctx, m, l, Y32, m, sML, Y, m, sML, false, F))) return st;
+    for (int it = 0; it < cfg->refine_steps; ++it) {
+        if ((st = zcopy2d_batched(ctx, m, l, Ahs_t, m, sML, R, m, sML, false, F))) return st;
+        if ((st = dfgemm_batched(ctx, m, l, m, -1.0, At, m, sMM, Y, m, sML, 1.0, R, m, sML, F))) return st;
+        if ((st = copy2d_batched<double2, float2>(ctx, m, l, R, m, sML, Y32, m, sML, false, F))) return st;
+        if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
+        if ((st = add2d_batched<float2>(ctx, m, l, Y32, m, sML, Y, m, sML, F))) return st;
+    }
+    return dfgemm_batched(ctx, m, l, m, 1.0, Bt, m, sMM, Y, m, sML, -1.0, Ht, m, sML, F);
+}
+
 int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                            const double *d_k, const ia_config *cfg, ia_complex *d_H, int *d_info)
 {
     if (!ctx || !mesh || !cfg || F < 1 || l < 1 || !d_mics || !d_k || !d_H || !d_info) return IA_ERR_ARG;
     const int m = mesh->m;
+    const bool mixed = cfg->precision == IA_PREC_MIXED;
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2;
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
@@ -452,7 +488,8 @@ int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
     int *ipiv = cur.take<int>((size_t)m * F);
     double2 *Ahs = cur.take<double2>((size_t)m * l * F);
     double2 *Ht = cur.take<double2>((size_t)m * l * F);
-    st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
+    if (mixed) st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info, cur);
+    else st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
     if (st) return st;
     return ztranspose_batched(ctx, m, l, Ht, m, (long long)m * l, (double2 *)d_H, l, (long long)m * l, false, F);
 }
@@ -493,6 +530,8 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
                       const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                       WsCursor &cur)
 {
+    if (m <= n && cfg->precision == IA_PREC_MIXED)
+        return wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;
@@ -506,8 +545,9 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
     return regularize_batched(ctx, m, n, p, F, U, s, V, nrhs, b, cfg, x, lambda);
 }
 
-static size_t solve_ws_bytes(int m, int n, int F, int nrhs)
+static size_t solve_ws_bytes(int m, int n, int F, int nrhs, const ia_config *cfg)
 {
+    if (m <= n && cfg->precision == IA_PREC_MIXED) return wide_solve_mixed_ws_bytes(m, n, nrhs, F);
     if (m <= n) return wide_solve_ws_bytes(m, n, nrhs, F);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;
@@ -520,7 +560,7 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
                    const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info)
 {
     if (!ctx || !cfg || m < 1 || n < 1 || F < 1 || nrhs < 1 || !d_H || !d_b || !d_x || !d_info) return IA_ERR_ARG;
-    int st = ws_reserve(ctx, solve_ws_bytes(m, n, F, nrhs));
+    int st = ws_reserve(ctx, solve_ws_bytes(m, n, F, nrhs, cfg));
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
@@ -535,8 +575,10 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     if (!ctx || !mesh || !cfg || l < 1 || F < 1 || nrhs < 1 || !d_mics || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
     const int m = mesh->m;
+    const bool mixed = cfg->precision == IA_PREC_MIXED;
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs);
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
+                  (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
@@ -546,7 +588,8 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     int *ipiv = cur.take<int>((size_t)m * F);
     double2 *Ahs = cur.take<double2>((size_t)m * l * F);
     double2 *Ht = cur.take<double2>((size_t)m * l * F);
-    st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
+    if (mixed) st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info, cur);
+    else st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
     if (st) return st;
     return solve_core(ctx, l, m, F, Ht, true, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
                       cur);
@@ -558,7 +601,7 @@ int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, cons
 {
     if (!ctx || !cfg || l < 1 || m < 1 || F < 1 || nrhs < 1 || !d_mics || !d_src || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
-    size_t need = ws_round(sizeof(double2) * (size_t)l * m * F) + solve_ws_bytes(l, m, F, nrhs);
+    size_t need = ws_round(sizeof(double2) * (size_t)l * m * F) + solve_ws_bytes(l, m, F, nrhs, cfg);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
@@ -577,7 +620,7 @@ int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, i
     if (!ctx || !cfg || l < 1 || n_sh < 0 || F < 1 || nrhs < 1 || !d_pts || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
     const int nt = (n_sh + 1) * (n_sh + 1);
-    size_t need = ws_round(sizeof(double2) * (size_t)l * nt * F) + solve_ws_bytes(l, nt, F, nrhs);
+    size_t need = ws_round(sizeof(double2) * (size_t)l * nt * F) + solve_ws_bytes(l, nt, F, nrhs, cfg);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;

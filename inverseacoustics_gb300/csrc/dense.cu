@@ -1,9 +1,11 @@
-// Batched complex FP64 dense kernels: GEMM, LU with partial pivoting,
-// triangular solves, transposes.  These replace the reference's cuBLAS /
-// cuSOLVER / LAPACK calls on the hot path (cusolverDnZZgels CUDA/ibem.cuh:391,
-// CUDA/esm.cuh:75; zgels_ CUDA/ibem.cuh:755; cublasZgemm CUDA/ibem.cuh:398;
-// cublasZgeam CUDA/esm.cuh:79).  Every launch covers the whole frequency batch
-// (grid.z or grid.x = batch).
+// Batched complex dense kernels: GEMM, LU with partial pivoting, triangular
+// solves, transposes -- templated on the element type (double2 for the FP64
+// path, float2 for the FP32 stages of the mixed path).  These replace the
+// reference's cuBLAS / cuSOLVER / LAPACK calls on the hot path
+// (cusolverDnZZgels CUDA/ibem.cuh:391, CUDA/esm.cuh:75; zgels_
+// CUDA/ibem.cuh:755; cublasZgemm CUDA/ibem.cuh:398; cublasZgeam
+// CUDA/esm.cuh:79).  Every launch covers the whole frequency batch (grid.z or
+// grid.x = batch).
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -15,37 +17,38 @@ namespace ia {
 // --------------------------------------------------------------------------
 constexpr int GB_M = 64, GB_N = 64, GB_K = 8;
 
-__device__ __forceinline__ double2 ld_op(const double2 *P, int ld, int r, int c, int R, int Cc, int op)
+template <class T>
+__device__ __forceinline__ T ld_op(const T *P, int ld, int r, int c, int R, int Cc, int op)
 {
     // element (r, c) of op(P) where op(P) is R x Cc
-    if (r >= R || c >= Cc) return make_double2(0.0, 0.0);
+    if (r >= R || c >= Cc) return ctraits<T>::make(0, 0);
     if (op == OP_N) return P[r + (size_t)c * ld];
-    double2 v = P[c + (size_t)r * ld];
+    T v = P[c + (size_t)r * ld];
     if (op == OP_C) v.y = -v.y;
     return v;
 }
 
-__global__ void __launch_bounds__(256) zgemm_kernel(int opa, int opb, int M, int N, int K, double2 alpha,
-                                                    const double2 *__restrict__ A, int lda, long long sA,
-                                                    const double2 *__restrict__ B, int ldb, long long sB,
-                                                    double2 beta, double2 *__restrict__ C, int ldc, long long sC)
+template <class T>
+__global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int N, int K, T alpha,
+                                                   const T *__restrict__ A, int lda, long long sA,
+                                                   const T *__restrict__ B, int ldb, long long sB, T beta,
+                                                   T *__restrict__ C, int ldc, long long sC)
 {
-    __shared__ double2 As[GB_K][GB_M];
-    __shared__ double2 Bs[GB_K][GB_N];
+    __shared__ T As[GB_K][GB_M];
+    __shared__ T Bs[GB_K][GB_N];
     const int f = blockIdx.z;
     A += f * sA;
     B += f * sB;
     C += f * sC;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-    double2 acc[4][4];
+    T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+        for (int j = 0; j < 4; ++j) acc[i][j] = ctraits<T>::make(0, 0);
 
     for (int k0 = 0; k0 < K; k0 += GB_K) {
-        // A tile: GB_M x GB_K = 512 elements, 2 per thread
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
             int e = threadIdx.x + t * 256;
@@ -65,7 +68,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int opa, int opb, int M, int
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < GB_K; ++kk) {
-            double2 a[4], b[4];
+            T a[4], b[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -77,7 +80,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int opa, int opb, int M, int
         }
         __syncthreads();
     }
-    const bool beta0 = (beta.x == 0.0 && beta.y == 0.0);
+    const bool beta0 = (beta.x == 0 && beta.y == 0);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         int r = m0 + ty + 16 * i;
@@ -86,21 +89,21 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int opa, int opb, int M, int
         for (int j = 0; j < 4; ++j) {
             int c = n0 + tx + 16 * j;
             if (c >= N) continue;
-            double2 v = zmul(alpha, acc[i][j]);
-            double2 *p = C + r + (size_t)c * ldc;
+            T v = zmul(alpha, acc[i][j]);
+            T *p = C + r + (size_t)c * ldc;
             if (!beta0) v = zadd(v, zmul(beta, *p));
             *p = v;
         }
     }
 }
 
-int zgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
-                  long long sA, const double2 *B, int ldb, long long sB, double2 beta, double2 *C, int ldc,
-                  long long sC, int batch)
+template <class T>
+int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda, long long sA,
+                 const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch)
 {
     if (M <= 0 || N <= 0 || batch <= 0) return IA_OK;
     dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch);
-    zgemm_kernel<<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    gemm_kernel<T><<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
@@ -109,15 +112,17 @@ int zgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double2 
 // LU with partial pivoting (LAPACK zgetrf semantics: pivot = largest
 // |re|+|im| in the column, first index on ties; row interchanges applied to
 // whole rows; ipiv 0-based).  Blocked right-looking: panel (one CTA per
-// matrix), U12 = L11^-1 A12 (trsm), A22 -= L21 U12 (zgemm).
+// matrix), U12 = L11^-1 A12 (trsm), A22 -= L21 U12 (gemm).
 // --------------------------------------------------------------------------
 constexpr int LU_NB = 32;
 constexpr int PANEL_THREADS = 256;
 
-__global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, double2 *A, int lda, long long sA,
-                                                                   int *ipiv, int k0, int kend, int *info)
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, T *A, int lda, long long sA, int *ipiv,
+                                                                   int k0, int kend, int *info)
 {
-    __shared__ double sval[PANEL_THREADS / 32];
+    typedef typename ctraits<T>::R R;
+    __shared__ R sval[PANEL_THREADS / 32];
     __shared__ int sidx[PANEL_THREADS / 32];
     __shared__ int s_piv;
     const int f = blockIdx.x;
@@ -125,28 +130,28 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, double2 
     ipiv += (size_t)f * n;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int j = k0; j < kend; ++j) {
-        double best = -1.0;
+        R best = -1;
         int bi = n;
         for (int i = j + tid; i < n; i += PANEL_THREADS) {
-            double2 a = A[i + (size_t)j * lda];
-            double v = fabs(a.x) + fabs(a.y);
+            T a = A[i + (size_t)j * lda];
+            R v = fabs(a.x) + fabs(a.y);
             if (v > best) { best = v; bi = i; }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            R ov = __shfl_xor_sync(0xffffffffu, best, o);
             int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
         }
         if (lane == 0) { sval[wid] = best; sidx[wid] = bi; }
         __syncthreads();
         if (tid == 0) {
-            double bv = sval[0];
+            R bv = sval[0];
             int bidx = sidx[0];
             for (int w = 1; w < PANEL_THREADS / 32; ++w)
                 if (sval[w] > bv || (sval[w] == bv && sidx[w] < bidx)) { bv = sval[w]; bidx = sidx[w]; }
-            if (!(bv > 0.0)) {
-                if (!(bv == 0.0)) info[f] |= IA_INFO_NONFINITE;
+            if (!(bv > 0)) {
+                if (!(bv == 0)) info[f] |= IA_INFO_NONFINITE;
                 else info[f] |= IA_INFO_SINGULAR;
                 bidx = j;
             }
@@ -157,15 +162,15 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, double2 
         const int piv = s_piv;
         if (piv != j) {
             for (int c = tid; c < n; c += PANEL_THREADS) {
-                double2 t = A[j + (size_t)c * lda];
+                T t = A[j + (size_t)c * lda];
                 A[j + (size_t)c * lda] = A[piv + (size_t)c * lda];
                 A[piv + (size_t)c * lda] = t;
             }
         }
         __syncthreads();
-        double2 d = A[j + (size_t)j * lda];
-        if (d.x != 0.0 || d.y != 0.0) {
-            double2 inv = zdiv(make_double2(1.0, 0.0), d);
+        T d = A[j + (size_t)j * lda];
+        if (d.x != 0 || d.y != 0) {
+            T inv = zdiv(ctraits<T>::make(1, 0), d);
             for (int i = j + 1 + tid; i < n; i += PANEL_THREADS)
                 A[i + (size_t)j * lda] = zmul(A[i + (size_t)j * lda], inv);
         }
@@ -174,7 +179,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, double2 
         for (int idx = tid; idx < rows * ncols; idx += PANEL_THREADS) {
             int r = j + 1 + idx % rows;
             int c = j + 1 + idx / rows;
-            double2 v = A[r + (size_t)c * lda];
+            T v = A[r + (size_t)c * lda];
             zfms(v, A[r + (size_t)j * lda], A[j + (size_t)c * lda]);
             A[r + (size_t)c * lda] = v;
         }
@@ -184,22 +189,22 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, double2 
 
 // Solve T X = X in place for an nbk x nbk diagonal block T (lower unit or
 // upper non-unit) and X = nbk x ncols; one thread per column.
-template <bool UPPER>
-__global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const double2 *T, int ldt, long long sT,
-                                                           double2 *X, int ldx, long long sX, int ncols)
+template <class T, bool UPPER>
+__global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const T *Tm, int ldt, long long sT, T *X, int ldx,
+                                                           long long sX, int ncols)
 {
-    __shared__ double2 Ts[LU_NB][LU_NB + 1];
+    __shared__ T Ts[LU_NB][LU_NB + 1];
     const int f = blockIdx.y;
-    T += f * sT;
+    Tm += f * sT;
     X += f * sX;
     for (int e = threadIdx.x; e < nbk * nbk; e += blockDim.x) {
         int r = e % nbk, c = e / nbk;
-        Ts[r][c] = T[r + (size_t)c * ldt];
+        Ts[r][c] = Tm[r + (size_t)c * ldt];
     }
     __syncthreads();
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= ncols) return;
-    double2 x[LU_NB];
+    T x[LU_NB];
 #pragma unroll
     for (int r = 0; r < LU_NB; ++r)
         if (r < nbk) x[r] = X[r + (size_t)col * ldx];
@@ -207,7 +212,7 @@ __global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const double2 
 #pragma unroll
         for (int r = 0; r < LU_NB; ++r) {
             if (r >= nbk) break;
-            double2 v = x[r];
+            T v = x[r];
 #pragma unroll
             for (int t = 0; t < LU_NB; ++t)
                 if (t < r) zfms(v, Ts[r][t], x[t]);
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const double2 
 #pragma unroll
         for (int r = LU_NB - 1; r >= 0; --r) {
             if (r >= nbk) continue;
-            double2 v = x[r];
+            T v = x[r];
 #pragma unroll
             for (int t = 0; t < LU_NB; ++t)
                 if (t > r && t < nbk) zfms(v, Ts[r][t], x[t]);
@@ -229,97 +234,102 @@ __global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const double2 
         if (r < nbk) X[r + (size_t)col * ldx] = x[r];
 }
 
-int zgetrf_batched(ia_context *ctx, int n, double2 *A, int lda, long long sA, int *ipiv, int *info, int batch)
+template <class T>
+int getrf_batched(ia_context *ctx, int n, T *A, int lda, long long sA, int *ipiv, int *info, int batch)
 {
+    const T one = ctraits<T>::make(1, 0), mone = ctraits<T>::make(-1, 0);
     for (int k0 = 0; k0 < n; k0 += LU_NB) {
         int kend = k0 + LU_NB < n ? k0 + LU_NB : n;
         int nb = kend - k0;
-        lu_panel_kernel<<<batch, PANEL_THREADS, 0, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend, info);
+        lu_panel_kernel<T><<<batch, PANEL_THREADS, 0, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend, info);
         IA_LAUNCH_CHECK(ctx);
         int rest = n - kend;
         if (rest <= 0) break;
         dim3 g((rest + 127) / 128, batch);
-        trsm_block_kernel<false><<<g, 128, 0, ctx->stream>>>(nb, A + k0 + (size_t)k0 * lda, lda, sA,
-                                                              A + k0 + (size_t)kend * lda, lda, sA, rest);
+        trsm_block_kernel<T, false><<<g, 128, 0, ctx->stream>>>(nb, A + k0 + (size_t)k0 * lda, lda, sA,
+                                                                 A + k0 + (size_t)kend * lda, lda, sA, rest);
         IA_LAUNCH_CHECK(ctx);
-        int r = zgemm_batched(ctx, OP_N, OP_N, rest, rest, nb, make_double2(-1.0, 0.0), A + kend + (size_t)k0 * lda,
-                              lda, sA, A + k0 + (size_t)kend * lda, lda, sA, make_double2(1.0, 0.0),
-                              A + kend + (size_t)kend * lda, lda, sA, batch);
+        int r = gemm_batched<T>(ctx, OP_N, OP_N, rest, rest, nb, mone, A + kend + (size_t)k0 * lda, lda, sA,
+                                A + k0 + (size_t)kend * lda, lda, sA, one, A + kend + (size_t)kend * lda, lda, sA,
+                                batch);
         if (r) return r;
     }
     return IA_OK;
 }
 
-__global__ void apply_pivots_kernel(int n, int nrhs, const int *ipiv, double2 *B, int ldb, long long sB)
+template <class T>
+__global__ void apply_pivots_kernel(int n, int nrhs, const int *ipiv, T *B, int ldb, long long sB)
 {
     const int f = blockIdx.y;
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= nrhs) return;
     ipiv += (size_t)f * n;
-    double2 *b = B + f * sB + (size_t)col * ldb;
+    T *b = B + f * sB + (size_t)col * ldb;
     for (int j = 0; j < n; ++j) {
         int p = ipiv[j];
         if (p != j) {
-            double2 t = b[j];
+            T t = b[j];
             b[j] = b[p];
             b[p] = t;
         }
     }
 }
 
-int zgetrs_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, const int *ipiv,
-                   double2 *B, int ldb, long long sB, int batch)
+template <class T>
+int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long long sA, T *B, int ldb,
+                            long long sB, int batch)
 {
-    dim3 gp((nrhs + 127) / 128, batch);
-    apply_pivots_kernel<<<gp, 128, 0, ctx->stream>>>(n, nrhs, ipiv, B, ldb, sB);
-    IA_LAUNCH_CHECK(ctx);
+    const T one = ctraits<T>::make(1, 0), mone = ctraits<T>::make(-1, 0);
     dim3 g((nrhs + 127) / 128, batch);
-    // forward: L Y = B
-    for (int k0 = 0; k0 < n; k0 += LU_NB) {
-        int kend = k0 + LU_NB < n ? k0 + LU_NB : n;
-        int nb = kend - k0;
-        trsm_block_kernel<false><<<g, 128, 0, ctx->stream>>>(nb, LU + k0 + (size_t)k0 * lda, lda, sA, B + k0, ldb, sB,
-                                                              nrhs);
-        IA_LAUNCH_CHECK(ctx);
-        if (kend < n) {
-            int r = zgemm_batched(ctx, OP_N, OP_N, n - kend, nrhs, nb, make_double2(-1.0, 0.0),
-                                  LU + kend + (size_t)k0 * lda, lda, sA, B + k0, ldb, sB, make_double2(1.0, 0.0),
-                                  B + kend, ldb, sB, batch);
-            if (r) return r;
-        }
-    }
-    return zbacksolve_upper_batched(ctx, n, nrhs, LU, lda, sA, B, ldb, sB, batch);
-}
-
-int zbacksolve_upper_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, double2 *B,
-                             int ldb, long long sB, int batch)
-{
-    dim3 g((nrhs + 127) / 128, batch);
-    // backward: U X = Y
     int nblk = (n + LU_NB - 1) / LU_NB;
     for (int bi = nblk - 1; bi >= 0; --bi) {
         int k0 = bi * LU_NB;
         int kend = k0 + LU_NB < n ? k0 + LU_NB : n;
         int nb = kend - k0;
-        trsm_block_kernel<true><<<g, 128, 0, ctx->stream>>>(nb, LU + k0 + (size_t)k0 * lda, lda, sA, B + k0, ldb, sB,
-                                                             nrhs);
+        trsm_block_kernel<T, true><<<g, 128, 0, ctx->stream>>>(nb, LU + k0 + (size_t)k0 * lda, lda, sA, B + k0, ldb,
+                                                                sB, nrhs);
         IA_LAUNCH_CHECK(ctx);
         if (k0 > 0) {
-            int r = zgemm_batched(ctx, OP_N, OP_N, k0, nrhs, nb, make_double2(-1.0, 0.0), LU + (size_t)k0 * lda, lda,
-                                  sA, B + k0, ldb, sB, make_double2(1.0, 0.0), B, ldb, sB, batch);
+            int r = gemm_batched<T>(ctx, OP_N, OP_N, k0, nrhs, nb, mone, LU + (size_t)k0 * lda, lda, sA, B + k0, ldb,
+                                    sB, one, B, ldb, sB, batch);
             if (r) return r;
         }
     }
     return IA_OK;
 }
 
+template <class T>
+int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long long sA, const int *ipiv, T *B,
+                  int ldb, long long sB, int batch)
+{
+    const T one = ctraits<T>::make(1, 0), mone = ctraits<T>::make(-1, 0);
+    dim3 g((nrhs + 127) / 128, batch);
+    apply_pivots_kernel<T><<<g, 128, 0, ctx->stream>>>(n, nrhs, ipiv, B, ldb, sB);
+    IA_LAUNCH_CHECK(ctx);
+    // forward: L Y = B
+    for (int k0 = 0; k0 < n; k0 += LU_NB) {
+        int kend = k0 + LU_NB < n ? k0 + LU_NB : n;
+        int nb = kend - k0;
+        trsm_block_kernel<T, false><<<g, 128, 0, ctx->stream>>>(nb, LU + k0 + (size_t)k0 * lda, lda, sA, B + k0, ldb,
+                                                                 sB, nrhs);
+        IA_LAUNCH_CHECK(ctx);
+        if (kend < n) {
+            int r = gemm_batched<T>(ctx, OP_N, OP_N, n - kend, nrhs, nb, mone, LU + kend + (size_t)k0 * lda, lda, sA,
+                                    B + k0, ldb, sB, one, B + kend, ldb, sB, batch);
+            if (r) return r;
+        }
+    }
+    return backsolve_upper_batched<T>(ctx, n, nrhs, LU, lda, sA, B, ldb, sB, batch);
+}
+
 // --------------------------------------------------------------------------
 // transposes / copies through a 32x32 shared tile
 // --------------------------------------------------------------------------
-__global__ void transpose_kernel(int rows, int cols, const double2 *in, int ldi, long long si, double2 *out, int ldo,
-                                 long long so, int conj)
+template <class T>
+__global__ void transpose_kernel(int rows, int cols, const T *in, int ldi, long long si, T *out, int ldo, long long so,
+                                 int conj)
 {
-    __shared__ double2 tile[32][33];
+    __shared__ T tile[32][33];
     const int f = blockIdx.z;
     in += f * si;
     out += f * so;
@@ -332,46 +342,103 @@ __global__ void transpose_kernel(int rows, int cols, const double2 *in, int ldi,
     for (int t = threadIdx.y; t < 32; t += blockDim.y) {
         int oc = r0 + t, orow = c0 + threadIdx.x;  // out(orow, oc) = in(oc, orow)
         if (oc < rows && orow < cols) {
-            double2 v = tile[threadIdx.x][t];
+            T v = tile[threadIdx.x][t];
             if (conj) v.y = -v.y;
             out[orow + (size_t)oc * ldo] = v;
         }
     }
 }
 
-int ztranspose_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
-                       int ldo, long long so, bool conj, int batch)
+template <class T>
+int transpose_batched(ia_context *ctx, int rows, int cols, const T *in, int ldi, long long si, T *out, int ldo,
+                      long long so, bool conj, int batch)
 {
     dim3 g((cols + 31) / 32, (rows + 31) / 32, batch);
-    transpose_kernel<<<g, dim3(32, 8), 0, ctx->stream>>>(rows, cols, in, ldi, si, out, ldo, so, conj ? 1 : 0);
+    transpose_kernel<T><<<g, dim3(32, 8), 0, ctx->stream>>>(rows, cols, in, ldi, si, out, ldo, so, conj ? 1 : 0);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
 
-__global__ void copy2d_kernel(int rows, int cols, const double2 *in, int ldi, long long si, double2 *out, int ldo,
-                              long long so, int conj)
+// 2-D copy with optional conjugation and element-type conversion
+template <class TI, class TO>
+__global__ void copy2d_kernel(int rows, int cols, const TI *in, int ldi, long long si, TO *out, int ldo, long long so,
+                              int conj)
+{
+    typedef typename ctraits<TO>::R RO;
+    const int f = blockIdx.y;
+    long long total = (long long)rows * cols;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int r = (int)(e % rows), c = (int)(e / rows);
+        TI v = in[f * si + r + (size_t)c * ldi];
+        out[f * so + r + (size_t)c * ldo] = ctraits<TO>::make((RO)v.x, conj ? -(RO)v.y : (RO)v.y);
+    }
+}
+
+template <class TI, class TO>
+int copy2d_batched(ia_context *ctx, int rows, int cols, const TI *in, int ldi, long long si, TO *out, int ldo,
+                   long long so, bool conj, int batch)
+{
+    long long total = (long long)rows * cols;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 1024) blocks = 1024;
+    dim3 g(blocks, batch);
+    copy2d_kernel<TI, TO><<<g, 256, 0, ctx->stream>>>(rows, cols, in, ldi, si, out, ldo, so, conj ? 1 : 0);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+template <class TI>
+__global__ void add2d_kernel(int rows, int cols, const TI *in, int ldi, long long si, double2 *out, int ldo,
+                             long long so)
 {
     const int f = blockIdx.y;
     long long total = (long long)rows * cols;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         int r = (int)(e % rows), c = (int)(e / rows);
-        double2 v = in[f * si + r + (size_t)c * ldi];
-        if (conj) v.y = -v.y;
-        out[f * so + r + (size_t)c * ldo] = v;
+        TI v = in[f * si + r + (size_t)c * ldi];
+        double2 *o = out + f * so + r + (size_t)c * ldo;
+        *o = make_double2(o->x + (double)v.x, o->y + (double)v.y);
     }
 }
 
-int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
-                    int ldo, long long so, bool conj, int batch)
+template <class TI>
+int add2d_batched(ia_context *ctx, int rows, int cols, const TI *in, int ldi, long long si, double2 *out, int ldo,
+                  long long so, int batch)
 {
     long long total = (long long)rows * cols;
     int blocks = (int)((total + 255) / 256);
     if (blocks > 1024) blocks = 1024;
-    dim3 g(blocks, batch);
-    copy2d_kernel<<<g, 256, 0, ctx->stream>>>(rows, cols, in, ldi, si, out, ldo, so, conj ? 1 : 0);
+    add2d_kernel<TI><<<dim3(blocks, batch), 256, 0, ctx->stream>>>(rows, cols, in, ldi, si, out, ldo, so);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
+template int add2d_batched<float2>(ia_context *, int, int, const float2 *, int, long long, double2 *, int, long long,
+                                   int);
+template int add2d_batched<double2>(ia_context *, int, int, const double2 *, int, long long, double2 *, int,
+                                    long long, int);
+
+// ---- instantiations ------------------------------------------------------
+#define IA_DENSE_INST(T)                                                                                              \
+    template int gemm_batched<T>(ia_context *, Op, Op, int, int, int, T, const T *, int, long long, const T *, int,   \
+                                 long long, T, T *, int, long long, int);                                            \
+    template int getrf_batched<T>(ia_context *, int, T *, int, long long, int *, int *, int);                         \
+    template int getrs_batched<T>(ia_context *, int, int, const T *, int, long long, const int *, T *, int, long long, \
+                                  int);                                                                               \
+    template int backsolve_upper_batched<T>(ia_context *, int, int, const T *, int, long long, T *, int, long long,    \
+                                            int);                                                                     \
+    template int transpose_batched<T>(ia_context *, int, int, const T *, int, long long, T *, int, long long, bool,   \
+                                      int);
+IA_DENSE_INST(double2)
+IA_DENSE_INST(float2)
+template int copy2d_batched<double2, double2>(ia_context *, int, int, const double2 *, int, long long, double2 *, int,
+                                              long long, bool, int);
+template int copy2d_batched<float2, float2>(ia_context *, int, int, const float2 *, int, long long, float2 *, int,
+                                            long long, bool, int);
+template int copy2d_batched<double2, float2>(ia_context *, int, int, const double2 *, int, long long, float2 *, int,
+                                             long long, bool, int);
+template int copy2d_batched<float2, double2>(ia_context *, int, int, const float2 *, int, long long, double2 *, int,
+                                             long long, bool, int);
 
 }  // namespace ia

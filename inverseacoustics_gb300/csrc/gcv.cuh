@@ -145,8 +145,8 @@ __device__ __forceinline__ double gcv_grid_point(bool fixed, double lhi, double 
 // Whole-CTA lambda selection.  s (descending), b2 = |beta|^2 in shared
 // memory; gval: shared scratch of cfg.gcv_points doubles.  Returns lambda
 // (the same value in every thread).
-__device__ double select_lambda(const double *s, const double *b2, int p, double delta0, double dof,
-                                const ia_config &cfg, double *gval)
+static __device__ double select_lambda(const double *s, const double *b2, int p, double delta0, double dof,
+                                       const ia_config &cfg, double *gval)
 {
     __shared__ double s_lam;
     __shared__ int s_jmin;

@@ -82,6 +82,69 @@ __device__ __forceinline__ double2 warp_sum2(double2 v)
     return v;
 }
 
+// ---- single-precision complex (float2) overloads of the same helpers
+__host__ __device__ __forceinline__ float2 zadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 zsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 zmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 zscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 zconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float zabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ void zfma(float2 &acc, float2 a, float2 b)
+{
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ void zfms(float2 &acc, float2 a, float2 b)
+{
+    acc.x = fmaf(-a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(-a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+}
+__device__ __forceinline__ void zcfma(float2 &acc, float2 a, float2 b)
+{
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+}
+__device__ __forceinline__ float2 zdiv(float2 a, float2 b)
+{
+    float s = 1.0f / (b.x * b.x + b.y * b.y);
+    return make_float2((a.x * b.x + a.y * b.y) * s, (a.y * b.x - a.x * b.y) * s);
+}
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float2 warp_sum2(float2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// complex element type -> real type, constructor
+template <class T> struct ctraits;
+template <> struct ctraits<double2> {
+    typedef double R;
+    __host__ __device__ static double2 make(double r, double i) { return make_double2(r, i); }
+};
+template <> struct ctraits<float2> {
+    typedef float R;
+    __host__ __device__ static float2 make(float r, float i) { return make_float2(r, i); }
+};
+
 // exp(i*t) / r
 __device__ __forceinline__ double2 green(double kr, double invr)
 {

@@ -62,30 +62,73 @@ inline size_t ws_round(size_t b) { return (b + 255) & ~size_t(255); }
 
 // ---- dense kernels (dense.cu)
 enum Op { OP_N = 0, OP_T = 1, OP_C = 2 };
-int zgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
-                  long long sA, const double2 *B, int ldb, long long sB, double2 beta, double2 *C, int ldc,
-                  long long sC, int batch);
-int zgetrf_batched(ia_context *ctx, int n, double2 *A, int lda, long long sA, int *ipiv, int *info, int batch);
-int zgetrs_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, const int *ipiv,
-                   double2 *B, int ldb, long long sB, int batch);
+// T = double2 (FP64) or float2 (FP32); instantiated in dense.cu
+template <class T>
+int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda, long long sA,
+                 const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch);
+template <class T>
+int getrf_batched(ia_context *ctx, int n, T *A, int lda, long long sA, int *ipiv, int *info, int batch);
+template <class T>
+int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long long sA, const int *ipiv, T *B,
+                  int ldb, long long sB, int batch);
 // X = U^-1 X for the upper triangle of LU (n x n), X n x nrhs
-int zbacksolve_upper_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, double2 *B,
-                             int ldb, long long sB, int batch);
+template <class T>
+int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long long sA, T *B, int ldb,
+                            long long sB, int batch);
+// out[f] (cols x rows) = op(in[f]) (rows x cols), transposed, optionally conjugated
+template <class T>
+int transpose_batched(ia_context *ctx, int rows, int cols, const T *in, int ldi, long long si, T *out, int ldo,
+                      long long so, bool conj, int batch);
+// out = in (optionally conjugated), converting the element type
+template <class TI, class TO>
+int copy2d_batched(ia_context *ctx, int rows, int cols, const TI *in, int ldi, long long si, TO *out, int ldo,
+                   long long so, bool conj, int batch);
+
+inline int zgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double2 alpha, const double2 *A,
+                         int lda, long long sA, const double2 *B, int ldb, long long sB, double2 beta, double2 *C,
+                         int ldc, long long sC, int batch)
+{
+    return gemm_batched<double2>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
+}
+inline int zgetrf_batched(ia_context *ctx, int n, double2 *A, int lda, long long sA, int *ipiv, int *info, int batch)
+{
+    return getrf_batched<double2>(ctx, n, A, lda, sA, ipiv, info, batch);
+}
+inline int zgetrs_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA, const int *ipiv,
+                          double2 *B, int ldb, long long sB, int batch)
+{
+    return getrs_batched<double2>(ctx, n, nrhs, LU, lda, sA, ipiv, B, ldb, sB, batch);
+}
+inline int zbacksolve_upper_batched(ia_context *ctx, int n, int nrhs, const double2 *LU, int lda, long long sA,
+                                    double2 *B, int ldb, long long sB, int batch)
+{
+    return backsolve_upper_batched<double2>(ctx, n, nrhs, LU, lda, sA, B, ldb, sB, batch);
+}
+inline int ztranspose_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si,
+                              double2 *out, int ldo, long long so, bool conj, int batch)
+{
+    return transpose_batched<double2>(ctx, rows, cols, in, ldi, si, out, ldo, so, conj, batch);
+}
+inline int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
+                           int ldo, long long so, bool conj, int batch)
+{
+    return copy2d_batched<double2, double2>(ctx, rows, cols, in, ldi, si, out, ldo, so, conj, batch);
+}
 // Householder QR of A (rows x cols, rows >= cols) applied to [A | B] in place:
 // on exit the upper triangle of A is R and B holds Q^H B.
 int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
                    int ldb, long long sB, int batch);
-// out[f] (cols x rows) = op(in[f]) (rows x cols), op in {T, C}; or copy/conj when transpose=false
-int ztranspose_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
-                       int ldo, long long so, bool conj, int batch);
-int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *in, int ldi, long long si, double2 *out,
-                    int ldo, long long so, bool conj, int batch);
+
+// C = alpha A B + beta C with FP64 inputs and output, products and sums in
+// double-float (FP32 pairs) arithmetic (dfgemm.cu); op(A) = op(B) = N
+int dfgemm_batched(ia_context *ctx, int M, int N, int K, double alpha, const double2 *A, int lda, long long sA,
+                   const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc, long long sC, int batch);
 
 // ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);
 // Jacobi on Y (M x N) with only the first Mdot rows in the dot products
-int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, double2 *Y, double2 *V, int batch, int max_sweeps,
-                        int *info);
+template <class T>
+int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int batch, int max_sweeps, int *info);
 // sigma, normalised sorted outputs: Uy (M x N) <- Y/sigma, Vs (N x N) <- V, both column-permuted to
 // descending sigma.  Either output may be null.
 int svd_finalize_batched(ia_context *ctx, int M, int N, const double2 *Y, const double2 *V, double *s,
@@ -114,6 +157,15 @@ size_t wide_solve_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                        const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                        WsCursor &cur);
+// mixed: QR / Jacobi / GCV in FP32, x by FP64 iterative refinement against A
+size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch);
+int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
+                             const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
+                             int *info, WsCursor &cur);
+// out += in (FP32 or FP64 in, FP64 out), rows x cols per matrix
+template <class TI>
+int add2d_batched(ia_context *ctx, int rows, int cols, const TI *in, int ldi, long long si, double2 *out, int ldo,
+                  long long so, int batch);
 
 // ---- assembly (assemble.cu)
 int monopole_batched(ia_context *ctx, int l, int m, int F, const double *mics, const double *src, const double *k,

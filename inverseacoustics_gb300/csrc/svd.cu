@@ -1,4 +1,5 @@
-// Batched one-sided (Hestenes) Jacobi SVD in FP64, one CTA per frequency.
+// Batched one-sided (Hestenes) Jacobi SVD, one CTA per frequency, templated
+// on the element type (double2 for the FP64 path, float2 for the mixed path).
 //
 // Replaces cusolverDnZgesvd in csvd() (CUDA/tsvd.cuh:39,93) and the MATLAB
 // svd() behind csvdG.m:17-24.  The columns of Y (M x N, M >= N) are
@@ -33,32 +34,45 @@ __device__ __forceinline__ void rr_pair(int N2, int round, int k, int &i, int &j
 }
 
 // Rotation that zeroes y_i^H y_j for column norms a, b and product g.
-__device__ __forceinline__ bool jacobi_rotation(double a, double b, double2 g, double tol, double &c, double2 &sp)
+template <class T, class R>
+__device__ __forceinline__ bool jacobi_rotation(R a, R b, T g, R tol, R &c, T &sp)
 {
-    double gm = sqrt(g.x * g.x + g.y * g.y);
-    if (!(gm > tol * sqrt(a) * sqrt(b)) || gm == 0.0) return false;
-    double zeta = (b - a) / (2.0 * gm);
-    double t;
-    if (fabs(zeta) > 1e150) t = 0.5 / zeta;
-    else t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-    c = 1.0 / sqrt(1.0 + t * t);
-    double s = t * c;
-    sp = make_double2(s * g.x / gm, s * g.y / gm);   // s' = s e^{i arg gamma}
+    R gm = sqrt(g.x * g.x + g.y * g.y);
+    if (!(gm > tol * sqrt(a) * sqrt(b)) || gm == 0) return false;
+    R zeta = (b - a) / (2 * gm);
+    R t;
+    if (fabs(zeta) > (R)1e30) t = (R)0.5 / zeta;
+    else t = (zeta >= 0 ? (R)1 : (R)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+    c = 1 / sqrt(1 + t * t);
+    R s = t * c;
+    sp = ctraits<T>::make(s * g.x / gm, s * g.y / gm);   // s' = s e^{i arg gamma}
     return true;
 }
 
-// KPL > 0: rows cached in registers (M <= 32*KPL); KPL == 0: streamed.
-template <int KPL>
-__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int Mdot, int N, double2 *Y, long long sY,
-                                                                      double2 *V, long long sV, int max_sweeps,
-                                                                      double tol, int *info)
+template <class T>
+__device__ __forceinline__ void rotate_pair(T &u, T &v, typename ctraits<T>::R c, T sp)
 {
+    T nu = zscale(u, c), nv = zscale(v, c);
+    zfms(nu, zconj(sp), v);
+    zfma(nv, sp, u);
+    u = nu;
+    v = nv;
+}
+
+// KPL > 0: rows cached in registers (M <= 32*KPL); KPL == 0: streamed.
+template <class T, int KPL>
+__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int Mdot, int N, T *Y, long long sY, T *V,
+                                                                      long long sV, int max_sweeps,
+                                                                      typename ctraits<T>::R tol, int *info)
+{
+    typedef typename ctraits<T>::R R;
     __shared__ int s_rot;
     const int f = blockIdx.x;
     Y += f * sY;
     if (V) V += f * sV;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int N2 = N + (N & 1);
+    const T zero = ctraits<T>::make(0, 0);
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         if (threadIdx.x == 0) s_rot = 0;
@@ -69,19 +83,19 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int M
                 int i, j;
                 rr_pair(N2, round, k, i, j);
                 if (j >= N) continue;
-                double2 *yi = Y + (size_t)i * M, *yj = Y + (size_t)j * M;
-                double a = 0.0, b = 0.0, c;
-                double2 g = make_double2(0.0, 0.0), sp;
+                T *yi = Y + (size_t)i * M, *yj = Y + (size_t)j * M;
+                R a = 0, b = 0, c;
+                T g = zero, sp;
                 if (KPL > 0) {
-                    double2 ui[KPL > 0 ? KPL : 1], vj[KPL > 0 ? KPL : 1];
+                    T ui[KPL > 0 ? KPL : 1], vj[KPL > 0 ? KPL : 1];
 #pragma unroll
                     for (int t = 0; t < KPL; ++t) {
                         int r = lane + 32 * t;
-                        ui[t] = r < M ? yi[r] : make_double2(0.0, 0.0);
-                        vj[t] = r < M ? yj[r] : make_double2(0.0, 0.0);
+                        ui[t] = r < M ? yi[r] : zero;
+                        vj[t] = r < M ? yj[r] : zero;
                         if (r < Mdot) {
-                            a = fma(ui[t].x, ui[t].x, fma(ui[t].y, ui[t].y, a));
-                            b = fma(vj[t].x, vj[t].x, fma(vj[t].y, vj[t].y, b));
+                            a += zabs2(ui[t]);
+                            b += zabs2(vj[t]);
                             zcfma(g, ui[t], vj[t]);
                         }
                     }
@@ -89,49 +103,40 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int M
                     b = warp_sum(b);
                     g = warp_sum2(g);
                     if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
-                    const double2 spc = zconj(sp);
 #pragma unroll
                     for (int t = 0; t < KPL; ++t) {
                         int r = lane + 32 * t;
                         if (r < M) {
-                            double2 nu = zscale(ui[t], c), nv = zscale(vj[t], c);
-                            zfms(nu, spc, vj[t]);
-                            zfma(nv, sp, ui[t]);
-                            yi[r] = nu;
-                            yj[r] = nv;
+                            rotate_pair(ui[t], vj[t], c, sp);
+                            yi[r] = ui[t];
+                            yj[r] = vj[t];
                         }
                     }
                 } else {
                     for (int r = lane; r < Mdot; r += 32) {
-                        double2 u = yi[r], v = yj[r];
-                        a = fma(u.x, u.x, fma(u.y, u.y, a));
-                        b = fma(v.x, v.x, fma(v.y, v.y, b));
+                        T u = yi[r], v = yj[r];
+                        a += zabs2(u);
+                        b += zabs2(v);
                         zcfma(g, u, v);
                     }
                     a = warp_sum(a);
                     b = warp_sum(b);
                     g = warp_sum2(g);
                     if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
-                    const double2 spc = zconj(sp);
                     for (int r = lane; r < M; r += 32) {
-                        double2 u = yi[r], v = yj[r];
-                        double2 nu = zscale(u, c), nv = zscale(v, c);
-                        zfms(nu, spc, v);
-                        zfma(nv, sp, u);
-                        yi[r] = nu;
-                        yj[r] = nv;
+                        T u = yi[r], v = yj[r];
+                        rotate_pair(u, v, c, sp);
+                        yi[r] = u;
+                        yj[r] = v;
                     }
                 }
                 if (V) {
-                    const double2 spc = zconj(sp);
-                    double2 *vi = V + (size_t)i * N, *vjp = V + (size_t)j * N;
+                    T *vi = V + (size_t)i * N, *vjp = V + (size_t)j * N;
                     for (int r = lane; r < N; r += 32) {
-                        double2 u = vi[r], v = vjp[r];
-                        double2 nu = zscale(u, c), nv = zscale(v, c);
-                        zfms(nu, spc, v);
-                        zfma(nv, sp, u);
-                        vi[r] = nu;
-                        vjp[r] = nv;
+                        T u = vi[r], v = vjp[r];
+                        rotate_pair(u, v, c, sp);
+                        vi[r] = u;
+                        vjp[r] = v;
                     }
                 }
                 rot_local++;
@@ -147,41 +152,46 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int M
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
 }
 
-__global__ void identity_kernel(int N, double2 *V, long long sV)
+template <class T>
+__global__ void identity_kernel(int N, T *V, long long sV)
 {
     const int f = blockIdx.y;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N * N; e += gridDim.x * blockDim.x) {
         int r = e % N, c = e / N;
-        V[f * sV + e] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+        V[f * sV + e] = ctraits<T>::make(r == c ? 1 : 0, 0);
     }
 }
 
-int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, double2 *Y, double2 *V, int batch, int max_sweeps,
-                        int *info)
+template <class T>
+int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int batch, int max_sweeps, int *info)
 {
+    typedef typename ctraits<T>::R R;
     if (V) {
         dim3 g((N * N + 255) / 256 < 256 ? (N * N + 255) / 256 : 256, batch);
-        identity_kernel<<<g, 256, 0, ctx->stream>>>(N, V, (long long)N * N);
+        identity_kernel<T><<<g, 256, 0, ctx->stream>>>(N, V, (long long)N * N);
         IA_LAUNCH_CHECK(ctx);
     }
     int nw = (N + 1) / 2;
     if (nw > SVD_MAX_WARPS) nw = SVD_MAX_WARPS;
     if (nw < 1) nw = 1;
-    const double tol = sqrt((double)Mdot) * 2.220446049250313e-16;
+    const double eps = sizeof(R) == 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+    const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;
     if (M <= 128)
-        jacobi_kernel<4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+        jacobi_kernel<T, 4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     else if (M <= 256)
-        jacobi_kernel<8><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+        jacobi_kernel<T, 8><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     else
-        jacobi_kernel<0><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+        jacobi_kernel<T, 0><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
+template int jacobi_rows_batched<double2>(ia_context *, int, int, int, double2 *, double2 *, int, int, int *);
+template int jacobi_rows_batched<float2>(ia_context *, int, int, int, float2 *, float2 *, int, int, int *);
 
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info)
 {
-    return jacobi_rows_batched(ctx, M, M, N, Y, V, batch, max_sweeps, info);
+    return jacobi_rows_batched<double2>(ctx, M, M, N, Y, V, batch, max_sweeps, info);
 }
 
 // sigma_j = ||y_j||, descending order (ties by index), U = Y/sigma, V permuted.

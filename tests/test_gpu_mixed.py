@@ -1,0 +1,105 @@
+"""GPU suite: the mixed-precision path (FP32 LU / QR / Jacobi, double-float
+refinement and transfer GEMMs, FP64 Tikhonov refinement) against the FP64
+oracle.  Stated bound: relative error <= 1e-6 on x; H at FP64 level (1e-11)."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from inverseacoustics_gb300 import geometry as g
+from inverseacoustics_gb300 import quadrature as Q
+from oracle import ia_oracle as O
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-6
+
+
+def T(a, dev):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), device=dev)
+
+
+def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
+    from inverseacoustics_gb300 import api
+    import torch
+    w = g.ibem_sphere(n_freq=64)
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    ks = w.k[[2, 53, 54, 63]]          # includes the two bins next to ka = pi
+    mesh = api.Mesh(ctx, nodes, elems)
+    H64, i64 = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
+    Hmx, imx = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), api.default_config(precision=1))
+    torch.cuda.synchronize()
+    assert int(imx.abs().sum()) == 0
+    for f in range(len(ks)):
+        assert relerr(Hmx[f].cpu().numpy(), H64[f].cpu().numpy()) < 1e-11
+
+
+def test_mixed_ibem_pipeline_full_size(cuda, ctx):
+    """Full bench configuration at 8 of its 64 frequencies (two next to the
+    interior resonance): mixed x and lambda against the FP64 oracle."""
+    from inverseacoustics_gb300 import api
+    import torch
+    w = g.ibem_sphere(n_freq=64)
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    idx = [0, 9, 21, 33, 45, 53, 54, 63]
+    ks = w.k[idx]
+    rng = np.random.default_rng(7)
+    p = np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0) +
+                              0.5 * g.oscillating_sphere_pressure(mics, k, 0.1, 1.0), 30.0)[None, :] for k in ks])
+    mesh = api.Mesh(ctx, nodes, elems)
+    cfg = api.default_config(precision=1)
+    x, lam, s, info = api.ibem_solve_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), T(p, cuda), cfg)
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0
+    reg, sing = Q.builtin()
+    for f in (0, 5, 6, 7):
+        H = O.ibem_transfer(nodes, elems, mics, ks[f], reg, sing, 343.0, 1.21)
+        xo, lo, so = O.solve_tikhonov_gcv(H, p[f, 0])
+        assert abs(lam[f, 0].item() - lo) < 1e-5 * lo
+        assert relerr(x[f, 0].cpu().numpy(), xo) < MIXED_TOL
+
+
+def test_mixed_matches_fp64_path_all_bins(cuda, ctx):
+    from inverseacoustics_gb300 import api
+    import torch
+    nodes, elems = g.icosphere(2, 0.1)
+    rng = np.random.default_rng(8)
+    mics = g.hemisphere_array(rng, 60, 0.3)
+    ks = 2 * np.pi * np.linspace(100, 2000, 16) / 343.0
+    p = np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0), 30.0)[None, :] for k in ks])
+    mesh = api.Mesh(ctx, nodes, elems)
+    x6, l6, _, _ = api.ibem_solve_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), T(p, cuda))
+    xm, lm, _, info = api.ibem_solve_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), T(p, cuda),
+                                           api.default_config(precision=1))
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0
+    for f in range(len(ks)):
+        assert relerr(xm[f, 0].cpu().numpy(), x6[f, 0].cpu().numpy()) < MIXED_TOL
+
+
+def test_mixed_esm_and_hels_pipelines(cuda, ctx):
+    from inverseacoustics_gb300 import api
+    import torch
+    rng = np.random.default_rng(9)
+    mics = g.planar_array(8, 8, 0.03, 0.10)
+    src, _ = g.icosphere(2, 0.05)
+    ks = 2 * np.pi * np.array([500.0, 1000.0, 3000.0]) / 343.0
+    p = np.stack([g.add_noise(rng, O.monopole_matrix(mics, src, k) @ g.complex_normal(rng, 162), 30.0)[None, :]
+                  for k in ks])
+    cfg = api.default_config(precision=1, gcv_lo=1e-8, gcv_hi=1e2)
+    x, lam, s, info = api.esm_solve_batch(ctx, T(mics, cuda), T(src, cuda), T(ks, cuda), T(p, cuda), cfg)
+    torch.cuda.synchronize()
+    for f, k in enumerate(ks):
+        xo, lo, _ = O.solve_tikhonov_gcv(O.monopole_matrix(mics, src, k), p[f, 0], grid=(1e-8, 1e2))
+        assert relerr(x[f, 0].cpu().numpy(), xo) < MIXED_TOL
+    pts = g.cartesian_to_spherical(g.planar_array(10, 10, 0.025, 0.15))
+    mic_xyz = g.planar_array(10, 10, 0.025, 0.15)
+    mono = rng.normal(size=(3, 6)) * 0.03
+    p = np.stack([g.add_noise(rng, O.monopole_matrix(mic_xyz, mono, k) @ g.complex_normal(rng, 6), 25.0)[None, :]
+                  for k in ks])
+    x, lam, s, info = api.hels_solve_batch(ctx, T(pts, cuda), 8, T(ks, cuda), T(p, cuda),
+                                           api.default_config(precision=1))
+    torch.cuda.synchronize()
+    for f, k in enumerate(ks):
+        _, He, _ = O.hels(pts, pts, k, 8, 343.0, 1.21)
+        xo, lo, _ = O.solve_tikhonov_gcv(He, p[f, 0])
+        assert relerr(x[f, 0].cpu().numpy(), xo) < MIXED_TOL
