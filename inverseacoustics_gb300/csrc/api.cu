@@ -334,6 +334,21 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
         g[11] = nz;
         g[12] = sqrt(nx * nx + ny * ny + nz * nz);
     }
+    // regular-rule points per element (colour order), structure of arrays
+    std::vector<double> qdat((size_t)9 * nq * n);
+    for (int t = 0; t < n; ++t) {
+        const double *g = &egeo[(size_t)16 * t];
+        for (int q = 0; q < nq; ++q) {
+            const double x1 = reg[q], x2 = reg[q + nq], w = reg[q + 2 * nq] * IA_INV4PI;
+            const double N[3] = {x1, x2, 1.0 - x1 - x2};
+            double *p = &qdat[(size_t)q * 9 * n + t];
+            for (int d = 0; d < 3; ++d) p[(size_t)d * n] = N[0] * g[d] + N[1] * g[3 + d] + N[2] * g[6 + d];
+            for (int v = 0; v < 3; ++v) {
+                p[(size_t)(3 + v) * n] = w * N[v];
+                p[(size_t)(6 + v) * n] = w * N[v] * g[12];
+            }
+        }
+    }
     std::vector<int> aptr(m + 1, 0), adj;
     adj.reserve((size_t)3 * n);
     for (int o = 0; o < m; ++o) {
@@ -368,6 +383,7 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
     up((void **)&M->d_adj, adj.data(), sizeof(int) * adj.size());
     up((void **)&M->d_reg, reg.data(), sizeof(double) * reg.size());
     up((void **)&M->d_sing, sing.data(), sizeof(double) * sing.size());
+    up((void **)&M->d_qdat, qdat.data(), sizeof(double) * qdat.size());
     if (e != cudaSuccess) {
         ia_mesh_destroy(M);
         return cuda_status(e);
@@ -387,6 +403,7 @@ int ia_mesh_destroy(ia_mesh *M)
     cudaFree(M->d_adj);
     cudaFree(M->d_reg);
     cudaFree(M->d_sing);
+    cudaFree(M->d_qdat);
     free(M);
     return IA_OK;
 }
@@ -463,12 +480,12 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     if ((st = copy2d_batched<float2, double2>(ctx, m, l, Y32, m, sML, Y, m, sML, false, F))) return st;
     for (int it = 0; it < cfg->refine_steps; ++it) {
         if ((st = zcopy2d_batched(ctx, m, l, Ahs_t, m, sML, R, m, sML, false, F))) return st;
-        if ((st = dfgemm_batched(ctx, m, l, m, -1.0, At, m, sMM, Y, m, sML, 1.0, R, m, sML, F))) return st;
+        if ((st = dfgemm_batched(ctx, OP_N, OP_N, m, l, m, -1.0, At, m, sMM, Y, m, sML, 1.0, R, m, sML, F))) return st;
         if ((st = copy2d_batched<double2, float2>(ctx, m, l, R, m, sML, Y32, m, sML, false, F))) return st;
         if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
         if ((st = add2d_batched<float2>(ctx, m, l, Y32, m, sML, Y, m, sML, F))) return st;
     }
-    return dfgemm_batched(ctx, m, l, m, 1.0, Bt, m, sMM, Y, m, sML, -1.0, Ht, m, sML, F);
+    return dfgemm_batched(ctx, OP_N, OP_N, m, l, m, 1.0, Bt, m, sMM, Y, m, sML, -1.0, Ht, m, sML, F);
 }
 
 int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,

@@ -2,7 +2,6 @@
 //
 //  * monopole_kernel   plain ESM matrix G = exp(ikr)/(4 pi r)      (esmV.m:29-30)
 //  * esm_system_kernel D^T, M_sq^T, M_hq^T of the reference esm()  (esm.cuh:1-36, :120-145)
-//  * ibem_rows_kernel  gather-form IBEM collocation rows           (ibem.cuh:1-261, :486-738)
 //  * hels_kernel       h_n(kr) Y_n^m and its radial derivative       (hels.cuh:86-183, :222-323)
 #include "ia_common.cuh"
 #include "ia_internal.h"
@@ -84,190 +83,6 @@ int esm_system(ia_context *ctx, int m, int l, const double *src, const double *m
     long long total = (long long)m * (m + l);
     esm_system_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(m, l, src, mics, r_i, k, c, rho, DT,
                                                                                RHS);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
-}
-
-// --------------------------------------------------------------------------
-// IBEM collocation rows, gather form.
-//
-// One warp owns one row (collocation point) of one frequency and keeps that
-// row of A and B in shared memory.  Lanes walk the elements 32 at a time in
-// colour order: elements of one colour share no vertex, so the three column
-// updates of 32 lanes never collide and need no atomics; colours are
-// separated by __syncwarp().  For a surface row, the ~6 elements incident to
-// the collocation node use the singular rule (the page of the node's slot);
-// the whole warp integrates each of them, lanes striding the rule's points,
-// then reduces with shuffles in a fixed order.  Result: deterministic rows,
-// each written once, coalesced, as row-major (the transpose of the
-// reference's column-major ass/bss/ahs/bhs, CUDA/ibem.cuh:481-482,621-622).
-// --------------------------------------------------------------------------
-constexpr int IBEM_WARPS = 4;
-constexpr int IBEM_MAX_NQ = 64;
-
-struct ElemAcc {
-    double2 a[3], b[3];
-    double ct;
-};
-
-__device__ __forceinline__ void integrate_elem(const double *__restrict__ eg, double xo, double yo, double zo,
-                                               double k, const double *rule, int nq, int q0, int qstep, ElemAcc &acc)
-{
-    const double v0x = eg[0], v0y = eg[1], v0z = eg[2];
-    const double v1x = eg[3], v1y = eg[4], v1z = eg[5];
-    const double v2x = eg[6], v2y = eg[7], v2z = eg[8];
-    const double nx = eg[9], ny = eg[10], nz = eg[11], an = eg[12];
-    for (int q = q0; q < nq; q += qstep) {
-        const double x1 = rule[q], x2 = rule[q + nq], w = rule[q + 2 * nq];
-        const double x3 = 1.0 - x1 - x2;
-        const double dx = x1 * v0x + x2 * v1x + x3 * v2x - xo;
-        const double dy = x1 * v0y + x2 * v1y + x3 * v2y - yo;
-        const double dz = x1 * v0z + x2 * v1z + x3 * v2z - zo;
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        const double invr = rsqrt(r2);
-        const double kr = k * r2 * invr;
-        double sn, cs;
-        sincos(kr, &sn, &cs);
-        const double gr = cs * invr, gi = sn * invr;
-        const double ft = (nx * dx + ny * dy + nz * dz) * (invr * invr);
-        // (ikr - 1) g
-        const double tr = -gr - kr * gi, ti = kr * gr - gi;
-        const double wa = w * IA_INV4PI * ft, wb = w * IA_INV4PI * an;
-        const double N[3] = {x1, x2, x3};
-#pragma unroll
-        for (int v = 0; v < 3; ++v) {
-            acc.a[v].x = fma(wa * N[v], tr, acc.a[v].x);
-            acc.a[v].y = fma(wa * N[v], ti, acc.a[v].y);
-            acc.b[v].x = fma(wb * N[v], gr, acc.b[v].x);
-            acc.b[v].y = fma(wb * N[v], gi, acc.b[v].y);
-        }
-        acc.ct = fma(-w * IA_INV4PI * ft, invr, acc.ct);
-    }
-}
-
-__global__ void __launch_bounds__(IBEM_WARPS * 32) ibem_rows_kernel(
-    int m, int n, int l, int n_ch, int ncolors, const double *__restrict__ nodes, const double *__restrict__ egeo,
-    const int *__restrict__ evert, const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr,
-    const int *__restrict__ adj, const double *__restrict__ reg, int nq, const double *__restrict__ sing, int nqs,
-    const double *__restrict__ mics, const double *__restrict__ cp, const double *__restrict__ kv, double c,
-    double rho, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
-    double2 *__restrict__ Bhs_t)
-{
-    extern __shared__ double2 rowbuf[];   // IBEM_WARPS x (2 m)
-    __shared__ double rule_s[3 * IBEM_MAX_NQ];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int f = blockIdx.y;
-    const int mt = m + n_ch;
-    const int rows_total = mt + l;
-    const int row = blockIdx.x * IBEM_WARPS + wid;
-    for (int t = threadIdx.x; t < 3 * nq; t += blockDim.x) rule_s[t] = reg[t];
-    __syncthreads();
-    if (row >= rows_total) return;
-    double2 *Ar = rowbuf + (size_t)wid * 2 * m;
-    double2 *Br = Ar + m;
-    for (int j = lane; j < m; j += 32) {
-        Ar[j] = make_double2(0.0, 0.0);
-        Br[j] = make_double2(0.0, 0.0);
-    }
-    const double k = kv[f];
-    double xo, yo, zo;
-    int self = -1;
-    if (row < m) {
-        xo = nodes[row]; yo = nodes[row + m]; zo = nodes[row + 2 * m];
-        self = row;
-    } else if (row < mt) {
-        int i = row - m;
-        xo = cp[i]; yo = cp[i + n_ch]; zo = cp[i + 2 * n_ch];
-    } else {
-        int i = row - mt;
-        xo = mics[i]; yo = mics[i + l]; zo = mics[i + 2 * l];
-    }
-    __syncwarp();
-    double ct_lane = 0.0;
-    // regular elements, colour by colour
-    for (int cidx = 0; cidx < ncolors; ++cidx) {
-        const int e0 = color_ptr[cidx], e1 = color_ptr[cidx + 1];
-        for (int e = e0 + lane; e < e1; e += 32) {
-            const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
-            if (vv.x == self || vv.y == self || vv.z == self) continue;
-            ElemAcc acc;
-#pragma unroll
-            for (int v = 0; v < 3; ++v) { acc.a[v] = make_double2(0.0, 0.0); acc.b[v] = make_double2(0.0, 0.0); }
-            acc.ct = 0.0;
-            integrate_elem(egeo + (size_t)e * 16, xo, yo, zo, k, rule_s, nq, 0, 1, acc);
-            ct_lane += acc.ct;
-            const int cols[3] = {vv.x, vv.y, vv.z};
-#pragma unroll
-            for (int v = 0; v < 3; ++v) {
-                Ar[cols[v]] = zadd(Ar[cols[v]], acc.a[v]);
-                Br[cols[v]] = zadd(Br[cols[v]], acc.b[v]);
-            }
-        }
-        __syncwarp();
-    }
-    // singular elements of a surface row: whole warp per incident element
-    if (self >= 0) {
-        for (int a = adj_ptr[self]; a < adj_ptr[self + 1]; ++a) {
-            const int code = adj[a];
-            const int e = code >> 2, slot = code & 3;
-            ElemAcc acc;
-#pragma unroll
-            for (int v = 0; v < 3; ++v) { acc.a[v] = make_double2(0.0, 0.0); acc.b[v] = make_double2(0.0, 0.0); }
-            acc.ct = 0.0;
-            integrate_elem(egeo + (size_t)e * 16, xo, yo, zo, k, sing + (size_t)3 * nqs * slot, nqs, lane, 32, acc);
-#pragma unroll
-            for (int v = 0; v < 3; ++v) {
-                acc.a[v] = warp_sum2(acc.a[v]);
-                acc.b[v] = warp_sum2(acc.b[v]);
-            }
-            acc.ct = warp_sum(acc.ct);
-            if (lane == 0) {
-                const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
-                const int cols[3] = {vv.x, vv.y, vv.z};
-#pragma unroll
-                for (int v = 0; v < 3; ++v) {
-                    Ar[cols[v]] = zadd(Ar[cols[v]], acc.a[v]);
-                    Br[cols[v]] = zadd(Br[cols[v]], acc.b[v]);
-                }
-                ct_lane += acc.ct;
-            }
-            __syncwarp();
-        }
-        double ct = warp_sum(ct_lane);
-        if (lane == 0) Ar[self].x -= 1.0 + ct;
-        __syncwarp();
-    }
-    // scale B by i rho c k and write the row
-    const double s = rho * c * k;
-    double2 *arow, *brow;
-    if (row < mt) {
-        arow = At ? At + ((size_t)f * mt + row) * m : nullptr;
-        brow = Bt ? Bt + ((size_t)f * mt + row) * m : nullptr;
-    } else {
-        arow = Ahs_t ? Ahs_t + ((size_t)f * l + (row - mt)) * m : nullptr;
-        brow = Bhs_t ? Bhs_t + ((size_t)f * l + (row - mt)) * m : nullptr;
-    }
-    for (int j = lane; j < m; j += 32) {
-        if (arow) arow[j] = Ar[j];
-        double2 bv = Br[j];
-        if (brow) brow[j] = make_double2(-s * bv.y, s * bv.x);
-    }
-}
-
-int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
-              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t)
-{
-    if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
-    const int m = mesh->m;
-    const int rows = m + n_ch + l;
-    size_t smem = sizeof(double2) * 2 * (size_t)m * IBEM_WARPS;
-    if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
-    IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    dim3 g((rows + IBEM_WARPS - 1) / IBEM_WARPS, F);
-    ibem_rows_kernel<<<g, IBEM_WARPS * 32, smem, ctx->stream>>>(
-        m, mesh->n, l, n_ch, mesh->ncolors, mesh->d_nodes, mesh->d_egeo, mesh->d_evert, mesh->d_color_ptr,
-        mesh->d_adj_ptr, mesh->d_adj, mesh->d_reg, mesh->nq, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, At, Bt,
-        Ahs_t, Bhs_t);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }

@@ -1,15 +1,16 @@
-// Double-float complex GEMM: C = alpha A B + beta C for FP64 operands, with
-// every product and sum carried as an unevaluated pair of FP32 values
-// (hi + lo, ~48-bit significand).  GB300 issues FP32 at ~64x its FP64 rate, so
-// this runs several times faster than an FP64 GEMM while keeping the
-// residuals and transfer products of the mixed path at FP64-level accuracy
-// (about 1e-13 relative over the K = 642 sums here).
+// Double-float complex GEMM: C = alpha op(A) op(B) + beta C for FP64
+// operands, with every product and sum carried as an unevaluated pair of FP32
+// values (hi + lo, ~48-bit significand).  GB300 issues FP32 at ~64x its FP64
+// rate, so this runs several times faster than an FP64 GEMM while keeping the
+// residuals, transfer products and eigen-refinement products of the mixed
+// path at FP64-level accuracy (about 1e-13 relative over K = 642 sums).
 //
 // Products use the error-free transformation p + e = x_hi y_hi (fmaf), plus
 // the cross terms x_hi y_lo + x_lo y_hi; sums use TwoSum on the high word with
 // the low word accumulated and renormalised after each K tile (Dekker 1971;
 // Hida, Li, Bailey 2001).  Tiles: 64 x 64 outputs, K tile 8, 256 threads with
 // a 4 x 4 block each, operands split to (hi, lo) on the way into shared memory.
+// op(A), op(B) in {N, C} (C = conjugate transpose).
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -21,8 +22,9 @@ struct df2 {   // complex double-float accumulator
     float rh, rl, ih, il;
 };
 
-__device__ __forceinline__ float4 split_c(double2 v)
+__device__ __forceinline__ float4 split_c(double2 v, bool conj)
 {
+    if (conj) v.y = -v.y;
     float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
     float rl = __double2float_rn(v.x - (double)rh), il = __double2float_rn(v.y - (double)ih);
     return make_float4(rh, ih, rl, il);
@@ -49,10 +51,10 @@ __device__ __forceinline__ void df_norm(float &ah, float &al)
     ah = s;
 }
 
-__global__ void __launch_bounds__(256) dfgemm_kernel(int M, int N, int K, double alpha, const double2 *__restrict__ A,
-                                                     int lda, long long sA, const double2 *__restrict__ B, int ldb,
-                                                     long long sB, double beta, double2 *__restrict__ C, int ldc,
-                                                     long long sC)
+__global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, int N, int K, double alpha,
+                                                     const double2 *__restrict__ A, int lda, long long sA,
+                                                     const double2 *__restrict__ B, int ldb, long long sB,
+                                                     double beta, double2 *__restrict__ C, int ldc, long long sC)
 {
     __shared__ float4 As[DF_K][DF_M];
     __shared__ float4 Bs[DF_K][DF_N];
@@ -72,16 +74,26 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int M, int N, int K, double
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
             int e = threadIdx.x + t * 256;
-            int r = e % DF_M, kk = e / DF_M;
+            int r, kk;
+            if (opa == OP_N) { r = e % DF_M; kk = e / DF_M; }
+            else { kk = e % DF_K; r = e / DF_K; }
             int gr = m0 + r, gk = k0 + kk;
-            As[kk][r] = (gr < M && gk < K) ? split_c(A[gr + (size_t)gk * lda]) : z4;
+            float4 v = z4;
+            if (gr < M && gk < K)
+                v = opa == OP_N ? split_c(A[gr + (size_t)gk * lda], false) : split_c(A[gk + (size_t)gr * lda], true);
+            As[kk][r] = v;
         }
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
             int e = threadIdx.x + t * 256;
-            int kk = e % DF_K, c = e / DF_K;
+            int kk, c;
+            if (opb == OP_N) { kk = e % DF_K; c = e / DF_K; }
+            else { c = e % DF_N; kk = e / DF_N; }
             int gk = k0 + kk, gc = n0 + c;
-            Bs[kk][c] = (gk < K && gc < N) ? split_c(B[gk + (size_t)gc * ldb]) : z4;
+            float4 v = z4;
+            if (gk < K && gc < N)
+                v = opb == OP_N ? split_c(B[gk + (size_t)gc * ldb], false) : split_c(B[gc + (size_t)gk * ldb], true);
+            Bs[kk][c] = v;
         }
         __syncthreads();
 #pragma unroll
@@ -133,12 +145,14 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int M, int N, int K, double
     }
 }
 
-int dfgemm_batched(ia_context *ctx, int M, int N, int K, double alpha, const double2 *A, int lda, long long sA,
-                   const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc, long long sC, int batch)
+int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
+                   long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                   long long sC, int batch)
 {
     if (M <= 0 || N <= 0 || batch <= 0) return IA_OK;
+    if ((opa != OP_N && opa != OP_C) || (opb != OP_N && opb != OP_C)) return IA_ERR_ARG;
     dim3 grid((N + DF_N - 1) / DF_N, (M + DF_M - 1) / DF_M, batch);
-    dfgemm_kernel<<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    dfgemm_kernel<<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }

@@ -27,6 +27,7 @@ struct ia_mesh {
     int *d_adj;            // 3n: element index (colour order) * 4 + slot
     double *d_reg;         // 3 x nq
     double *d_sing;        // 9 x nqs
+    double *d_qdat;        // regular-rule points: [q][x, y, z, w N_v / 4pi (3), w N_v |n| / 4pi (3)][element]
 };
 
 namespace ia {
@@ -119,10 +120,11 @@ inline int zcopy2d_batched(ia_context *ctx, int rows, int cols, const double2 *i
 int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
                    int ldb, long long sB, int batch);
 
-// C = alpha A B + beta C with FP64 inputs and output, products and sums in
-// double-float (FP32 pairs) arithmetic (dfgemm.cu); op(A) = op(B) = N
-int dfgemm_batched(ia_context *ctx, int M, int N, int K, double alpha, const double2 *A, int lda, long long sA,
-                   const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc, long long sC, int batch);
+// C = alpha op(A) op(B) + beta C with FP64 inputs and output, products and
+// sums in double-float (FP32 pairs) arithmetic (dfgemm.cu); op in {N, C}
+int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
+                   long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                   long long sC, int batch);
 
 // ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);

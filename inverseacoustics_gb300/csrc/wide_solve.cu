@@ -256,110 +256,176 @@ int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *
 }
 
 // --------------------------------------------------------------------------
-// mixed path
+// mixed path: FP32 start, FP64-accurate finish in data space.
+//
+// H H^H = U S^2 U^H (m x m) holds everything GCV and Tikhonov need:
+//   beta = U^H b, s, and x = V diag(phi) beta = H^H U diag(phi/s) beta.
+// 1. FP32: Y = H^H = Q R, one-sided Jacobi R J = U_R S with J accumulated;
+//    J approximates U.
+// 2. E = H H^H in FP64.
+// 3. Eigen-refinement of E from X = J (Ogita & Aishima 2018, Hermitian form):
+//      R = I - X^H X, S = X^H E X, lambda_i = S_ii / (1 - R_ii),
+//      F_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i)  (separated pairs)
+//      F_ij = R_ij / 2                                         (clustered pairs,
+//             |lambda_i - lambda_j| <= 2 (||S - diag(lambda)|| + max|lambda| ||R||))
+//      X <- X (I + F)
+//    E X and X^H (E X) in FP64, X^H X and X F in double-float; each step
+//    squares the error of X.
+// 4. s = sqrt(lambda) sorted, beta = U^H b, GCV in FP64, x = H^H U (phi/s .* beta).
+// For H given as H^T, E is formed as (H^T)^H H^T = conj(H H^H), whose
+// eigenvectors are conj(U).
 // --------------------------------------------------------------------------
-constexpr int REFINE_THREADS = 256;
+constexpr int OA_THREADS = 256;
 
-// One CTA per (frequency, right-hand side).  H is m x n (FP64): given as H
-// (column-major m x n) or as H^T (column-major n x m).  V (n x N, FP32) and
-// s (N) approximate H's right singular vectors and values; lambda fixed.
-// x_{k+1} = x_k + V diag(1/(s^2+lambda^2)) V^H (H^H (b - H x_k) - lambda^2 x_k)
-__global__ void __launch_bounds__(REFINE_THREADS) tikhonov_refine_kernel(int m, int n, int N, const double2 *H,
-                                                                           int transposed, const float2 *V,
-                                                                           const double *S, const double *LAM,
-                                                                           int nrhs, const double2 *Bv, int steps,
-                                                                           double2 *X)
+__global__ void __launch_bounds__(OA_THREADS) oa_update_kernel(int N, const double2 *S, const double2 *Rm,
+                                                                 double2 *Fc, double *LAM)
 {
-    extern __shared__ double2 smz[];
-    double2 *x = smz;          // n
-    double2 *g = x + n;        // n
-    double2 *r1 = g + n;       // m
-    double2 *t2 = r1 + m;      // N
-    const int f = blockIdx.x, rr = blockIdx.y;
+    __shared__ double red[2][OA_THREADS / 32];
+    __shared__ double s_delta;
+    extern __shared__ double lam[];   // N
+    const int f = blockIdx.x;
+    const size_t off = (size_t)f * N * N;
+    S += off;
+    Rm += off;
+    Fc += off;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    H += (size_t)f * m * n;
-    V += (size_t)f * n * N;
-    S += (size_t)f * N;
-    const double lam = LAM[(size_t)f * nrhs + rr], l2 = lam * lam;
-    const double2 *b = Bv + ((size_t)f * nrhs + rr) * m;
-    const double2 zero = make_double2(0.0, 0.0);
-    for (int i = tid; i < n; i += blockDim.x) x[i] = zero;
+    for (int i = tid; i < N; i += blockDim.x) {
+        double l = S[i + (size_t)i * N].x / Rm[i + (size_t)i * N].x;
+        lam[i] = l;
+        LAM[(size_t)f * N + i] = l;
+    }
     __syncthreads();
-    for (int it = 0; it < steps; ++it) {
-        // r1 = b - H x
-        if (transposed) {
-            // H(i, j) = Ht[j + i n]: column i of Ht is row i of H -> warp per row
-            for (int i = wid; i < m; i += nw) {
-                double2 acc = zero;
-                const double2 *col = H + (size_t)i * n;
-                for (int j = lane; j < n; j += 32) zfma(acc, col[j], x[j]);
-                acc = warp_sum2(acc);
-                if (lane == 0) r1[i] = zsub(b[i], acc);
-            }
+    double so = 0.0, ro = 0.0;
+    for (int e = tid; e < N * N; e += blockDim.x) {
+        int i = e % N, j = e / N;
+        double2 sv = S[e], rv = Rm[e];
+        if (i == j) {
+            sv.x -= lam[i];
+            rv.x = 1.0 - rv.x;
+            rv.y = -rv.y;
         } else {
-            for (int i = tid; i < m; i += blockDim.x) {
-                double2 acc = zero;
-                for (int j = 0; j < n; ++j) zfma(acc, H[i + (size_t)j * m], x[j]);
-                r1[i] = zsub(b[i], acc);
-            }
+            rv.x = -rv.x;
+            rv.y = -rv.y;
         }
-        __syncthreads();
-        // g = H^H r1 - lambda^2 x
-        if (transposed) {
-            for (int j = tid; j < n; j += blockDim.x) {
-                double2 acc = zero;
-                for (int i = 0; i < m; ++i) zcfma(acc, H[j + (size_t)i * n], r1[i]);
-                g[j] = zsub(acc, zscale(x[j], l2));
-            }
+        so += zabs2(sv);
+        ro += zabs2(rv);
+    }
+    so = warp_sum(so);
+    ro = warp_sum(ro);
+    if (lane == 0) { red[0][wid] = so; red[1][wid] = ro; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, b = 0.0, lmax = 0.0;
+        for (int w = 0; w < nw; ++w) { a += red[0][w]; b += red[1][w]; }
+        for (int i = 0; i < N; ++i) lmax = fmax(lmax, fabs(lam[i]));
+        s_delta = 2.0 * (sqrt(a) + lmax * sqrt(b));
+    }
+    __syncthreads();
+    const double delta = s_delta;
+    for (int e = tid; e < N * N; e += blockDim.x) {
+        int i = e % N, j = e / N;
+        double2 r = Rm[e];
+        double2 R = (i == j) ? make_double2(1.0 - r.x, -r.y) : make_double2(-r.x, -r.y);
+        double2 v;
+        double gap = lam[j] - lam[i];
+        if (i != j && fabs(gap) > delta) {
+            double2 num = zadd(S[e], zscale(R, lam[j]));
+            v = zscale(num, 1.0 / gap);
         } else {
-            for (int j = wid; j < n; j += nw) {
-                double2 acc = zero;
-                const double2 *col = H + (size_t)j * m;
-                for (int i = lane; i < m; i += 32) zcfma(acc, col[i], r1[i]);
-                acc = warp_sum2(acc);
-                if (lane == 0) g[j] = zsub(acc, zscale(x[j], l2));
-            }
+            v = zscale(R, 0.5);
         }
-        __syncthreads();
-        // preconditioner V diag(1/(s^2+l^2)) V^H + (I - V V^H)/l^2:
-        // t2 = (1/(s^2+l^2) - 1/l^2) V^H g, correction V t2 + g/l^2
-        const double il2 = l2 > 0.0 ? 1.0 / l2 : 0.0;
-        for (int k = wid; k < N; k += nw) {
-            double2 acc = zero;
-            const float2 *vc = V + (size_t)k * n;
-            for (int j = lane; j < n; j += 32) {
-                float2 v = vc[j];
-                zcfma(acc, make_double2(v.x, v.y), g[j]);
+        Fc[e] = v;
+    }
+}
+
+// s (sorted descending), beta = U^H b (sorted like s), rank of every column;
+// U = X, or conj(X) when conj_u.
+__global__ void eig_beta_kernel(int m, int N, const double *LAM, const double2 *X, int conj_u, int nrhs,
+                                const double2 *Bv, double *S, double2 *BETA, int *RANK)
+{
+    const int f = blockIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    LAM += (size_t)f * N;
+    X += (size_t)f * N * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double li = LAM[i];
+        int rk = 0;
+        for (int j = 0; j < N; ++j) {
+            double lj = LAM[j];
+            if (lj > li || (lj == li && j < i)) rk++;
+        }
+        RANK[(size_t)f * N + i] = rk;
+        S[(size_t)f * N + rk] = sqrt(fmax(li, 0.0));
+    }
+    __syncthreads();
+    for (int r = 0; r < nrhs; ++r) {
+        const double2 *b = Bv + ((size_t)f * nrhs + r) * m;
+        for (int i = wid; i < N; i += nw) {
+            double2 acc = make_double2(0.0, 0.0);
+            const double2 *xc = X + (size_t)i * N;
+            for (int j = lane; j < m; j += 32) {
+                if (conj_u) zfma(acc, xc[j], b[j]);       // conj(conj(X)) b
+                else zcfma(acc, xc[j], b[j]);
             }
             acc = warp_sum2(acc);
-            if (lane == 0) {
-                double sk = S[k];
-                double d = sk * sk + l2;
-                t2[k] = zscale(acc, d > 0.0 ? 1.0 / d - il2 : 0.0);
-            }
+            if (lane == 0) BETA[((size_t)f * nrhs + r) * N + RANK[(size_t)f * N + i]] = acc;
         }
-        __syncthreads();
-        // x += V t2 + g / l^2
-        for (int j = tid; j < n; j += blockDim.x) {
-            double2 acc = zadd(x[j], zscale(g[j], il2));
-            for (int k = 0; k < N; ++k) {
-                float2 v = V[j + (size_t)k * n];
-                zfma(acc, make_double2(v.x, v.y), t2[k]);
-            }
-            x[j] = acc;
-        }
-        __syncthreads();
     }
-    double2 *xo = X + ((size_t)f * nrhs + rr) * n;
-    for (int j = tid; j < n; j += blockDim.x) xo[j] = x[j];
+}
+
+// x = H^H U (z / s), one CTA per (frequency, right-hand side)
+__global__ void eig_backproject_kernel(int m, int n, int N, const double2 *H, int transposed, const double2 *X,
+                                       int conj_u, const int *RANK, const double *S, const double2 *Z, int nrhs,
+                                       double2 *Xout)
+{
+    extern __shared__ double2 smw[];
+    double2 *coef = smw;       // N, original column order
+    double2 *w = smw + N;      // m
+    const int f = blockIdx.x, rr = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    X += (size_t)f * N * N;
+    H += (size_t)f * m * n;
+    const double2 *z = Z + ((size_t)f * nrhs + rr) * N;
+    for (int i = tid; i < N; i += blockDim.x) {
+        int rk = RANK[(size_t)f * N + i];
+        double s = S[(size_t)f * N + rk];
+        coef[i] = s > 0.0 ? zscale(z[rk], 1.0 / s) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int j = tid; j < m; j += blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int i = 0; i < N; ++i) {
+            double2 u = X[j + (size_t)i * N];
+            if (conj_u) u.y = -u.y;
+            zfma(acc, u, coef[i]);
+        }
+        w[j] = acc;
+    }
+    __syncthreads();
+    double2 *x = Xout + ((size_t)f * nrhs + rr) * n;
+    if (transposed) {
+        for (int k = tid; k < n; k += blockDim.x) {
+            double2 acc = make_double2(0.0, 0.0);
+            for (int j = 0; j < m; ++j) zcfma(acc, H[k + (size_t)j * n], w[j]);
+            x[k] = acc;
+        }
+    } else {
+        for (int k = wid; k < n; k += nw) {
+            double2 acc = make_double2(0.0, 0.0);
+            const double2 *col = H + (size_t)k * m;
+            for (int j = lane; j < m; j += 32) zcfma(acc, col[j], w[j]);
+            acc = warp_sum2(acc);
+            if (lane == 0) x[k] = acc;
+        }
+    }
 }
 
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
 {
     const size_t F = batch, N = m, M = n, R = nrhs;
-    return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + ws_round(8 * (N + R) * N * F) +
-           ws_round(8 * N * F) + ws_round(16 * R * N * F) * 2 + ws_round(8 * N * N * F) + ws_round(8 * M * N * F) +
-           4096;
+    return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
+           7 * ws_round(16 * N * N * F) + 2 * ws_round(8 * N * F) + ws_round(4 * N * F) +
+           2 * ws_round(16 * R * N * F) + ws_round(8 * R * F) + 8192;
 }
 
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
@@ -368,19 +434,28 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
 {
     const int N = m, Mr = n;
     const bool qr = n > m;
+    const size_t NN = (size_t)N * N;
     double2 *Yd = transposed ? nullptr : cur.take<double2>((size_t)Mr * N * batch);
     float2 *Y = cur.take<float2>((size_t)Mr * N * batch);
     float2 *tau = cur.take<float2>((size_t)N * batch);
-    float2 *Rg = cur.take<float2>((size_t)(N + nrhs) * N * batch);
+    float2 *R32 = cur.take<float2>(NN * batch);
+    float2 *J32 = cur.take<float2>(NN * batch);
+    double2 *E = cur.take<double2>(NN * batch);
+    double2 *X = cur.take<double2>(NN * batch);
+    double2 *Xn = cur.take<double2>(NN * batch);
+    double2 *T1 = cur.take<double2>(NN * batch);
+    double2 *Sm = cur.take<double2>(NN * batch);
+    double2 *Rm = cur.take<double2>(NN * batch);
+    double2 *Fc = cur.take<double2>(NN * batch);
+    double *lam_e = cur.take<double>((size_t)N * batch);
     double *s = s_out ? s_out : cur.take<double>((size_t)N * batch);
+    int *rank = cur.take<int>((size_t)N * batch);
     double2 *beta = cur.take<double2>((size_t)nrhs * N * batch);
     double2 *z = cur.take<double2>((size_t)nrhs * N * batch);
-    float2 *UR = cur.take<float2>((size_t)N * N * batch);
-    float2 *V = cur.take<float2>((size_t)Mr * N * batch);
     double *lam = lambda ? lambda : cur.take<double>((size_t)nrhs * batch);
-    const long long sA = (long long)m * n, sY = (long long)Mr * N;
+    const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
-    // Y = A^H in FP32
+    // 1. FP32 start: Y = H^H, QR, Jacobi with J accumulated
     if (transposed) {
         st = copy2d_batched<double2, float2>(ctx, n, m, A, n, sA, Y, Mr, sY, true, batch);
     } else {
@@ -393,40 +468,44 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
         IA_LAUNCH_CHECK(ctx);
     }
     {
-        long long total = (long long)(N + nrhs) * N;
+        long long total = (long long)N * N;
         int blocks = (int)((total + 255) / 256);
         if (blocks > 512) blocks = 512;
-        build_raug_kernel<float2><<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, nrhs, Y, b, qr ? 0 : 1, Rg);
+        build_raug_kernel<float2><<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, 0, Y, b, qr ? 0 : 1, R32);
         IA_LAUNCH_CHECK(ctx);
     }
-    st = jacobi_rows_batched<float2>(ctx, N + nrhs, N, N, Rg, nullptr, batch, cfg->svd_max_sweeps, info);
+    st = jacobi_rows_batched<float2>(ctx, N, N, N, R32, J32, batch, cfg->svd_max_sweeps, info);
     if (st) return st;
-    finalize_wide_kernel<float2><<<batch, 256, (size_t)N * (sizeof(double) + sizeof(int)), ctx->stream>>>(
-        N, nrhs, Rg, s, beta, UR, info);
+    // 2. E = H H^H (or its conjugate for H^T input).  E and S = X^H E X set
+    // the accuracy of the eigenvectors as eps ||E|| / gap, so they are FP64
+    // products; X^H X and X F only need double-float.
+    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
+    if (transposed) st = zgemm_batched(ctx, OP_C, OP_N, N, N, n, one, A, n, sA, A, n, sA, zero, E, N, sN, batch);
+    else st = zgemm_batched(ctx, OP_N, OP_C, N, N, n, one, A, m, sA, A, m, sA, zero, E, N, sN, batch);
+    if (st) return st;
+    // 3. eigen-refinement from X = J (conj(J) for H^T input)
+    if ((st = copy2d_batched<float2, double2>(ctx, N, N, J32, N, sN, X, N, sN, transposed, batch))) return st;
+    const int steps = cfg->refine_steps > 0 ? cfg->refine_steps : 1;
+    for (int it = 0; it < steps; ++it) {
+        if ((st = zgemm_batched(ctx, OP_N, OP_N, N, N, N, one, E, N, sN, X, N, sN, zero, T1, N, sN, batch))) return st;
+        if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;
+        if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
+        oa_update_kernel<<<batch, OA_THREADS, sizeof(double) * (size_t)N, ctx->stream>>>(N, Sm, Rm, Fc, lam_e);
+        IA_LAUNCH_CHECK(ctx);
+        if ((st = zcopy2d_batched(ctx, N, N, X, N, sN, Xn, N, sN, false, batch))) return st;
+        if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, 1.0, X, N, sN, Fc, N, sN, 1.0, Xn, N, sN, batch))) return st;
+        double2 *t = X;
+        X = Xn;
+        Xn = t;
+    }
+    // 4. s, beta, GCV, back-projection
+    eig_beta_kernel<<<batch, 256, 0, ctx->stream>>>(m, N, lam_e, X, transposed ? 1 : 0, nrhs, b, s, beta, rank);
     IA_LAUNCH_CHECK(ctx);
     st = gcv_beta_batched(ctx, m, N, batch, s, nrhs, beta, nullptr, cfg, z, lam);
     if (st) return st;
-    // V_H = Q [U_R; 0] (n x N, FP32)
-    if (qr) {
-        apply_q_kernel<float2><<<batch, 256, 0, ctx->stream>>>(Mr, N, Y, tau, N, UR, N, (long long)N * N, V, sY);
-        IA_LAUNCH_CHECK(ctx);
-    } else {
-        st = copy2d_batched<float2, float2>(ctx, N, N, UR, N, (long long)N * N, V, N, (long long)N * N, false, batch);
-        if (st) return st;
-    }
-    if (cfg->method == IA_METHOD_TSVD) {
-        // TSVD keeps the FP32 factors: x = V (phi .* beta), phi from gcv_beta_batched (lambda = 0)
-        double2 *Vd = cur.take<double2>((size_t)Mr * N * batch);
-        st = copy2d_batched<float2, double2>(ctx, Mr, N, V, Mr, sY, Vd, Mr, sY, false, batch);
-        if (st) return st;
-        return zgemm_batched(ctx, OP_N, OP_N, Mr, nrhs, N, make_double2(1.0, 0.0), Vd, Mr, sY, z, N,
-                             (long long)N * nrhs, make_double2(0.0, 0.0), x, Mr, (long long)Mr * nrhs, batch);
-    }
-    size_t smem = sizeof(double2) * (2 * (size_t)n + (size_t)m + (size_t)N);
-    if (smem > 200 * 1024) return IA_ERR_TOO_LARGE;
-    IA_CUDA_TRY(cudaFuncSetAttribute(tikhonov_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    tikhonov_refine_kernel<<<dim3(batch, nrhs), REFINE_THREADS, smem, ctx->stream>>>(
-        m, n, N, A, transposed ? 1 : 0, V, s, lam, nrhs, b, cfg->refine_steps + 1, x);
+    size_t smem = sizeof(double2) * ((size_t)N + (size_t)m);
+    eig_backproject_kernel<<<dim3(batch, nrhs), 256, smem, ctx->stream>>>(m, n, N, A, transposed ? 1 : 0, X,
+                                                                         transposed ? 1 : 0, rank, s, z, nrhs, x);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
