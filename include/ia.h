@@ -196,6 +196,23 @@ int ia_regularize_batch(ia_context *ctx, int m, int n, int F, const ia_complex *
 int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_b,
                    const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info);
 
+/* Size of the device array that ia_solve_batch_noalloc works in. */
+#define IA_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* ia_solve_batch without any device allocation (no counterpart in the
+ * reference).  For callers that may not allocate device memory: a real-time
+ * acquisition loop, where cudaMalloc's implicit synchronisation and latency
+ * would drop frames, or code recording the solve into a CUDA graph during
+ * stream capture.  Scratch comes from one static device array of
+ * IA_NOALLOC_SCRATCH_BYTES (held by every GPU that loads the library until
+ * exit).  Wide or square operators only (m <= n), FP64 path; larger problems
+ * return IA_ERR_TOO_LARGE.  The first call on a device looks the array's
+ * address up and should come before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race. */
+int ia_solve_batch_noalloc(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs,
+                           const ia_complex *d_b, const ia_config *cfg, ia_complex *d_x, double *d_lambda,
+                           double *d_s, int *d_info);
+
 /* The whole IBEM pipeline for F frequencies: assembly, H, SVD, GCV/Tikhonov.
  * d_p F x (l x nrhs) measured pressures, d_x F x (m x nrhs) surface velocity. */
 int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,

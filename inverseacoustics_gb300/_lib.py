@@ -74,6 +74,7 @@ _SIGS = {
     "ia_svd_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
     "ia_regularize_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _I, _P, _P, _P, _P]),
     "ia_solve_batch": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_solve_batch_noalloc": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_ibem_solve_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_esm_solve_batch": (_I, [_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_hels_solve_batch": (_I, [_P, _I, _P, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
