@@ -73,7 +73,8 @@ typedef struct {
     int tsvd_k;            /* truncation index for IA_METHOD_TSVD, 1 <= k <= p */
     int precision;         /* IA_PREC_FP64 or IA_PREC_MIXED */
     int svd_max_sweeps;    /* Jacobi sweep cap (default 40) */
-    int refine_steps;      /* iterative-refinement steps of the mixed path (default 2) */
+    int refine_steps;      /* refinement steps of the mixed path: LU residual steps and
+                              eigen-refinement steps (default 1; each squares the error) */
 } ia_config;
 
 /* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,

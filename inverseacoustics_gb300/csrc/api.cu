@@ -183,7 +183,7 @@ void ia_config_default(ia_config *cfg)
     cfg->tsvd_k = 1;
     cfg->precision = IA_PREC_FP64;
     cfg->svd_max_sweeps = 40;
-    cfg->refine_steps = 2;
+    cfg->refine_steps = 1;
 }
 
 const char *ia_status_string(int status)

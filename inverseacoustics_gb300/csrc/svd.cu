@@ -152,6 +152,99 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int M
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
 }
 
+// Same iteration with Y held in shared memory for the whole run (M x N small
+// enough); V, when accumulated, stays in global memory and its two columns
+// are fetched before the dot products so their latency overlaps them.
+template <class T, int KPL>
+__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_smem_kernel(int M, int Mdot, int N, T *Yg, long long sY,
+                                                                           T *V, long long sV, int max_sweeps,
+                                                                           typename ctraits<T>::R tol, int *info)
+{
+    typedef typename ctraits<T>::R R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *Y = reinterpret_cast<T *>(smraw);
+    __shared__ int s_rot;
+    const int f = blockIdx.x;
+    Yg += f * sY;
+    if (V) V += f * sV;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int N2 = N + (N & 1);
+    const T zero = ctraits<T>::make(0, 0);
+    for (int e = threadIdx.x; e < M * N; e += blockDim.x) Y[e] = Yg[e];
+    __syncthreads();
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) s_rot = 0;
+        __syncthreads();
+        int rot_local = 0;
+        for (int round = 0; round < N2 - 1; ++round) {
+            for (int k = wid; k < N2 / 2; k += nw) {
+                int i, j;
+                rr_pair(N2, round, k, i, j);
+                if (j >= N) continue;
+                T vi[KPL], vj[KPL];
+                T *gvi = V ? V + (size_t)i * N : nullptr, *gvj = V ? V + (size_t)j * N : nullptr;
+                if (V) {
+#pragma unroll
+                    for (int t = 0; t < KPL; ++t) {
+                        int r = lane + 32 * t;
+                        vi[t] = r < N ? gvi[r] : zero;
+                        vj[t] = r < N ? gvj[r] : zero;
+                    }
+                }
+                T *yi = Y + (size_t)i * M, *yj = Y + (size_t)j * M;
+                R a = 0, b = 0, c;
+                T g = zero, sp;
+                T ui[KPL], uj[KPL];
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    int r = lane + 32 * t;
+                    ui[t] = r < M ? yi[r] : zero;
+                    uj[t] = r < M ? yj[r] : zero;
+                    if (r < Mdot) {
+                        a += zabs2(ui[t]);
+                        b += zabs2(uj[t]);
+                        zcfma(g, ui[t], uj[t]);
+                    }
+                }
+                a = warp_sum(a);
+                b = warp_sum(b);
+                g = warp_sum2(g);
+                if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    int r = lane + 32 * t;
+                    if (r < M) {
+                        rotate_pair(ui[t], uj[t], c, sp);
+                        yi[r] = ui[t];
+                        yj[r] = uj[t];
+                    }
+                }
+                if (V) {
+#pragma unroll
+                    for (int t = 0; t < KPL; ++t) {
+                        int r = lane + 32 * t;
+                        if (r < N) {
+                            rotate_pair(vi[t], vj[t], c, sp);
+                            gvi[r] = vi[t];
+                            gvj[r] = vj[t];
+                        }
+                    }
+                }
+                rot_local++;
+            }
+            __syncthreads();
+        }
+        if (lane == 0 && rot_local) atomicAdd(&s_rot, rot_local);
+        __syncthreads();
+        int total = s_rot;
+        __syncthreads();
+        if (total == 0) break;
+    }
+    for (int e = threadIdx.x; e < M * N; e += blockDim.x) Yg[e] = Y[e];
+    if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
+}
+
 template <class T>
 __global__ void identity_kernel(int N, T *V, long long sV)
 {
@@ -177,7 +270,13 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     const double eps = sizeof(R) == 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
     const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;
-    if (M <= 128)
+    const size_t smem = sizeof(T) * (size_t)M * N;
+    if (M <= 128 && N <= 128 && smem <= 200 * 1024) {
+        IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_smem_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024));
+        jacobi_smem_kernel<T, 4><<<batch, nw * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol,
+                                                                        info);
+    } else if (M <= 128)
         jacobi_kernel<T, 4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     else if (M <= 256)
         jacobi_kernel<T, 8><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);

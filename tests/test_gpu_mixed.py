@@ -26,7 +26,8 @@ def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
     ks = w.k[[2, 53, 54, 63]]          # includes the two bins next to ka = pi
     mesh = api.Mesh(ctx, nodes, elems)
     H64, i64 = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
-    Hmx, imx = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), api.default_config(precision=1))
+    Hmx, imx = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda),
+                                       api.default_config(precision=1, refine_steps=2))
     torch.cuda.synchronize()
     assert int(imx.abs().sum()) == 0
     for f in range(len(ks)):
