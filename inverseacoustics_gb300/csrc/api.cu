@@ -349,6 +349,20 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
             }
         }
     }
+    std::vector<double> qnrm((size_t)3 * n);
+    for (int t = 0; t < n; ++t)
+        for (int d = 0; d < 3; ++d) qnrm[(size_t)d * n + t] = egeo[(size_t)16 * t + 9 + d];
+    // double-float copies (hi, lo) for the mixed-path assembly
+    auto split = [](const std::vector<double> &src) {
+        std::vector<float> out(2 * src.size());
+        for (size_t i = 0; i < src.size(); ++i) {
+            float h = (float)src[i];
+            out[2 * i] = h;
+            out[2 * i + 1] = (float)(src[i] - (double)h);
+        }
+        return out;
+    };
+    const std::vector<float> qdat_f = split(qdat), qnrm_f = split(qnrm);
     std::vector<int> aptr(m + 1, 0), adj;
     adj.reserve((size_t)3 * n);
     for (int o = 0; o < m; ++o) {
@@ -384,6 +398,9 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
     up((void **)&M->d_reg, reg.data(), sizeof(double) * reg.size());
     up((void **)&M->d_sing, sing.data(), sizeof(double) * sing.size());
     up((void **)&M->d_qdat, qdat.data(), sizeof(double) * qdat.size());
+    up((void **)&M->d_qnrm, qnrm.data(), sizeof(double) * qnrm.size());
+    up((void **)&M->d_qdat_f, qdat_f.data(), sizeof(float) * qdat_f.size());
+    up((void **)&M->d_qnrm_f, qnrm_f.data(), sizeof(float) * qnrm_f.size());
     if (e != cudaSuccess) {
         ia_mesh_destroy(M);
         return cuda_status(e);
@@ -404,6 +421,9 @@ int ia_mesh_destroy(ia_mesh *M)
     cudaFree(M->d_reg);
     cudaFree(M->d_sing);
     cudaFree(M->d_qdat);
+    cudaFree(M->d_qnrm);
+    cudaFree(M->d_qdat_f);
+    cudaFree(M->d_qnrm_f);
     free(M);
     return IA_OK;
 }
@@ -431,7 +451,7 @@ int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
     if (!ctx || !mesh || !cfg || F < 1 || l < 0 || n_ch < 0 || !d_k) return IA_ERR_ARG;
     if ((l > 0 && !d_mics) || (n_ch > 0 && !d_cp)) return IA_ERR_ARG;
     return ibem_rows(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, cfg->c, cfg->rho, (double2 *)d_At, (double2 *)d_Bt,
-                     (double2 *)d_Ahs_t, (double2 *)d_Bhs_t);
+                     (double2 *)d_Ahs_t, (double2 *)d_Bhs_t, cfg->precision == IA_PREC_MIXED);
 }
 
 // H^T (m x l per frequency) into Ht, given workspace for A^T, B^T, pivots.
@@ -470,7 +490,7 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     float2 *Y32 = cur.take<float2>((size_t)m * l * F);
     double2 *Y = cur.take<double2>((size_t)m * l * F);
     double2 *R = cur.take<double2>((size_t)m * l * F);
-    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
+    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true);
     if (st) return st;
     const long long sMM = (long long)m * m, sML = (long long)m * l;
     if ((st = copy2d_batched<double2, float2>(ctx, m, m, At, m, sMM, M32, m, sMM, false, F))) return st;

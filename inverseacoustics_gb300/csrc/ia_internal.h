@@ -28,6 +28,9 @@ struct ia_mesh {
     double *d_reg;         // 3 x nq
     double *d_sing;        // 9 x nqs
     double *d_qdat;        // regular-rule points: [q][x, y, z, w N_v / 4pi (3), w N_v |n| / 4pi (3)][element]
+    double *d_qnrm;        // element normals [3][element]
+    float *d_qdat_f;       // d_qdat as double-float (hi, lo) pairs
+    float *d_qnrm_f;       // d_qnrm as double-float (hi, lo) pairs
 };
 
 namespace ia {
@@ -174,8 +177,10 @@ int monopole_batched(ia_context *ctx, int l, int m, int F, const double *mics, c
                      double2 *G);
 int esm_system(ia_context *ctx, int m, int l, const double *src, const double *mics, double r_i, double k, double c,
                double rho, double2 *DT, double2 *RHS);
+// df32: regular-element arithmetic in double-float (mixed path) instead of FP64
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
-              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t);
+              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
+              bool df32 = false);
 int hels_batched(ia_context *ctx, int npts, const double *pts, int order, int F, const double *k, double c,
                  double rho, double2 *Me, double2 *Qe);
 

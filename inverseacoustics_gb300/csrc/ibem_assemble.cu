@@ -1,4 +1,4 @@
-// IBEM collocation rows, FP64, gather form, frequency-blocked.
+// IBEM collocation rows, gather form, frequency-blocked.
 //
 // Follows the reference's CPU ibem() assembly (CUDA/ibem.cuh:486-738; GPU
 // kernels :1-261), the OpenBEM collocation scheme on linear triangles:
@@ -25,6 +25,12 @@
 // coalesced, row-major (the transpose of the reference's column-major
 // ass/bss/ahs/bhs, CUDA/ibem.cuh:481-482, :621-622).  Results are
 // deterministic.
+//
+// The regular-element arithmetic is generic in its real type R: double for
+// the FP64 path, double-float (dfl, df32.cuh) for the mixed path, which moves
+// the dominant work from GB300's FP64 pipe to its FP32 pipe at ~1e-14
+// relative accuracy.  The singular elements stay FP64 in both.
+#include "df32.cuh"
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -33,6 +39,46 @@ namespace ia {
 constexpr int IBEM_FB = 4;          // frequencies per CTA
 constexpr int IBEM_THREADS = 128;   // 4 warps
 constexpr int IBEM_MAX_NQ = 64;
+
+// ---- the real-type policy -------------------------------------------------
+__device__ __forceinline__ double r_from(double x) { return x; }
+__device__ __forceinline__ double r_to_double(double x) { return x; }
+__device__ __forceinline__ double r_add(double a, double b) { return a + b; }
+__device__ __forceinline__ double r_sub(double a, double b) { return a - b; }
+__device__ __forceinline__ double r_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ void r_mac(double &acc, double a, double b) { acc = fma(a, b, acc); }
+__device__ __forceinline__ double r_norm(double a) { return a; }
+__device__ __forceinline__ double r_rsqrt(double a) { return rsqrt(a); }
+__device__ __forceinline__ double r_zero(double) { return 0.0; }
+__device__ __forceinline__ void r_sincos(double theta, const DfTrigCoef &, double &s, double &c) { sincos(theta, &s, &c); }
+
+__device__ __forceinline__ dfl r_from(dfl x) { return x; }
+__device__ __forceinline__ double r_to_double(dfl x) { return df_to_double(x); }
+__device__ __forceinline__ dfl r_add(dfl a, dfl b) { return df_add(a, b); }
+__device__ __forceinline__ dfl r_sub(dfl a, dfl b) { return df_sub(a, b); }
+__device__ __forceinline__ dfl r_mul(dfl a, dfl b) { return df_mul(a, b); }
+__device__ __forceinline__ void r_mac(dfl &acc, dfl a, dfl b) { df_mac(acc, a, b); }
+__device__ __forceinline__ dfl r_norm(dfl a) { return df_norm(a); }
+__device__ __forceinline__ dfl r_rsqrt(dfl a) { return df_rsqrt(a); }
+__device__ __forceinline__ dfl r_zero(dfl) { return dfl{0.0f, 0.0f}; }
+__device__ __forceinline__ void r_sincos(double theta, const DfTrigCoef &C, dfl &s, dfl &c) { df_sincos(theta, C, s, c); }
+
+template <class R> __device__ __forceinline__ R r_of_double(double x);
+template <> __device__ __forceinline__ double r_of_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ dfl r_of_double<dfl>(double x) { return df_from_double(x); }
+
+template <class R>
+struct cx {
+    R re, im;
+};
+
+template <class R> __device__ __forceinline__ cx<R> cx_zero() { return cx<R>{r_zero(R()), r_zero(R())}; }
+template <class R> __device__ __forceinline__ cx<R> cx_add(cx<R> a, cx<R> b) { return cx<R>{r_add(a.re, b.re), r_add(a.im, b.im)}; }
+template <class R> __device__ __forceinline__ cx<R> cx_mul(cx<R> a, cx<R> b)
+{
+    return cx<R>{r_sub(r_mul(a.re, b.re), r_mul(a.im, b.im)), r_add(r_mul(a.re, b.im), r_mul(a.im, b.re))};
+}
+template <class R> __device__ __forceinline__ cx<R> cx_norm(cx<R> a) { return cx<R>{r_norm(a.re), r_norm(a.im)}; }
 
 // per-frequency phase factors of one block
 struct FreqBlock {
@@ -45,59 +91,54 @@ struct FreqBlock {
 // Regular-rule integral of one element against x_o for the block's
 // frequencies.  qd: precomputed (x, y, z, wa0..2, wb0..2) for each point,
 // structure of arrays with stride n (elements) and 9 * n per point.
-__device__ __forceinline__ void regular_element(const double *__restrict__ qd, int n, int e, int nq, double nx,
-                                                double ny, double nz, double xo, double yo, double zo,
-                                                const FreqBlock &fb, double2 (&a)[IBEM_FB][3],
-                                                double2 (&b)[IBEM_FB][3], double &ct)
+template <class R>
+__device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
+                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[IBEM_FB],
+                                                const DfTrigCoef &C, cx<R> (&a)[IBEM_FB][3], cx<R> (&b)[IBEM_FB][3],
+                                                R &ct)
 {
     for (int q = 0; q < nq; ++q) {
-        const double *p = qd + (size_t)q * 9 * n + e;
-        const double dx = p[0] - xo, dy = p[(size_t)n] - yo, dz = p[2 * (size_t)n] - zo;
-        const double wa[3] = {p[3 * (size_t)n], p[4 * (size_t)n], p[5 * (size_t)n]};
-        const double wb[3] = {p[6 * (size_t)n], p[7 * (size_t)n], p[8 * (size_t)n]};
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        const double invr = rsqrt(r2);
-        const double r = r2 * invr;
-        const double ft = (nx * dx + ny * dy + nz * dz) * (invr * invr);
-        ct = fma(-(wa[0] + wa[1] + wa[2]) * ft, invr, ct);
-        double2 ph, step = make_double2(1.0, 0.0);
-        {
-            double s, c;
-            sincos(fb.k[0] * r, &s, &c);
-            ph = make_double2(c, s);
-            if (fb.uniform && fb.nf > 1) {
-                sincos(fb.dk * r, &s, &c);
-                step = make_double2(c, s);
-            }
-        }
+        const R *p = qd + (size_t)q * 9 * n + e;
+        const R dx = r_sub(p[0], xo), dy = r_sub(p[(size_t)n], yo), dz = r_sub(p[2 * (size_t)n], zo);
+        const R wa[3] = {p[3 * (size_t)n], p[4 * (size_t)n], p[5 * (size_t)n]};
+        const R wb[3] = {p[6 * (size_t)n], p[7 * (size_t)n], p[8 * (size_t)n]};
+        const R r2 = r_add(r_add(r_mul(dx, dx), r_mul(dy, dy)), r_mul(dz, dz));
+        const R invr = r_rsqrt(r2);
+        const R r = r_mul(r2, invr);
+        const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
+        const R ft = r_mul(nd, r_mul(invr, invr));
+        r_mac(ct, r_mul(r_add(r_add(wa[0], wa[1]), wa[2]), ft), r_sub(r_zero(R()), invr));
+        const double rd = r_to_double(r);
+        cx<R> ph, step;
+        r_sincos(fb.k[0] * rd, C, ph.im, ph.re);
+        if (fb.uniform && fb.nf > 1) r_sincos(fb.dk * rd, C, step.im, step.re);
+        R sa[3];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) sa[v] = r_mul(wa[v], ft);
 #pragma unroll
         for (int f = 0; f < IBEM_FB; ++f) {
             if (f >= fb.nf) break;
             if (f > 0) {
-                if (fb.uniform) ph = zmul(ph, step);
-                else {
-                    double s, c;
-                    sincos(fb.k[f] * r, &s, &c);
-                    ph = make_double2(c, s);
-                }
+                if (fb.uniform) ph = cx_mul(ph, step);
+                else r_sincos(fb.k[f] * rd, C, ph.im, ph.re);
             }
-            const double gr = ph.x * invr, gi = ph.y * invr;
-            const double kr = fb.k[f] * r;
-            const double tr = -gr - kr * gi, ti = kr * gr - gi;   // (ikr - 1) g
+            const R gr = r_mul(ph.re, invr), gi = r_mul(ph.im, invr);
+            const R kr = r_mul(kf[f], r);
+            const R tr = r_sub(r_sub(r_zero(R()), gr), r_mul(kr, gi));   // (ikr - 1) g
+            const R ti = r_sub(r_mul(kr, gr), gi);
 #pragma unroll
             for (int v = 0; v < 3; ++v) {
-                const double sa = wa[v] * ft;
-                a[f][v].x = fma(sa, tr, a[f][v].x);
-                a[f][v].y = fma(sa, ti, a[f][v].y);
-                b[f][v].x = fma(wb[v], gr, b[f][v].x);
-                b[f][v].y = fma(wb[v], gi, b[f][v].y);
+                r_mac(a[f][v].re, sa[v], tr);
+                r_mac(a[f][v].im, sa[v], ti);
+                r_mac(b[f][v].re, wb[v], gr);
+                r_mac(b[f][v].im, wb[v], gi);
             }
         }
     }
 }
 
 // Singular-rule integral of one element (raw geometry eg, rule SoA) against
-// x_o, lanes striding the points; reduced over the warp on return.
+// x_o, lanes striding the points, FP64; the caller reduces over the warp.
 __device__ __forceinline__ void singular_element(const double *__restrict__ eg, const double *__restrict__ rule, int nq,
                                                  double xo, double yo, double zo, const FreqBlock &fb, int lane,
                                                  double2 (&a)[IBEM_FB][3], double2 (&b)[IBEM_FB][3], double &ct)
@@ -138,15 +179,17 @@ __device__ __forceinline__ void singular_element(const double *__restrict__ eg, 
     }
 }
 
+template <class R>
 __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
-    const double *__restrict__ qdat, const int *__restrict__ evert, const int *__restrict__ color_ptr,
-    const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq, const double *__restrict__ sing, int nqs,
-    const double *__restrict__ mics, const double *__restrict__ cp, const double *__restrict__ kv, double c,
-    double rho, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
-    double2 *__restrict__ Bhs_t)
+    const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
+    const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
+    const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
+    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, double2 *__restrict__ At,
+    double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
 {
-    extern __shared__ double2 rowbuf[];   // IBEM_FB x (A row, B row), m each
+    extern __shared__ __align__(16) unsigned char ibem_smem[];
+    cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // IBEM_FB x (A row, B row), m each
     __shared__ double ct_red[IBEM_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int row = blockIdx.x;
@@ -161,7 +204,10 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
 #pragma unroll
     for (int f = 2; f < IBEM_FB; ++f)
         if (f < fb.nf && fabs(fb.k[f] - (fb.k[0] + f * fb.dk)) > 1e-12 * fabs(fb.k[f])) fb.uniform = false;
-    for (int j = tid; j < 2 * IBEM_FB * m; j += blockDim.x) rowbuf[j] = make_double2(0.0, 0.0);
+    R kf[IBEM_FB];
+#pragma unroll
+    for (int f = 0; f < IBEM_FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
+    for (int j = tid; j < 2 * IBEM_FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
     double xo, yo, zo;
     int self = -1;
     if (row < m) {
@@ -174,35 +220,37 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         int i = row - mt;
         xo = mics[i]; yo = mics[i + l]; zo = mics[i + 2 * l];
     }
+    const R xr = r_of_double<R>(xo), yr = r_of_double<R>(yo), zr = r_of_double<R>(zo);
     __syncthreads();
-    double ct = 0.0;
-    const double *nrm = egeo;   // normals at egeo[(9 + d) + 16 e]
+    R ctr = r_zero(R());
     for (int cidx = 0; cidx < ncolors; ++cidx) {
         const int e0 = color_ptr[cidx], e1 = color_ptr[cidx + 1];
         for (int e = e0 + tid; e < e1; e += blockDim.x) {
             const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
             if (vv.x == self || vv.y == self || vv.z == self) continue;
-            double2 a[IBEM_FB][3], b[IBEM_FB][3];
+            cx<R> a[IBEM_FB][3], b[IBEM_FB][3];
 #pragma unroll
             for (int f = 0; f < IBEM_FB; ++f)
 #pragma unroll
-                for (int v = 0; v < 3; ++v) { a[f][v] = make_double2(0.0, 0.0); b[f][v] = make_double2(0.0, 0.0); }
-            const double *g = nrm + (size_t)e * 16;
-            regular_element(qdat, n, e, nq, g[9], g[10], g[11], xo, yo, zo, fb, a, b, ct);
+                for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
+            regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, C,
+                               a, b, ctr);
+            ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
             for (int f = 0; f < IBEM_FB; ++f) {
                 if (f >= fb.nf) break;
-                double2 *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
+                cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
 #pragma unroll
                 for (int v = 0; v < 3; ++v) {
-                    Ar[cols[v]] = zadd(Ar[cols[v]], a[f][v]);
-                    Br[cols[v]] = zadd(Br[cols[v]], b[f][v]);
+                    Ar[cols[v]] = cx_add(Ar[cols[v]], cx_norm(a[f][v]));
+                    Br[cols[v]] = cx_add(Br[cols[v]], cx_norm(b[f][v]));
                 }
             }
         }
         __syncthreads();
     }
+    double ct = r_to_double(ctr);
     // singular elements of a surface row: one warp per incident element
     if (self >= 0) {
         const int a0 = adj_ptr[self], a1 = adj_ptr[self + 1];
@@ -237,11 +285,11 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
 #pragma unroll
                         for (int f = 0; f < IBEM_FB; ++f) {
                             if (f >= fb.nf) break;
-                            double2 *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
+                            cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
 #pragma unroll
                             for (int v = 0; v < 3; ++v) {
-                                Ar[cols[v]] = zadd(Ar[cols[v]], a[f][v]);
-                                Br[cols[v]] = zadd(Br[cols[v]], b[f][v]);
+                                Ar[cols[v]] = cx_add(Ar[cols[v]], cx<R>{r_of_double<R>(a[f][v].x), r_of_double<R>(a[f][v].y)});
+                                Br[cols[v]] = cx_add(Br[cols[v]], cx<R>{r_of_double<R>(b[f][v].x), r_of_double<R>(b[f][v].y)});
                             }
                         }
                     }
@@ -256,15 +304,19 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         if (tid == 0) {
             double tot = 0.0;
             for (int w = 0; w < IBEM_THREADS / 32; ++w) tot += ct_red[w];
-            for (int f = 0; f < fb.nf; ++f) rowbuf[(size_t)f * 2 * m + self].x -= 1.0 + tot;
+            const R diag = r_of_double<R>(-(1.0 + tot));
+            for (int f = 0; f < fb.nf; ++f) {
+                cx<R> &d = rowbuf[(size_t)f * 2 * m + self];
+                d.re = r_add(d.re, diag);
+            }
         }
         __syncthreads();
     }
-    // scale B by i rho c k and write the rows
+    // scale B by i rho c k and write the rows (FP64)
     for (int f = 0; f < fb.nf; ++f) {
         const int fg = f0 + f;
         const double s = rho * c * fb.k[f];
-        const double2 *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
+        const cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
         double2 *arow, *brow;
         if (row < mt) {
             arow = At ? At + ((size_t)fg * mt + row) * m : nullptr;
@@ -274,27 +326,38 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             brow = Bhs_t ? Bhs_t + ((size_t)fg * l + (row - mt)) * m : nullptr;
         }
         for (int j = tid; j < m; j += blockDim.x) {
-            if (arow) arow[j] = Ar[j];
-            const double2 bv = Br[j];
-            if (brow) brow[j] = make_double2(-s * bv.y, s * bv.x);
+            if (arow) arow[j] = make_double2(r_to_double(Ar[j].re), r_to_double(Ar[j].im));
+            const double br = r_to_double(Br[j].re), bi = r_to_double(Br[j].im);
+            if (brow) brow[j] = make_double2(-s * bi, s * br);
         }
     }
 }
 
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
-              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t)
+              const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
+              bool df32)
 {
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
     const int rows = m + n_ch + l;
     const size_t smem = sizeof(double2) * 2 * (size_t)m * IBEM_FB;
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
-    IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    static const DfTrigCoef coef = df_trig_coefficients();
     dim3 g(rows, (F + IBEM_FB - 1) / IBEM_FB);
-    ibem_rows_kernel<<<g, IBEM_THREADS, smem, ctx->stream>>>(
-        m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_evert,
-        mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, At,
-        Bt, Ahs_t, Bhs_t);
+    if (df32) {
+        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+        ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
+            m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
+            (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
+            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, At, Bt, Ahs_t, Bhs_t);
+    } else {
+        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         220 * 1024));
+        ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
+            m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
+            mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics,
+            cp, k, c, rho, coef, At, Bt, Ahs_t, Bhs_t);
+    }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }

@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_kernel(int M, int M
 // enough); V, when accumulated, stays in global memory and its two columns
 // are fetched before the dot products so their latency overlaps them.
 template <class T, int KPL>
-__global__ void __launch_bounds__(SVD_MAX_WARPS * 32) jacobi_smem_kernel(int M, int Mdot, int N, T *Yg, long long sY,
+__global__ void __launch_bounds__(sizeof(T) <= 8 ? 2 * SVD_MAX_WARPS * 32 : SVD_MAX_WARPS * 32)
+    jacobi_smem_kernel(int M, int Mdot, int N, T *Yg, long long sY,
                                                                            T *V, long long sV, int max_sweeps,
                                                                            typename ctraits<T>::R tol, int *info)
 {
@@ -267,15 +268,22 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     int nw = (N + 1) / 2;
     if (nw > SVD_MAX_WARPS) nw = SVD_MAX_WARPS;
     if (nw < 1) nw = 1;
-    const double eps = sizeof(R) == 8 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+    // FP64: rotate while |y_i^H y_j| > sqrt(Mdot) eps |y_i||y_j|.  FP32 (the
+    // mixed path, always followed by FP64 eigen-refinement): 8x that, above
+    // the rounding noise of FP32 dot products, so sweeps stop when the
+    // remaining rotations would only chase noise.
+    const double eps = sizeof(R) == 8 ? 2.220446049250313e-16 : 8.0 * 1.1920928955078125e-07;
     const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;
     const size_t smem = sizeof(T) * (size_t)M * N;
     if (M <= 128 && N <= 128 && smem <= 200 * 1024) {
+        const int wmax = sizeof(T) <= 8 ? 2 * SVD_MAX_WARPS : SVD_MAX_WARPS;
+        int nws = (N + 1) / 2 < wmax ? (N + 1) / 2 : wmax;
+        if (nws < 1) nws = 1;
         IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_smem_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          200 * 1024));
-        jacobi_smem_kernel<T, 4><<<batch, nw * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol,
-                                                                        info);
+        jacobi_smem_kernel<T, 4><<<batch, nws * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol,
+                                                                         info);
     } else if (M <= 128)
         jacobi_kernel<T, 4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     else if (M <= 256)

@@ -485,7 +485,9 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     if (st) return st;
     // 3. eigen-refinement from X = J (conj(J) for H^T input)
     if ((st = copy2d_batched<float2, double2>(ctx, N, N, J32, N, sN, X, N, sN, transposed, batch))) return st;
-    const int steps = cfg->refine_steps > 0 ? cfg->refine_steps : 1;
+    // the FP32 Jacobi leaves X accurate to ~1e-5 (its stopping threshold sits
+    // above FP32 rounding noise); two quadratic steps reach FP64 level
+    const int steps = cfg->refine_steps > 2 ? cfg->refine_steps : 2;
     for (int it = 0; it < steps; ++it) {
         if ((st = zgemm_batched(ctx, OP_N, OP_N, N, N, N, one, E, N, sN, X, N, sN, zero, T1, N, sN, batch))) return st;
         if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;

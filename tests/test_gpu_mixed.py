@@ -18,6 +18,26 @@ def T(a, dev):
     return torch.as_tensor(np.ascontiguousarray(a), device=dev)
 
 
+def test_mixed_assembly_matches_fp64(cuda, ctx):
+    """The mixed path assembles in double-float (FP32 pairs, own sin/cos by
+    Cody-Waite reduction + Taylor series): rows agree with the FP64 kernel
+    (CUDA sincos/rsqrt) to 1e-13, element by element to 1e-12."""
+    from inverseacoustics_gb300 import api
+    import torch
+    w = g.ibem_sphere(n_freq=64)
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    ks = w.k[[0, 1, 2, 3, 30, 61, 62, 63]]           # two uniform blocks + a non-uniform block edge
+    mesh = api.Mesh(ctx, nodes, elems)
+    r64 = api.ibem_assemble_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
+    rmx = api.ibem_assemble_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), api.default_config(precision=1))
+    torch.cuda.synchronize()
+    for a, b in zip(r64, rmx):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        for f in range(len(ks)):
+            assert relerr(b[f], a[f]) < 1e-13
+        assert np.max(np.abs(b - a)) < 1e-12 * np.max(np.abs(a))
+
+
 def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
     from inverseacoustics_gb300 import api
     import torch
