@@ -285,11 +285,16 @@ def run_ours(args):
         del a64
     except Exception:
         pass
-    roofline = {"kernel": "ibem_rows_kernel (assembly)", "bound": "hbm",
+    # DRAM bytes (read + write) of one 64-frequency launch of the mixed-path
+    # assembly kernel, from the ncu launch list in
+    # profiles/ibem_pipeline_mixed_launches_F64.txt (1891.5 MB over 2 launches)
+    asm_traffic = 945.8e6
+    roofline = {"kernel": "ibem_rows_kernel<dfl> (mixed-path assembly)", "bound": "hbm",
                 "achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": None,
+                "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": asm_traffic,
                 "peak_kind": peak_kind,
-                "note": "FP64-issue bound, not HBM bound; see compute",
+                "note": "issue/latency bound on the FP32 pipe (ncu: FMA 26%, FP64 34%, issue 32%), "
+                        "not HBM bound; traffic equals the algorithmic output",
                 "compute": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
                             "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
                             "peak_dgemm_measured": fp64_tflops_dgemm}}
