@@ -75,6 +75,9 @@ typedef struct {
     int svd_max_sweeps;    /* Jacobi sweep cap (default 40) */
     int refine_steps;      /* refinement steps of the mixed path: LU residual steps and
                               eigen-refinement steps (default 1; each squares the error) */
+    int mode_iters;        /* radiation modes: subspace iterations (default 10; FP32 in the
+                              mixed path, which then adds refine_steps FP64 ones) */
+    int mode_oversample;   /* radiation modes: subspace vectors beyond the requested modes (default 16) */
 } ia_config;
 
 /* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,
@@ -224,6 +227,32 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
 int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, const double *d_src, int F,
                        const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
                        double *d_lambda, double *d_s, int *d_info);
+
+/* Radiation resistance matrices of n baffled radiators of equal area at
+ * d_x (3 x n SoA) for F wavenumbers:
+ *   R_f(i,j) = omega^2 rho A^2 / (4 pi c) sinc(k_f r_ij),  omega = k_f c,
+ * real symmetric, column-major, d_R F x (n x n) FP64; c and rho from cfg.
+ * The reference names this model for its radiation-mode configuration but
+ * has no code for it (its BEM variant is invr(), CUDA/invr.cuh:457). */
+int ia_sinc_resistance_batch(ia_context *ctx, int n, const double *d_x, int F, const double *d_k, double area,
+                             const ia_config *cfg, double *d_R);
+
+/* Leading radiation modes: the nmodes largest eigenvalues (descending) and
+ * orthonormal eigenvectors of each real symmetric positive semidefinite
+ * R_f (d_R F x (n x n)), by subspace iteration on nmodes + cfg->mode_oversample
+ * vectors and an FP64 Rayleigh-Ritz step.  d_lambda F x nmodes, d_modes
+ * F x (n x nmodes), each mode's largest component positive.  Eigenvalues at
+ * rounding level (below ~1e-15 lambda_1) carry no digits.  No reference
+ * counterpart (the reference's invr() takes an SVD of a BEM resistance
+ * matrix, MATLAB/invrV.m:65-119). */
+int ia_radiation_modes_batch(ia_context *ctx, int n, int F, const double *d_R, int nmodes, const ia_config *cfg,
+                             double *d_lambda, double *d_modes, int *d_info);
+
+/* Sound power W_f,r = 1/2 Re(v^H R_f v) of F x nrhs velocity fields
+ * d_v F x (n x nrhs) (the reference's 1/2 Re(v^H p), CUDA/utils.cuh:265-280,
+ * with p = R v): d_W F x nrhs. */
+int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,
+                         double *d_W);
 
 /* The HELS pipeline (He of order n_sh at field points) for F frequencies. */
 int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, int nrhs,

@@ -31,7 +31,8 @@ class Config(C.Structure):
     _fields_ = [("c", C.c_double), ("rho", C.c_double), ("method", C.c_int), ("gcv_mode", C.c_int),
                 ("gcv_points", C.c_int), ("gcv_lo", C.c_double), ("gcv_hi", C.c_double),
                 ("lambda_fixed", C.c_double), ("tsvd_k", C.c_int), ("precision", C.c_int),
-                ("svd_max_sweeps", C.c_int), ("refine_steps", C.c_int)]
+                ("svd_max_sweeps", C.c_int), ("refine_steps", C.c_int), ("mode_iters", C.c_int),
+                ("mode_oversample", C.c_int)]
 
 
 class Rules(C.Structure):
@@ -78,6 +79,9 @@ _SIGS = {
     "ia_ibem_solve_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_esm_solve_batch": (_I, [_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_hels_solve_batch": (_I, [_P, _I, _P, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_sinc_resistance_batch": (_I, [_P, _I, _P, _I, _P, _D, _P, _P]),
+    "ia_radiation_modes_batch": (_I, [_P, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "ia_sound_power_batch": (_I, [_P, _I, _I, _P, _I, _P, _P]),
 }
 
 

@@ -377,3 +377,41 @@ def hels_solve_batch(ctx, pts, n_sh, k, p, cfg=None):
                                          _dptr(k, torch.float64), nrhs, _dptr(p), C.byref(cfg), _dptr(x), _dptr(lam),
                                          _dptr(s), _dptr(info)), "ia_hels_solve_batch")
     return x, lam, s, info
+
+
+def sinc_resistance_batch(ctx, x, k, area, cfg=None):
+    """R (F, n, n) float64: omega^2 rho A^2/(4 pi c) sinc(k r_ij) for radiators
+    at x (3 x n SoA, device) and wavenumbers k (F, device).  Symmetric, so the
+    row-major tensor equals the column-major matrix."""
+    import torch
+    n, F = x.shape[-1], k.numel()
+    R = torch.empty((F, n, n), dtype=torch.float64, device=k.device)
+    check(_lib.lib().ia_sinc_resistance_batch(ctx.handle, n, _dptr(x, torch.float64), F, _dptr(k, torch.float64),
+                                              float(area), C.byref(cfg) if cfg is not None else None, _dptr(R)),
+          "ia_sinc_resistance_batch")
+    return R
+
+
+def radiation_modes_batch(ctx, R, nmodes, cfg=None):
+    """Leading nmodes eigenpairs of each R[f]: (lambda (F, nmodes) descending,
+    modes (F, nmodes, n) -- mode j of frequency f is modes[f, j], info (F))."""
+    import torch
+    cfg = cfg or default_config()
+    F, n = R.shape[0], R.shape[-1]
+    lam = torch.empty((F, nmodes), dtype=torch.float64, device=R.device)
+    modes = torch.empty((F, nmodes, n), dtype=torch.float64, device=R.device)
+    info = torch.zeros(F, dtype=torch.int32, device=R.device)
+    check(_lib.lib().ia_radiation_modes_batch(ctx.handle, n, F, _dptr(R, torch.float64), int(nmodes), C.byref(cfg),
+                                              _dptr(lam), _dptr(modes), _dptr(info)), "ia_radiation_modes_batch")
+    return lam, modes, info
+
+
+def sound_power_batch(ctx, R, v):
+    """W (F, nrhs) = 1/2 Re(v^H R v) for velocity fields v (F, nrhs, n) complex128."""
+    import torch
+    F, n = R.shape[0], R.shape[-1]
+    nrhs = v.shape[1]
+    W = torch.empty((F, nrhs), dtype=torch.float64, device=R.device)
+    check(_lib.lib().ia_sound_power_batch(ctx.handle, n, F, _dptr(R, torch.float64), nrhs, _dptr(v), _dptr(W)),
+          "ia_sound_power_batch")
+    return W

@@ -184,6 +184,8 @@ void ia_config_default(ia_config *cfg)
     cfg->precision = IA_PREC_FP64;
     cfg->svd_max_sweeps = 40;
     cfg->refine_steps = 1;
+    cfg->mode_iters = 10;
+    cfg->mode_oversample = 16;
 }
 
 const char *ia_status_string(int status)
@@ -667,6 +669,38 @@ int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, i
     if (st) return st;
     return solve_core(ctx, l, nt, F, H, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
                       cur);
+}
+
+int ia_sinc_resistance_batch(ia_context *ctx, int n, const double *d_x, int F, const double *d_k, double area,
+                             const ia_config *cfg, double *d_R)
+{
+    if (!ctx || n < 1 || F < 1 || !d_x || !d_k || !d_R || !(area > 0.0)) return IA_ERR_ARG;
+    ia_config dc;
+    if (!cfg) { ia_config_default(&dc); cfg = &dc; }
+    return sinc_resistance_batched(ctx, n, d_x, F, d_k, area, cfg->c, cfg->rho, d_R, nullptr);
+}
+
+int ia_radiation_modes_batch(ia_context *ctx, int n, int F, const double *d_R, int nmodes, const ia_config *cfg,
+                             double *d_lambda, double *d_modes, int *d_info)
+{
+    if (!ctx || !cfg || n < 1 || F < 1 || nmodes < 1 || nmodes > n || !d_R || !d_lambda || !d_modes || !d_info ||
+        cfg->mode_iters < 0 || cfg->mode_oversample < 0)
+        return IA_ERR_ARG;
+    int st = ws_reserve(ctx, radiation_modes_ws_bytes(n, F, nmodes, cfg));
+    if (!st) st = clear_info(ctx, d_info, F);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return radiation_modes_batched(ctx, n, F, d_R, nmodes, cfg, d_lambda, d_modes, d_info, cur);
+}
+
+int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,
+                         double *d_W)
+{
+    if (!ctx || n < 1 || F < 1 || nrhs < 1 || !d_R || !d_v || !d_W) return IA_ERR_ARG;
+    int st = ws_reserve(ctx, sound_power_ws_bytes(n, F));
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return sound_power_batched(ctx, n, F, d_R, nrhs, (const double2 *)d_v, d_W, cur);
 }
 
 }  // extern "C"

@@ -167,6 +167,13 @@ size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                              const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
                              int *info, WsCursor &cur);
+// Householder QR (reflectors below the diagonal, tau per column) and the
+// explicit product X = Q [W; 0] (wide_solve.cu)
+template <class T>
+int qr_batched(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int batch);
+template <class T>
+int apply_q_batched(ia_context *ctx, int rows, int cols, const T *Y, const T *tau, int ncol, const T *W, int ldw,
+                    long long sW, T *X, long long sX, int batch);
 // out += in (FP32 or FP64 in, FP64 out), rows x cols per matrix
 template <class TI>
 int add2d_batched(ia_context *ctx, int rows, int cols, const TI *in, int ldi, long long si, double2 *out, int ldo,
@@ -183,5 +190,16 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
               bool df32 = false);
 int hels_batched(ia_context *ctx, int npts, const double *pts, int order, int F, const double *k, double c,
                  double rho, double2 *Me, double2 *Qe);
+
+// ---- radiation modes (radiation.cu)
+// R (F x n x n FP64) and optionally an FP32 copy R32
+int sinc_resistance_batched(ia_context *ctx, int n, const double *x, int F, const double *k, double area, double c,
+                            double rho, double *R, float *R32);
+size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg);
+int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int nm, const ia_config *cfg,
+                            double *lambda, double *modes, int *info, WsCursor &cur);
+size_t sound_power_ws_bytes(int n, int F);
+int sound_power_batched(ia_context *ctx, int n, int F, const double *R, int nrhs, const double2 *v, double *W,
+                        WsCursor &cur);
 
 }  // namespace ia

@@ -98,6 +98,16 @@ int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, lon
     return IA_OK;
 }
 
+template <class T>
+int qr_batched(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int batch)
+{
+    qr_kernel<T><<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, tau, 0, nullptr, 0, 0);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+template int qr_batched<float2>(ia_context *, int, int, float2 *, int, long long, float2 *, int);
+template int qr_batched<double2>(ia_context *, int, int, double2 *, int, long long, double2 *, int);
+
 // Raug ((N + nrhs) x N): R (upper triangle of Y, or all of Y when full) over
 // the rows conj(b_r)^T.
 template <class T>
@@ -196,6 +206,19 @@ __global__ void apply_q_kernel(int rows, int cols, const T *Y, const T *TAU, int
         }
     }
 }
+
+template <class T>
+int apply_q_batched(ia_context *ctx, int rows, int cols, const T *Y, const T *tau, int ncol, const T *W, int ldw,
+                    long long sW, T *X, long long sX, int batch)
+{
+    apply_q_kernel<T><<<batch, 256, 0, ctx->stream>>>(rows, cols, Y, tau, ncol, W, ldw, sW, X, sX);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+template int apply_q_batched<float2>(ia_context *, int, int, const float2 *, const float2 *, int, const float2 *, int,
+                                     long long, float2 *, long long, int);
+template int apply_q_batched<double2>(ia_context *, int, int, const double2 *, const double2 *, int, const double2 *,
+                                      int, long long, double2 *, long long, int);
 
 size_t wide_solve_ws_bytes(int m, int n, int nrhs, int batch)
 {

@@ -78,6 +78,17 @@ def plate_grid(lx: float, ly: float, nx: int, ny: int):
     return np.ascontiguousarray(P), dx * dy
 
 
+def rayleigh_pressure(P, centres, area, k, vel, c=C_DEFAULT, rho=RHO_DEFAULT):
+    """Pressure at points P (3, l) radiated by a baffled plate of elements of
+    equal area at centres (3, n) with normal velocity vel (n,), by the
+    midpoint-rule Rayleigh integral p = -i omega rho/(2 pi) sum A v e^{ikR}/R.
+    In the monopole form p = G q, G = e^{ikR}/(4 pi R), the equivalent source
+    strengths are q = -2 i omega rho A v."""
+    R = np.sqrt(((P.T[:, None, :] - centres.T[None, :, :]) ** 2).sum(-1))
+    G = np.exp(1j * k * R) / (4 * np.pi * R)
+    return G @ (-2j * k * c * rho * area * np.asarray(vel))
+
+
 def planar_array(nx: int, ny: int, pitch: float, z: float):
     """nx x ny microphones on a grid of the given pitch, centred on the z axis."""
     xs = (np.arange(nx) - (nx - 1) / 2) * pitch
