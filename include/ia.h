@@ -254,6 +254,24 @@ int ia_radiation_modes_batch(ia_context *ctx, int n, int F, const double *d_R, i
 int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,
                          double *d_W);
 
+/* Differentiable ESM array design (no reference counterpart; the operator is
+ * the plain monopole G of MATLAB/esmV.m:29-30, the inverse Tikhonov,
+ * MATLAB/regtools/tikhonovG.m:26-30).  Equivalent sources
+ * s_j = u_j (1 - retreat / |u_j|) from surface points d_surface (3 x m),
+ * microphones d_mics (3 x l, l <= m), source fields d_q F x (m x nrhs),
+ * pressures p = G q + noise (d_noise F x (l x nrhs), or NULL), reconstruction
+ * q^ = G^H (G G^H + lambda_f^2 I)^-1 p with lambda_f = exp(d_loglam[f]).
+ * d_err F x nrhs receives ||q^ - q|| / ||q||; the gradients of their mean with
+ * respect to the microphone coordinates (d_grad_mics 3 x l SoA), the retreat
+ * (d_grad_retreat, 1) and the log lambdas (d_grad_loglam, F) come from a
+ * hand-written adjoint.  The retreat is a device scalar so optimisers can
+ * update it without a host round trip.  The three gradient pointers are all
+ * NULL (forward only) or all set.  nrhs <= 32.  FP64. */
+int ia_esm_design_batch(ia_context *ctx, int l, int m, int F, int nrhs, const double *d_mics,
+                        const double *d_surface, const double *d_retreat, const double *d_k, const double *d_loglam,
+                        const ia_complex *d_q, const ia_complex *d_noise, double *d_err, double *d_grad_mics,
+                        double *d_grad_retreat, double *d_grad_loglam, int *d_info);
+
 /* The HELS pipeline (He of order n_sh at field points) for F frequencies. */
 int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, int nrhs,
                         const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x, double *d_lambda,

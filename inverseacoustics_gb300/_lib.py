@@ -82,6 +82,7 @@ _SIGS = {
     "ia_sinc_resistance_batch": (_I, [_P, _I, _P, _I, _P, _D, _P, _P]),
     "ia_radiation_modes_batch": (_I, [_P, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ia_sound_power_batch": (_I, [_P, _I, _I, _P, _I, _P, _P]),
+    "ia_esm_design_batch": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 }
 
 

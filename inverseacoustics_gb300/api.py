@@ -415,3 +415,29 @@ def sound_power_batch(ctx, R, v):
     check(_lib.lib().ia_sound_power_batch(ctx.handle, n, F, _dptr(R, torch.float64), nrhs, _dptr(v), _dptr(W)),
           "ia_sound_power_batch")
     return W
+
+
+def esm_design_batch(ctx, mics, surface, retreat, k, loglam, q, noise=None, grad=True):
+    """Differentiable ESM design objective on the device.
+
+    mics (3, l), surface (3, m), retreat (1,), k (F,), loglam (F,) float64 and
+    q (F, nrhs, m), noise (F, nrhs, l) complex128 CUDA tensors.  Returns
+    (err (F, nrhs), grad_mics (3, l), grad_retreat (1,), grad_loglam (F,),
+    info (F,)); the gradients are those of err.mean() and are None when
+    grad is False."""
+    import torch
+    l, m, F, nrhs = mics.shape[-1], surface.shape[-1], k.numel(), q.shape[1]
+    dev = k.device
+    err = torch.empty((F, nrhs), dtype=torch.float64, device=dev)
+    info = torch.zeros(F, dtype=torch.int32, device=dev)
+    gm = gd = gl = None
+    if grad:
+        gm = torch.empty((3, l), dtype=torch.float64, device=dev)
+        gd = torch.empty(1, dtype=torch.float64, device=dev)
+        gl = torch.empty(F, dtype=torch.float64, device=dev)
+    check(_lib.lib().ia_esm_design_batch(ctx.handle, l, m, F, nrhs, _dptr(mics, torch.float64),
+                                         _dptr(surface, torch.float64), _dptr(retreat, torch.float64),
+                                         _dptr(k, torch.float64), _dptr(loglam, torch.float64), _dptr(q),
+                                         _dptr(noise), _dptr(err), _dptr(gm), _dptr(gd), _dptr(gl), _dptr(info)),
+          "ia_esm_design_batch")
+    return err, gm, gd, gl, info

@@ -693,6 +693,25 @@ int ia_radiation_modes_batch(ia_context *ctx, int n, int F, const double *d_R, i
     return radiation_modes_batched(ctx, n, F, d_R, nmodes, cfg, d_lambda, d_modes, d_info, cur);
 }
 
+int ia_esm_design_batch(ia_context *ctx, int l, int m, int F, int nrhs, const double *d_mics,
+                        const double *d_surface, const double *d_retreat, const double *d_k, const double *d_loglam,
+                        const ia_complex *d_q, const ia_complex *d_noise, double *d_err, double *d_grad_mics,
+                        double *d_grad_retreat, double *d_grad_loglam, int *d_info)
+{
+    if (!ctx || l < 1 || m < l || F < 1 || nrhs < 1 || nrhs > 32 || !d_mics || !d_surface || !d_retreat || !d_k ||
+        !d_loglam || !d_q || !d_err || !d_info)
+        return IA_ERR_ARG;
+    const int ng = (d_grad_mics != nullptr) + (d_grad_retreat != nullptr) + (d_grad_loglam != nullptr);
+    if (ng != 0 && ng != 3) return IA_ERR_ARG;
+    int st = ws_reserve(ctx, esm_design_ws_bytes(l, m, F, nrhs));
+    if (!st) st = clear_info(ctx, d_info, F);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return esm_design_batched(ctx, l, m, F, nrhs, d_mics, d_surface, d_retreat, d_k, d_loglam, (const double2 *)d_q,
+                              (const double2 *)d_noise, d_err, d_grad_mics, d_grad_retreat, d_grad_loglam, d_info,
+                              cur);
+}
+
 int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,
                          double *d_W)
 {

@@ -199,6 +199,13 @@ size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg);
 int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int nm, const ia_config *cfg,
                             double *lambda, double *modes, int *info, WsCursor &cur);
 size_t sound_power_ws_bytes(int n, int F);
+
+// ---- differentiable ESM design (adjoint.cu); gm == nullptr: forward only
+size_t esm_design_ws_bytes(int l, int m, int F, int R);
+int esm_design_batched(ia_context *ctx, int l, int m, int F, int R, const double *mics, const double *surf,
+                       const double *retreat, const double *k, const double *loglam, const double2 *q,
+                       const double2 *noise, double *err, double *gm, double *gd, double *gl, int *info,
+                       WsCursor &cur);
 int sound_power_batched(ia_context *ctx, int n, int F, const double *R, int nrhs, const double2 *v, double *W,
                         WsCursor &cur);
 

@@ -462,3 +462,72 @@ def solve_tikhonov_gcv(H, b, npoints=200, grid=None, mode="standard"):
     U, s, V = csvd(H)
     lam = gcv(U, s, b, npoints, grid, mode)
     return tikhonov(U, s, V, b, lam), lam, s
+
+
+# ---------------------------------------------------------------------------
+# Differentiable ESM array design (no reference code; the forward operator is
+# the plain monopole G of esmV.m:29-30, the inverse tikhonovG.m:26-30 in its
+# data-space form).  FP64 reference loss and analytic gradient.
+# ---------------------------------------------------------------------------
+def esm_design_solve(mics, surface, retreat, k, lam, q, noise=None):
+    """One frequency: G, p = G q (+ noise), y = (G G^H + lam^2 I)^-1 p,
+    q^ = G^H y.  q (m, R).  Returns (G, y, qhat)."""
+    src = retreat_sources(surface, retreat)
+    G = monopole_matrix(mics, src, k)
+    p = G @ q
+    if noise is not None:
+        p = p + noise
+    K = G @ G.conj().T + lam * lam * np.eye(G.shape[0])
+    y = np.linalg.solve(K, p)
+    return G, y, G.conj().T @ y
+
+
+def esm_design_terms(mics, surface, retreat, k, loglam, q, noise=None):
+    """Relative reconstruction errors ||q^ - q|| / ||q|| per (frequency,
+    field): k, loglam (F,), q (F, m, R), noise (F, l, R) or None -> (F, R)."""
+    F, R = q.shape[0], q.shape[2]
+    out = np.zeros((F, R))
+    for f in range(F):
+        nz = None if noise is None else noise[f]
+        _, _, qh = esm_design_solve(mics, surface, retreat, k[f], math.exp(loglam[f]), q[f], nz)
+        out[f] = np.linalg.norm(qh - q[f], axis=0) / np.linalg.norm(q[f], axis=0)
+    return out
+
+
+def esm_design_loss(mics, surface, retreat, k, loglam, q, noise=None):
+    """Mean relative reconstruction error over frequencies and fields."""
+    return float(esm_design_terms(mics, surface, retreat, k, loglam, q, noise).mean())
+
+
+def esm_design_grad(mics, surface, retreat, k, loglam, q, noise=None):
+    """Gradient of esm_design_loss by the adjoint of the Tikhonov solve:
+    with e = q^ - q, g = e / (||e|| ||q|| F R), z = K^-1 G g, w = g - G^H z,
+    dL = Re sum_ij A_ij dG_ij - 2 lam^2 Re(z^H y) dloglam,
+    A_ij = sum_r conj(y_ir) w_jr - conj(z_ir) e_jr,
+    dG_ij = G_ij (ik - 1/r_ij) dr_ij.  Returns (dL/dmics (3, l), dL/dretreat,
+    dL/dloglam (F,))."""
+    M = _soa(mics)
+    S = _soa(surface)
+    unit = S / np.linalg.norm(S, axis=0)
+    src = retreat_sources(surface, retreat)
+    F, R = q.shape[0], q.shape[2]
+    gm = np.zeros_like(M)
+    gd = 0.0
+    gl = np.zeros(F)
+    for f in range(F):
+        lam = math.exp(loglam[f])
+        nz = None if noise is None else noise[f]
+        G, y, qh = esm_design_solve(mics, surface, retreat, k[f], lam, q[f], nz)
+        K = G @ G.conj().T + lam * lam * np.eye(G.shape[0])
+        e = qh - q[f]
+        g = e / (np.linalg.norm(e, axis=0) * np.linalg.norm(q[f], axis=0) * F * R)
+        z = np.linalg.solve(K, G @ g)
+        w = g - G.conj().T @ z
+        A = y.conj() @ w.T - z.conj() @ e.T
+        D = M[:, :, None] - src[:, None, :]                  # (3, l, m)
+        r = np.sqrt((D * D).sum(0))
+        c = np.real(A * G * (1j * k[f] - 1.0 / r)) / r
+        gm += (c[None] * D).sum(2)
+        gd += float((c[None] * D * unit[:, None, :]).sum())
+        gl[f] = -2.0 * lam * lam * float(np.real(np.sum(z.conj() * y)))
+    return gm, gd, gl

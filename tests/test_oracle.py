@@ -160,3 +160,39 @@ def test_sinc_resistance_properties():
     assert w.min() > -1e-10 * w.max()          # positive semidefinite
     om = k * 343.0
     assert abs(R[0, 0] - om * om * 1.21 * area * area / (4 * np.pi * 343.0)) < 1e-12 * R[0, 0]
+
+
+def _design_case(seed=0, l=12, subdiv=1, F=3, R=4):
+    rng = np.random.default_rng(seed)
+    surf, _ = g.icosphere(subdiv, 0.1)
+    mics = np.stack([rng.uniform(-.2, .2, l), rng.uniform(-.2, .2, l), np.full(l, .12)])
+    k = 2 * np.pi * np.linspace(300.0, 3000.0, F) / 343.0
+    q = g.complex_normal(rng, (F, surf.shape[1], R))
+    noise = 0.01 * g.complex_normal(rng, (F, l, R))
+    loglam = np.array([math.log(0.05 * np.linalg.norm(O.monopole_matrix(mics, O.retreat_sources(surf, 0.04), kk), 2))
+                       for kk in k])
+    return mics, surf, 0.04, k, loglam, q, noise
+
+
+def test_design_gradient_matches_central_differences():
+    """The FP64 reference gradient of the design loss (adjoint of the
+    Tikhonov solve) against central differences, h = 1e-6."""
+    mics, surf, d, k, ll, q, noise = _design_case()
+    gm, gd, gl = O.esm_design_grad(mics, surf, d, k, ll, q, noise)
+    h = 1e-6
+
+    def L(M=mics, D=d, LL=ll):
+        return O.esm_design_loss(M, surf, D, k, LL, q, noise)
+
+    fd = np.zeros_like(gm)
+    for a in range(3):
+        for i in range(mics.shape[1]):
+            Mp, Mm = mics.copy(), mics.copy()
+            Mp[a, i] += h
+            Mm[a, i] -= h
+            fd[a, i] = (L(M=Mp) - L(M=Mm)) / (2 * h)
+    assert np.max(np.abs(fd - gm)) <= 1e-6 * np.max(np.abs(gm))
+    assert abs((L(D=d + h) - L(D=d - h)) / (2 * h) - gd) <= 1e-6 * abs(gd)
+    E = np.eye(len(k))
+    fl = np.array([(L(LL=ll + h * E[f]) - L(LL=ll - h * E[f])) / (2 * h) for f in range(len(k))])
+    assert np.max(np.abs(fl - gl)) <= 1e-6 * np.max(np.abs(gl))
