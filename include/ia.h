@@ -49,7 +49,8 @@ typedef enum {
     IA_ERR_SINGULAR = 5,     /* an exactly zero pivot in an LU factorisation */
     IA_ERR_NONFINITE = 6,    /* NaN or Inf in an input or a result */
     IA_ERR_RULE = 7,         /* invalid quadrature rule */
-    IA_ERR_TOO_LARGE = 8     /* size above a fixed limit of the called entry point */
+    IA_ERR_TOO_LARGE = 8,    /* size above a fixed limit of the called entry point */
+    IA_ERR_CAPTURE = 9       /* the call would allocate during stream capture: run it once uncaptured first */
 } ia_status;
 
 /* per-frequency info words written by the batched solvers (bit flags) */
@@ -150,6 +151,25 @@ int ia_set_stream(ia_context *ctx, void *stream);
 int ia_synchronize(ia_context *ctx);
 /* number of kernels this context has launched since creation */
 long long ia_launch_count(const ia_context *ctx);
+
+/* CUDA graphs of batched calls (no reference counterpart: the reference
+ * creates streams and handles per call).  Between ia_capture_begin and
+ * ia_capture_end the context's stream records instead of running; the
+ * recorded kernels, copies and memsets replay with ia_graph_launch on the
+ * context's current stream, reading and writing the same device buffers, so a
+ * caller refills its input buffers and replays.  The context's stream must be
+ * a created stream (not the legacy default one).  A captured call must not
+ * grow the workspace: run it once uncaptured first (otherwise it returns
+ * IA_ERR_CAPTURE).  The graph holds pointers into the context's workspace:
+ * keep the context alive and do not run larger calls on it before the last
+ * replay. */
+typedef struct ia_graph ia_graph;
+int ia_capture_begin(ia_context *ctx);
+int ia_capture_end(ia_context *ctx, ia_graph **graph);
+int ia_graph_launch(ia_graph *graph);
+/* kernel nodes in the graph */
+int ia_graph_kernel_count(const ia_graph *graph);
+int ia_graph_destroy(ia_graph *graph);
 
 /* Upload a triangle mesh (host arrays) with its quadrature rules; builds the
  * element geometry, the element colouring and the node-to-element adjacency

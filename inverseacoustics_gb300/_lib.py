@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(HERE, "libia.so")
 IA_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "allocation failed",
           4: "Jacobi iteration did not converge", 5: "singular matrix", 6: "non-finite value",
-          7: "invalid quadrature rule", 8: "size above the entry point's limit"}
+          7: "invalid quadrature rule", 8: "size above the entry point's limit",
+          9: "workspace would grow during stream capture"}
 IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE = 1, 2, 4
 IA_GCV_STANDARD, IA_GCV_REFERENCE = 0, 1
 IA_PREC_FP64, IA_PREC_MIXED = 0, 1
@@ -66,6 +67,11 @@ _SIGS = {
     "ia_set_stream": (_I, [_P, _P]),
     "ia_synchronize": (_I, [_P]),
     "ia_launch_count": (C.c_longlong, [_P]),
+    "ia_capture_begin": (_I, [_P]),
+    "ia_capture_end": (_I, [_P, _PP]),
+    "ia_graph_launch": (_I, [_P]),
+    "ia_graph_kernel_count": (_I, [_P]),
+    "ia_graph_destroy": (_I, [_P]),
     "ia_mesh_create": (_I, [_P, _I, _I, _P, _P, _P, _PP]),
     "ia_mesh_destroy": (_I, [_P]),
     "ia_monopole_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P]),

@@ -18,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import IAError, check, default_config  # noqa: F401
+from ._lib import IA_OK, IAError, check, default_config  # noqa: F401
 
 _P = C.c_void_p
 
@@ -199,9 +199,49 @@ class Context:
     def synchronize(self):
         check(_lib.lib().ia_synchronize(self._h), "ia_synchronize")
 
+    def capture(self, fn):
+        """Record fn() (batched calls on this context) into a CUDA graph.
+        Run fn once uncaptured first so the workspace is sized; the stream
+        must be a created stream, e.g. torch.cuda.Stream()."""
+        L = _lib.lib()
+        check(L.ia_capture_begin(self._h), "ia_capture_begin")
+        g = _P()
+        try:
+            fn()
+        except BaseException:
+            if L.ia_capture_end(self._h, C.byref(g)) == IA_OK:
+                L.ia_graph_destroy(g)
+            raise
+        check(L.ia_capture_end(self._h, C.byref(g)), "ia_capture_end")
+        return Graph(g)
+
     def close(self):
         if self._h:
             _lib.lib().ia_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Graph:
+    """A captured sequence of batched calls (ia_graph)."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def launch(self):
+        check(_lib.lib().ia_graph_launch(self._h), "ia_graph_launch")
+
+    def kernel_count(self) -> int:
+        return int(_lib.lib().ia_graph_kernel_count(self._h))
+
+    def close(self):
+        if self._h:
+            _lib.lib().ia_graph_destroy(self._h)
             self._h = _P()
 
     def __del__(self):
@@ -330,33 +370,44 @@ def solve_batch(ctx, H_colmajor, m, n, b, cfg=None):
     return x, lam, s, info
 
 
-def ibem_solve_batch(ctx, mesh, mics, k, p, cfg=None):
+def ibem_solve_outputs(mesh, mics, k, p):
+    """Output tensors (x, lambda, s, info) for ibem_solve_batch."""
+    import torch
+    l, F, nrhs, m, dev = mics.shape[-1], k.numel(), p.shape[1], mesh.m, k.device
+    return (torch.empty((F, nrhs, m), dtype=torch.complex128, device=dev),
+            torch.empty((F, nrhs), dtype=torch.float64, device=dev),
+            torch.empty((F, min(l, m)), dtype=torch.float64, device=dev),
+            torch.zeros(F, dtype=torch.int32, device=dev))
+
+
+def ibem_solve_batch(ctx, mesh, mics, k, p, cfg=None, out=None):
     """The IBEM pipeline: p (F, nrhs, l) measured pressures -> surface
-    velocity x (F, nrhs, m), lambda (F, nrhs), s (F, min(l, m)), info (F,)."""
+    velocity x (F, nrhs, m), lambda (F, nrhs), s (F, min(l, m)), info (F,).
+    out: preallocated outputs (ibem_solve_outputs), e.g. for graph capture."""
     import torch
     cfg = cfg or default_config()
     l, F, nrhs = mics.shape[-1], k.numel(), p.shape[1]
-    m = mesh.m
-    dev = k.device
-    x = torch.empty((F, nrhs, m), dtype=torch.complex128, device=dev)
-    lam = torch.empty((F, nrhs), dtype=torch.float64, device=dev)
-    s = torch.empty((F, min(l, m)), dtype=torch.float64, device=dev)
-    info = torch.zeros(F, dtype=torch.int32, device=dev)
+    x, lam, s, info = out if out is not None else ibem_solve_outputs(mesh, mics, k, p)
     check(_lib.lib().ia_ibem_solve_batch(ctx.handle, mesh._h, l, _dptr(mics, torch.float64), F,
                                          _dptr(k, torch.float64), nrhs, _dptr(p), C.byref(cfg), _dptr(x), _dptr(lam),
                                          _dptr(s), _dptr(info)), "ia_ibem_solve_batch")
     return x, lam, s, info
 
 
-def esm_solve_batch(ctx, mics, src, k, p, cfg=None):
+def esm_solve_batch(ctx, mics, src, k, p, cfg=None, out=None):
+    """The ESM pipeline: p (F, nrhs, l) -> source strengths x (F, nrhs, m),
+    lambda (F, nrhs), s (F, min(l, m)), info (F,); out: preallocated outputs."""
     import torch
     cfg = cfg or default_config()
     l, m, F, nrhs = mics.shape[-1], src.shape[-1], k.numel(), p.shape[1]
     dev = k.device
-    x = torch.empty((F, nrhs, m), dtype=torch.complex128, device=dev)
-    lam = torch.empty((F, nrhs), dtype=torch.float64, device=dev)
-    s = torch.empty((F, min(l, m)), dtype=torch.float64, device=dev)
-    info = torch.zeros(F, dtype=torch.int32, device=dev)
+    if out is not None:
+        x, lam, s, info = out
+    else:
+        x = torch.empty((F, nrhs, m), dtype=torch.complex128, device=dev)
+        lam = torch.empty((F, nrhs), dtype=torch.float64, device=dev)
+        s = torch.empty((F, min(l, m)), dtype=torch.float64, device=dev)
+        info = torch.zeros(F, dtype=torch.int32, device=dev)
     check(_lib.lib().ia_esm_solve_batch(ctx.handle, l, m, _dptr(mics, torch.float64), _dptr(src, torch.float64), F,
                                         _dptr(k, torch.float64), nrhs, _dptr(p), C.byref(cfg), _dptr(x), _dptr(lam),
                                         _dptr(s), _dptr(info)), "ia_esm_solve_batch")

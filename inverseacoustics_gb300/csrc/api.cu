@@ -24,6 +24,7 @@ int cuda_status(cudaError_t e)
 int ws_reserve(ia_context *ctx, size_t bytes)
 {
     if (bytes <= ctx->ws_bytes) return IA_OK;
+    if (ctx->capturing) return IA_ERR_CAPTURE;
     if (ctx->ws) {
         cudaError_t e = cudaFreeAsync(ctx->ws, ctx->stream);
         ctx->ws = nullptr;
@@ -200,6 +201,7 @@ const char *ia_status_string(int status)
     case IA_ERR_NONFINITE: return "non-finite value";
     case IA_ERR_RULE: return "invalid quadrature rule";
     case IA_ERR_TOO_LARGE: return "size above the entry point's limit";
+    case IA_ERR_CAPTURE: return "workspace would grow during stream capture";
     default: return "unknown status";
     }
 }
@@ -239,15 +241,19 @@ int ia_destroy(ia_context *ctx)
 
 int ia_set_stream(ia_context *ctx, void *stream)
 {
-    if (!ctx) return IA_ERR_ARG;
-    if (ctx->ws) {
-        // the workspace was allocated on the old stream: release it there
-        cudaFreeAsync(ctx->ws, ctx->stream);
-        cudaStreamSynchronize(ctx->stream);
-        ctx->ws = nullptr;
-        ctx->ws_bytes = 0;
+    if (!ctx || ctx->capturing) return IA_ERR_ARG;
+    cudaStream_t ns = (cudaStream_t)stream;
+    if (ctx->ws && ns != ctx->stream) {
+        // keep the workspace: work on the new stream waits for what the old
+        // stream has queued on it
+        cudaEvent_t ev;
+        IA_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t e = cudaEventRecord(ev, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ns, ev, 0);
+        cudaEventDestroy(ev);
+        if (e != cudaSuccess) return cuda_status(e);
     }
-    ctx->stream = (cudaStream_t)stream;
+    ctx->stream = ns;
     return IA_OK;
 }
 

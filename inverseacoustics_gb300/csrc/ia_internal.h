@@ -12,6 +12,7 @@ struct ia_context {
     size_t ws_bytes;
     long long launches;    // kernels launched through this context
     int sm_count;
+    int capturing;         // between ia_capture_begin and ia_capture_end
 };
 
 struct ia_mesh {
