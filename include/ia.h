@@ -163,6 +163,16 @@ long long ia_launch_count(const ia_context *ctx);
  * IA_ERR_CAPTURE).  The graph holds pointers into the context's workspace:
  * keep the context alive and do not run larger calls on it before the last
  * replay. */
+/* Autotuner.  GEMM-type kernels come in several tile shapes; the first call
+ * of each (kernel, shape, transposition, batch) outside stream capture times
+ * every shape on scratch outputs and keeps the fastest in a process-wide
+ * table.  All shapes sum in the same order, so results do not depend on the
+ * choice.  Environment: IA_TUNE=0 disables tuning (first shape everywhere);
+ * IA_TUNE_FILE=<path> loads choices from, and appends new ones to, a text
+ * file.  ia_tune_reset forgets the table and re-reads the environment. */
+int ia_tune_table_size(void);
+void ia_tune_reset(void);
+
 typedef struct ia_graph ia_graph;
 int ia_capture_begin(ia_context *ctx);
 int ia_capture_end(ia_context *ctx, ia_graph **graph);

@@ -67,6 +67,8 @@ _SIGS = {
     "ia_set_stream": (_I, [_P, _P]),
     "ia_synchronize": (_I, [_P]),
     "ia_launch_count": (C.c_longlong, [_P]),
+    "ia_tune_table_size": (_I, []),
+    "ia_tune_reset": (None, []),
     "ia_capture_begin": (_I, [_P]),
     "ia_capture_end": (_I, [_P, _PP]),
     "ia_graph_launch": (_I, [_P]),

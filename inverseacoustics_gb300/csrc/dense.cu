@@ -8,14 +8,18 @@
 // grid.x = batch).
 #include "ia_common.cuh"
 #include "ia_internal.h"
+#include "tune.h"
 
 namespace ia {
 
 // --------------------------------------------------------------------------
-// GEMM: C = alpha op(A) op(B) + beta C, 64x64 tiles, 256 threads, each thread
-// a 4x4 block of outputs strided by 16 so shared-memory reads are conflict free.
+// GEMM: C = alpha op(A) op(B) + beta C.  A BM x BN tile per CTA of 256
+// threads, each thread a TM x TN block of outputs strided by BM/TM rows and
+// BN/TN columns so shared-memory reads are conflict free; K in steps of 8.
+// Every variant sums k in the same order (0..K-1, one thread per output), so
+// the autotuner's choice of tile does not change results.
 // --------------------------------------------------------------------------
-constexpr int GB_M = 64, GB_N = 64, GB_K = 8;
+constexpr int GB_K = 8;
 
 template <class T>
 __device__ __forceinline__ T ld_op(const T *P, int ld, int r, int c, int R, int Cc, int op)
@@ -28,66 +32,66 @@ __device__ __forceinline__ T ld_op(const T *P, int ld, int r, int c, int R, int 
     return v;
 }
 
-template <class T>
+template <class T, int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int N, int K, T alpha,
                                                    const T *__restrict__ A, int lda, long long sA,
                                                    const T *__restrict__ B, int ldb, long long sB, T beta,
                                                    T *__restrict__ C, int ldc, long long sC)
 {
-    __shared__ T As[GB_K][GB_M];
-    __shared__ T Bs[GB_K][GB_N];
+    constexpr int NTX = BN / TN, NTY = BM / TM;
+    static_assert(NTX * NTY == 256, "256 threads per tile");
+    __shared__ T As[GB_K][BM];
+    __shared__ T Bs[GB_K][BN];
     const int f = blockIdx.z;
     A += f * sA;
     B += f * sB;
     C += f * sC;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-    T acc[4][4];
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    T acc[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = ctraits<T>::make(0, 0);
+        for (int j = 0; j < TN; ++j) acc[i][j] = ctraits<T>::make(0, 0);
 
     for (int k0 = 0; k0 < K; k0 += GB_K) {
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            int e = threadIdx.x + t * 256;
+        for (int e = threadIdx.x; e < GB_K * BM; e += 256) {
             int r, kk;
-            if (opa == OP_N) { r = e % GB_M; kk = e / GB_M; }
+            if (opa == OP_N) { r = e % BM; kk = e / BM; }
             else { kk = e % GB_K; r = e / GB_K; }
             As[kk][r] = ld_op(A, lda, m0 + r, k0 + kk, M, K, opa);
         }
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            int e = threadIdx.x + t * 256;
+        for (int e = threadIdx.x; e < GB_K * BN; e += 256) {
             int kk, c;
             if (opb == OP_N) { kk = e % GB_K; c = e / GB_K; }
-            else { c = e % GB_N; kk = e / GB_N; }
+            else { c = e % BN; kk = e / BN; }
             Bs[kk][c] = ld_op(B, ldb, k0 + kk, n0 + c, K, N, opb);
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < GB_K; ++kk) {
-            T a[4], b[4];
+            T a[TM], b[TN];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + NTY * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + NTX * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) zfma(acc[i][j], a[i], b[j]);
+                for (int j = 0; j < TN; ++j) zfma(acc[i][j], a[i], b[j]);
         }
         __syncthreads();
     }
     const bool beta0 = (beta.x == 0 && beta.y == 0);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        int r = m0 + ty + 16 * i;
+    for (int i = 0; i < TM; ++i) {
+        int r = m0 + ty + NTY * i;
         if (r >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int c = n0 + tx + 16 * j;
+        for (int j = 0; j < TN; ++j) {
+            int c = n0 + tx + NTX * j;
             if (c >= N) continue;
             T v = zmul(alpha, acc[i][j]);
             T *p = C + r + (size_t)c * ldc;
@@ -97,15 +101,53 @@ __global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int 
     }
 }
 
+template <class T, int BM, int BN, int TM, int TN>
+static int gemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda,
+                       long long sA, const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch)
+{
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+    gemm_kernel<T, BM, BN, TM, TN>
+        <<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+// tile variants: 64x64 (4x4 per thread), 32x32 (2x2), 128x64 (8x4)
+constexpr int GEMM_VARIANTS = 3;
+
 template <class T>
 int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda, long long sA,
                  const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch)
 {
     if (M <= 0 || N <= 0 || batch <= 0) return IA_OK;
-    dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch);
-    gemm_kernel<T><<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
+    auto launch = [&](int v, T *Cout) -> int {
+        switch (v) {
+        case 1: return gemm_launch<T, 32, 32, 2, 2>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cout,
+                                                    ldc, sC, batch);
+        case 2: return gemm_launch<T, 128, 64, 8, 4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta,
+                                                     Cout, ldc, sC, batch);
+        default: return gemm_launch<T, 64, 64, 4, 4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta,
+                                                     Cout, ldc, sC, batch);
+        }
+    };
+    TuneKey key{};
+    key.kernel = sizeof(T) == sizeof(double2) ? TK_GEMM_Z : TK_GEMM_C;
+    key.v[0] = opa;
+    key.v[1] = opb;
+    key.v[2] = M;
+    key.v[3] = N;
+    key.v[4] = K;
+    key.v[5] = batch;
+    const size_t cbytes = sizeof(T) * ((size_t)(batch - 1) * sC + (size_t)ldc * (N - 1) + M);
+    TuneScratch scratch{ctx};
+    const int v = tune_select(ctx, key, GEMM_VARIANTS, [&](int vv) -> int {
+        if (!scratch.p) {
+            int st = scratch.init(C, cbytes);
+            if (st) return st;
+        }
+        return launch(vv, (T *)scratch.p);
+    });
+    return launch(v, C);
 }
 
 // --------------------------------------------------------------------------

@@ -8,15 +8,17 @@
 // Products use the error-free transformation p + e = x_hi y_hi (fmaf), plus
 // the cross terms x_hi y_lo + x_lo y_hi; sums use TwoSum on the high word with
 // the low word accumulated and renormalised after each K tile (Dekker 1971;
-// Hida, Li, Bailey 2001).  Tiles: 64 x 64 outputs, K tile 8, 256 threads with
-// a 4 x 4 block each, operands split to (hi, lo) on the way into shared memory.
+// Hida, Li, Bailey 2001).  Tiles of 64 x 64, 32 x 32 or 64 x 32 outputs (the
+// autotuner picks per shape; all sum k in the same order), K tile 8, 256
+// threads, operands split to (hi, lo) on the way into shared memory.
 // op(A), op(B) in {N, C} (C = conjugate transpose).
 #include "ia_common.cuh"
 #include "ia_internal.h"
+#include "tune.h"
 
 namespace ia {
 
-constexpr int DF_M = 64, DF_N = 64, DF_K = 8;
+constexpr int DF_K = 8;
 
 struct df2 {   // complex double-float accumulator
     float rh, rl, ih, il;
@@ -51,31 +53,33 @@ __device__ __forceinline__ void df_norm(float &ah, float &al)
     ah = s;
 }
 
+template <int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, int N, int K, double alpha,
                                                      const double2 *__restrict__ A, int lda, long long sA,
                                                      const double2 *__restrict__ B, int ldb, long long sB,
                                                      double beta, double2 *__restrict__ C, int ldc, long long sC)
 {
-    __shared__ float4 As[DF_K][DF_M];
-    __shared__ float4 Bs[DF_K][DF_N];
+    constexpr int NTX = BN / TN, NTY = BM / TM;
+    static_assert(NTX * NTY == 256, "256 threads per tile");
+    __shared__ float4 As[DF_K][BM];
+    __shared__ float4 Bs[DF_K][BN];
     const int f = blockIdx.z;
     A += f * sA;
     B += f * sB;
     C += f * sC;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int m0 = blockIdx.y * DF_M, n0 = blockIdx.x * DF_N;
-    df2 acc[4][4];
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    df2 acc[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = df2{0.f, 0.f, 0.f, 0.f};
+        for (int j = 0; j < TN; ++j) acc[i][j] = df2{0.f, 0.f, 0.f, 0.f};
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k0 = 0; k0 < K; k0 += DF_K) {
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            int e = threadIdx.x + t * 256;
+        for (int e = threadIdx.x; e < DF_K * BM; e += 256) {
             int r, kk;
-            if (opa == OP_N) { r = e % DF_M; kk = e / DF_M; }
+            if (opa == OP_N) { r = e % BM; kk = e / BM; }
             else { kk = e % DF_K; r = e / DF_K; }
             int gr = m0 + r, gk = k0 + kk;
             float4 v = z4;
@@ -84,11 +88,10 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
             As[kk][r] = v;
         }
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            int e = threadIdx.x + t * 256;
+        for (int e = threadIdx.x; e < DF_K * BN; e += 256) {
             int kk, c;
             if (opb == OP_N) { kk = e % DF_K; c = e / DF_K; }
-            else { c = e % DF_N; kk = e / DF_N; }
+            else { c = e % BN; kk = e / BN; }
             int gk = k0 + kk, gc = n0 + c;
             float4 v = z4;
             if (gk < K && gc < N)
@@ -98,15 +101,15 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < DF_K; ++kk) {
-            float4 a[4], b[4];
+            float4 a[TM], b[TN];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + NTY * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + NTX * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < TN; ++j) {
                     // a = (x: re_h, y: im_h, z: re_l, w: im_l)
                     df2 &c = acc[i][j];
                     df_mac(c.rh, c.rl, a[i].x, a[i].z, b[j].x, b[j].z);
@@ -116,21 +119,21 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
                 }
         }
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < TM; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < TN; ++j) {
                 df_norm(acc[i][j].rh, acc[i][j].rl);
                 df_norm(acc[i][j].ih, acc[i][j].il);
             }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        int r = m0 + ty + 16 * i;
+    for (int i = 0; i < TM; ++i) {
+        int r = m0 + ty + NTY * i;
         if (r >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int c = n0 + tx + 16 * j;
+        for (int j = 0; j < TN; ++j) {
+            int c = n0 + tx + NTX * j;
             if (c >= N) continue;
             double2 v = make_double2(alpha * ((double)acc[i][j].rh + (double)acc[i][j].rl),
                                      alpha * ((double)acc[i][j].ih + (double)acc[i][j].il));
@@ -145,16 +148,53 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
     }
 }
 
+template <int BM, int BN, int TM, int TN>
+static int dfgemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A,
+                         int lda, long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C,
+                         int ldc, long long sC, int batch)
+{
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+    dfgemm_kernel<BM, BN, TM, TN>
+        <<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+// tile variants: 64x64 (4x4 per thread), 32x32 (2x2), 64x32 (4x2)
 int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
                    long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
                    long long sC, int batch)
 {
     if (M <= 0 || N <= 0 || batch <= 0) return IA_OK;
     if ((opa != OP_N && opa != OP_C) || (opb != OP_N && opb != OP_C)) return IA_ERR_ARG;
-    dim3 grid((N + DF_N - 1) / DF_N, (M + DF_M - 1) / DF_M, batch);
-    dfgemm_kernel<<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
+    auto launch = [&](int v, double2 *Cout) -> int {
+        switch (v) {
+        case 1: return dfgemm_launch<32, 32, 2, 2>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cout,
+                                                   ldc, sC, batch);
+        case 2: return dfgemm_launch<64, 32, 4, 2>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cout,
+                                                   ldc, sC, batch);
+        default: return dfgemm_launch<64, 64, 4, 4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta,
+                                                    Cout, ldc, sC, batch);
+        }
+    };
+    TuneKey key{};
+    key.kernel = TK_DFGEMM;
+    key.v[0] = opa;
+    key.v[1] = opb;
+    key.v[2] = M;
+    key.v[3] = N;
+    key.v[4] = K;
+    key.v[5] = batch;
+    const size_t cbytes = sizeof(double2) * ((size_t)(batch - 1) * sC + (size_t)ldc * (N - 1) + M);
+    TuneScratch scratch{ctx};
+    const int v = tune_select(ctx, key, 3, [&](int vv) -> int {
+        if (!scratch.p) {
+            int st = scratch.init(C, cbytes);
+            if (st) return st;
+        }
+        return launch(vv, (double2 *)scratch.p);
+    });
+    return launch(v, C);
 }
 
 }  // namespace ia

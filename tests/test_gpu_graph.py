@@ -35,7 +35,7 @@ def test_graph_replay_matches_direct_calls(cuda, precision):
         out = api.ibem_solve_outputs(mesh, M, K, P)
         n0 = ctx.launches()
         graph = ctx.capture(lambda: api.ibem_solve_batch(ctx, mesh, M, K, P, cfg, out=out))
-        assert ctx.launches() - n0 == graph.kernel_count() > 50
+        assert ctx.launches() - n0 == graph.kernel_count() > 20
         graph.launch()
         stream.synchronize()
         for a, b in zip(out, ref1):

@@ -1,0 +1,60 @@
+"""GPU suite: the kernel-variant autotuner.  Tuned and untuned runs of the
+mixed IBEM pipeline must agree bit for bit (variants differ only in the
+thread mapping), the table must fill, and a tuning file must round-trip."""
+import os
+
+import numpy as np
+import pytest
+
+from inverseacoustics_gb300 import geometry as g
+
+pytestmark = pytest.mark.gpu
+
+
+def T(a, dev):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), device=dev)
+
+
+def test_tuned_equals_untuned(cuda, ctx, tmp_path, monkeypatch):
+    from inverseacoustics_gb300 import _lib, api
+    import torch
+    L = _lib.lib()
+    nodes, elems = g.icosphere(2, 0.1)
+    rng = np.random.default_rng(31)
+    mics = g.hemisphere_array(rng, 50, 0.3)
+    ks = 2 * np.pi * np.linspace(200, 1500, 6) / 343.0
+    p = np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0), 30.0)[None, :] for k in ks])
+    mesh = api.Mesh(ctx, nodes, elems)
+    args = (T(mics, cuda), T(ks, cuda), T(p, cuda))
+    cfg = api.default_config(precision=1)
+    tune_file = tmp_path / "tune.txt"
+    monkeypatch.setenv("IA_TUNE", "1")
+    monkeypatch.setenv("IA_TUNE_FILE", str(tune_file))
+    L.ia_tune_reset()
+    tuned = api.ibem_solve_batch(ctx, mesh, *args, cfg)
+    torch.cuda.synchronize()
+    n = L.ia_tune_table_size()
+    assert n > 5
+    lines = tune_file.read_text().split("\n")
+    assert len([x for x in lines if x.strip()]) == n
+    monkeypatch.setenv("IA_TUNE", "0")
+    monkeypatch.delenv("IA_TUNE_FILE")
+    L.ia_tune_reset()
+    plain = api.ibem_solve_batch(ctx, mesh, *args, cfg)
+    torch.cuda.synchronize()
+    assert L.ia_tune_table_size() == 0
+    for a, b in zip(tuned, plain):
+        assert torch.equal(a, b)
+    # the file restores the table without timing anything
+    monkeypatch.setenv("IA_TUNE_FILE", str(tune_file))
+    L.ia_tune_reset()
+    again = api.ibem_solve_batch(ctx, mesh, *args, cfg)
+    torch.cuda.synchronize()
+    assert L.ia_tune_table_size() == n
+    for a, b in zip(tuned, again):
+        assert torch.equal(a, b)
+    monkeypatch.delenv("IA_TUNE_FILE")
+    monkeypatch.setenv("IA_TUNE", "1")
+    L.ia_tune_reset()
+    mesh.close()
