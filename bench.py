@@ -151,6 +151,101 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _bench_radiation(ctx, dev, stream, flush, reps=2):
+    """The baffled-plate workload (1280 elements, 256 frequencies 20-2000 Hz,
+    192 microphones): sinc resistance R, 32 leading radiation modes, ESM
+    velocity reconstruction by TSVD (k = 36), sound power of the
+    reconstruction.  Mixed path timed, FP64 path timed once for comparison."""
+    import numpy as np
+    import torch
+
+    from inverseacoustics_gb300 import api
+    from inverseacoustics_gb300 import geometry as g
+    w = g.radiation_plate(n_freq=256)
+    x, area, mics = w.arrays["centres"], w.params["area"], w.arrays["mics"]
+    F, n, nm = len(w.k), x.shape[1], 32
+    rng = np.random.default_rng(3)
+    vel = w.params["vel"]
+    p = np.stack([g.add_noise(rng, g.rayleigh_pressure(mics, x, area, k, vel[f]), 30.0)[None, :]
+                  for f, k in enumerate(w.k)])
+    xd, md, kd, pd = (torch.as_tensor(np.ascontiguousarray(a), device=dev) for a in (x, mics, w.k, p))
+    R = api.sinc_resistance_batch(ctx, xd, kd, area)
+    cfgs = {prec: (api.default_config(precision=prec), api.default_config(method=1, tsvd_k=36, precision=prec))
+            for prec in (0, 1)}
+    outs = {}
+
+    def stage_times(prec, r):
+        cm, cs = cfgs[prec]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        flush.zero_()
+        ev[0].record(stream)
+        api.sinc_resistance_batch(ctx, xd, kd, area, out=R)
+        ev[1].record(stream)
+        lam, modes, info = api.radiation_modes_batch(ctx, R, nm, cm)
+        ev[2].record(stream)
+        q, _, _, info2 = api.esm_solve_batch(ctx, md, xd, kd, pd, cs)
+        ev[3].record(stream)
+        W = api.sound_power_batch(ctx, R, q)
+        ev[4].record(stream)
+        ev[4].synchronize()
+        outs[prec] = (lam, modes, q, W, info, info2)
+        return [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+
+    stage_times(1, 0)
+    mixed = [stage_times(1, r) for r in range(reps)]
+    fp64 = stage_times(0, 0)
+    mixed = [sum(t[i] for t in mixed) / reps for i in range(4)]
+    lam1, _, q1, W1, i1, j1 = outs[1]
+    lam0, _, q0, W0, i0, j0 = outs[0]
+    err_lam = float(((lam1 - lam0).abs().amax(1) / lam0[:, 0]).max())
+    err_q = float(((q1 - q0).abs().pow(2).sum((1, 2)).sqrt() / q0.abs().pow(2).sum((1, 2)).sqrt()).max())
+    err_w = float(((W1 - W0).abs() / W0.abs()).max())
+    tot, tot64 = sum(mixed), sum(fp64)
+    return {"workload": f"sinc_plate_{n}el_192mic_F{F}", "frequencies": F, "modes": nm,
+            "value": F / (tot / 1000.0), "unit": "freq/s (R + modes + TSVD + power)",
+            "fp64_value": F / (tot64 / 1000.0), "mixed_speedup": tot64 / tot,
+            "stages_ms": dict(zip(["sinc_R", "modes", "esm_tsvd", "sound_power"], mixed)),
+            "fp64_stages_ms": dict(zip(["sinc_R", "modes", "esm_tsvd", "sound_power"], fp64)),
+            "accuracy": {"modes_lambda_vs_fp64_rel_lambda1": err_lam, "tsvd_x_vs_fp64": err_q,
+                         "sound_power_vs_fp64": err_w},
+            "info_clean": int(i1.abs().sum() + j1.abs().sum() + i0.abs().sum() + j0.abs().sum()) == 0}
+
+
+def _bench_design(ctx, dev, stream, flush, reps=3):
+    """Differentiable ESM array design (128 microphones, 642 sources, 128
+    frequencies 200-4000 Hz, 16 source fields): one forward + hand-written
+    adjoint step."""
+    import math
+
+    import numpy as np
+    import torch
+
+    from inverseacoustics_gb300 import api
+    from inverseacoustics_gb300 import geometry as g
+    w = g.esm_design(n_freq=128)
+    mics, surf, q = w.arrays["mics"], w.arrays["surface"], w.params["q"]
+    rng = np.random.default_rng(41)
+    F, R = len(w.k), q.shape[2]
+    noise = 10 ** (-30 / 20) * g.complex_normal(rng, (F, R, mics.shape[1])) * 0.05
+    ll = np.full(F, math.log(0.05))
+    args = [torch.as_tensor(np.ascontiguousarray(a), device=dev) for a in
+            (mics, surf, np.array([w.params["retreat"]]), w.k, ll, np.transpose(q, (0, 2, 1)), noise)]
+    api.esm_design_batch(ctx, *args)
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        err, gm, gd, gl, info = api.esm_design_batch(ctx, *args)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = sum(times) / reps
+    return {"workload": f"esm_design_128mic_642src_F{F}_R{R}", "ms_per_step": ms,
+            "value": F * R / (ms / 1000.0), "unit": "reconstructions/s with gradients (forward + adjoint)",
+            "steps_per_s": 1000.0 / ms, "info_clean": int(info.abs().sum()) == 0}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -165,7 +260,8 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     w, p_np = _workload()
     nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)                 # a created stream: capturable
+    torch.cuda.set_stream(stream)
     ctx = api.Context(local, stream)
     mesh = api.Mesh(ctx, nodes, elems)
     mics_d = torch.as_tensor(mics, device=dev)
@@ -176,9 +272,6 @@ def run_ours(args):
     cfg = api.default_config(precision=1)          # the mixed path: the headline
     m, l = nodes.shape[1], mics.shape[1]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
-
-    def step(c=cfg):
-        return api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, c)
 
     def barrier():
         if world > 1:
@@ -194,60 +287,68 @@ def run_ours(args):
             return float(t.item())
         return v
 
-    def timed_steps(c, steps):
-        """W warm-up steps, then `steps` steps each bracketed by CUDA events on
-        the launching stream, L2 flushed between them."""
+    def make_graph(c):
+        """W warm-up calls (they also tune the GEMM tiles and size the
+        workspace), then the whole 64-frequency solve captured as one graph."""
+        out = api.ibem_solve_outputs(mesh, mics_d, k_d, p_d)
         for _ in range(max(args.warmup, 3)):
-            out = step(c)
+            api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, c, out=out)
         torch.cuda.synchronize()
         assert int(out[3].abs().sum()) == 0, f"solver info flags {out[3].tolist()}"
+        graph = ctx.capture(lambda: api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, c, out=out))
+        graph.launch()
+        torch.cuda.synchronize()
+        return graph, out
+
+    def timed(run, steps, pre=None, post=None):
+        """`steps` steps each bracketed by CUDA events on the launching
+        stream, L2 flushed (256 MB write) before each."""
         times = []
-        l0 = ctx.launches()
         barrier()
         for _ in range(steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            out = step(c)
+            if pre:
+                pre()
+            run()
+            if post:
+                post()
             e1.record(stream)
             times.append((e0, e1))
         barrier()
-        total = max_over_ranks(sum(a.elapsed_time(b) for a, b in times))
-        return total, ctx.launches() - l0, out
+        return max_over_ranks(sum(a.elapsed_time(b) for a, b in times))
 
     # ---- FP64 path (the comparison point of the mixed path)
-    fp64_ms, _, out64 = timed_steps(cfg64, max(1, min(args.steps, 3)))
-    fp64_value = world * N_FREQ * max(1, min(args.steps, 3)) / (fp64_ms / 1000.0)
-    # ---- mixed path, device-resident
+    steps64 = max(1, min(args.steps, 3))
+    g64, out64 = make_graph(cfg64)
+    fp64_ms = timed(g64.launch, steps64)
+    fp64_value = world * N_FREQ * steps64 / (fp64_ms / 1000.0)
+    x64, lam64 = out64[0].clone(), out64[1].clone()
+    g64.close()
+    # ---- mixed path, device-resident, graph replay
+    graph, out = make_graph(cfg)
     with ClockSampler(local) as clk:
-        total_ms, launches, out = timed_steps(cfg, args.steps)
+        total_ms = timed(graph.launch, args.steps)
+    launches = graph.kernel_count() * args.steps
     x, lam, s, info = out
     value = world * N_FREQ * args.steps / (total_ms / 1000.0)
-    x64, lam64 = out64[0], out64[1]
     err_x = float(((x - x64).abs().pow(2).sum(dim=(1, 2)).sqrt() / x64.abs().pow(2).sum(dim=(1, 2)).sqrt()).max())
     err_lam = float(((lam - lam64).abs() / lam64.abs()).max())
+    # the same solve by direct calls (no graph), for the launch-overhead comparison
+    direct_ms = timed(lambda: api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, cfg, out=out), max(1, args.steps // 2))
+    direct_value = world * N_FREQ * max(1, args.steps // 2) / (direct_ms / 1000.0)
 
-    # ---- end to end through the public API, host buffers
+    # ---- end to end through the public API, host buffers: pinned H2D of the
+    # pressures, graph replay, D2H of x and lambda
     x_h = torch.empty((N_FREQ, 1, m), dtype=torch.complex128).pin_memory()
     lam_h = torch.empty((N_FREQ, 1), dtype=torch.float64).pin_memory()
-    e2e_times = []
-    barrier()
-    for _ in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        p_d.copy_(p_h, non_blocking=True)
-        x, lam, s, info = step()
-        x_h.copy_(x, non_blocking=True)
-        lam_h.copy_(lam, non_blocking=True)
-        e1.record(stream)
-        e2e_times.append((e0, e1))
-    barrier()
-    e2e_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in e2e_times))
+    e2e_ms = timed(graph.launch, args.steps, pre=lambda: p_d.copy_(p_h, non_blocking=True),
+                   post=lambda: (x_h.copy_(out[0], non_blocking=True), lam_h.copy_(out[1], non_blocking=True)))
     e2e_value = world * N_FREQ * args.steps / (e2e_ms / 1000.0)
 
     # ---- per-stage timing (same stream, CUDA events) for the roofline
-    def timed(fn, reps=3):
+    def stage(fn, reps=3):
         fn()
         torch.cuda.synchronize()
         acc = 0.0
@@ -261,12 +362,13 @@ def run_ours(args):
             acc += a.elapsed_time(b)
         return acc / reps
 
-    t_asm = timed(lambda: api.ibem_assemble_batch(ctx, mesh, mics_d, k_d, cfg))
-    t_transfer = timed(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg))
+    t_asm = stage(lambda: api.ibem_assemble_batch(ctx, mesh, mics_d, k_d, cfg))
+    t_transfer = stage(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg))
     H, _ = api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg)
-    t_solve = timed(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg))
-    t_transfer64 = timed(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg64), reps=1)
-    t_solve64 = timed(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg64), reps=1)
+    t_solve = stage(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg))
+    t_transfer64 = stage(lambda: api.ibem_transfer_batch(ctx, mesh, mics_d, k_d, cfg64), reps=1)
+    t_solve64 = stage(lambda: api.solve_batch(ctx, H, l, m, p_d, cfg64), reps=1)
+    del H
     hbm_peak, bf16_peak, peak_kind = _peaks()
     # assembly: algorithmic bytes = rows written, (m + l) rows x m columns x (A, B) x 16 B per frequency
     asm_bytes = N_FREQ * (m + l) * m * 2 * 16
@@ -298,6 +400,13 @@ def run_ours(args):
                 "compute": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
                             "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
                             "peak_dgemm_measured": fp64_tflops_dgemm}}
+    other = {}
+    if world == 1:
+        for name, fn in (("radiation_modes", _bench_radiation), ("esm_design_adjoint", _bench_design)):
+            try:
+                other[name] = fn(ctx, dev, stream, flush)
+            except Exception as e:  # a side workload must not hide the headline line
+                other[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -316,9 +425,11 @@ def run_ours(args):
                 "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies_per_gpu": N_FREQ,
                            "nodes": m, "triangles": int(elems.shape[1]), "mics": l,
                            "rules": "7-point Radon regular, 4x4 Duffy singular", "parallelism": f"freq-shard x{world}",
-                           "l2": "flushed between timed steps (256 MB write)"},
-                "fp64_path": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms / max(1, min(args.steps, 3)),
+                           "l2": "flushed between timed steps (256 MB write)",
+                           "launch": "one CUDA graph replay per step (graph of the whole batched solve)"},
+                "fp64_path": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms / steps64,
                               "mixed_speedup": value / fp64_value},
+                "direct_calls": {"value": direct_value, "unit": UNIT, "note": "same solve without the graph"},
                 "accuracy": {"max_rel_err_x_vs_fp64": err_x, "max_rel_err_lambda_vs_fp64": err_lam,
                              "bound": 1e-6, "note": "FP64 path parity-tested against the oracle at 1e-10"},
                 "stages_ms": {"assembly": t_asm, "transfer_incl_assembly": t_transfer, "svd_gcv_tikhonov": t_solve,
@@ -326,7 +437,7 @@ def run_ours(args):
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(p_np.nbytes),
                         "d2h_bytes_per_step": int(x_h.numel() * 16 + lam_h.numel() * 8)},
-                "gpu_launches": int(launches)}
+                "gpu_launches": int(launches), "other_workloads": other}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -430,13 +430,13 @@ def hels_solve_batch(ctx, pts, n_sh, k, p, cfg=None):
     return x, lam, s, info
 
 
-def sinc_resistance_batch(ctx, x, k, area, cfg=None):
+def sinc_resistance_batch(ctx, x, k, area, cfg=None, out=None):
     """R (F, n, n) float64: omega^2 rho A^2/(4 pi c) sinc(k r_ij) for radiators
     at x (3 x n SoA, device) and wavenumbers k (F, device).  Symmetric, so the
     row-major tensor equals the column-major matrix."""
     import torch
     n, F = x.shape[-1], k.numel()
-    R = torch.empty((F, n, n), dtype=torch.float64, device=k.device)
+    R = out if out is not None else torch.empty((F, n, n), dtype=torch.float64, device=k.device)
     check(_lib.lib().ia_sinc_resistance_batch(ctx.handle, n, _dptr(x, torch.float64), F, _dptr(k, torch.float64),
                                               float(area), C.byref(cfg) if cfg is not None else None, _dptr(R)),
           "ia_sinc_resistance_batch")

@@ -12,11 +12,13 @@
 //   x = Q [U_R z; 0]             small GEMM, then the reflectors
 // Neither U_H nor V_H is formed.
 //
-// Mixed path (wide_solve_mixed_batched): the same QR / Jacobi / GCV chain in
-// FP32 (sigma, beta and lambda carried to FP64), V_H = Q [U_R; 0] formed in
-// FP32, then x is recovered in FP64 by preconditioned iterative refinement of
-// the Tikhonov normal equations (H^H H + lambda^2 I) x = H^H b: residuals with
-// the FP64 operator, corrections through V_H diag(1/(s^2+lambda^2)) V_H^H.
+// Mixed path (wide_solve_mixed_batched): QR of H^H and one-sided Jacobi on R
+// in FP32 give X ~ U_H (eigenvectors of E = H H^H) to ~1e-5; E is formed in
+// FP64; Ogita-Aishima refinement steps (X^H E X in FP64, X^H X and the update
+// in double-float) bring separated eigenpairs to FP64 accuracy; a two-sided
+// FP64 Jacobi on S = X^H E X separates the near-equal pairs those steps leave
+// coupled; then s = sqrt(eig E), beta = U^H b, GCV in FP64, and
+// x = H^H U diag(phi / s) beta against the FP64 operator.
 //
 // Both replace the reference's csvd + gcvG + tikhonovG / tsvd chain
 // (CUDA/tsvd.cuh:10-172, MATLAB/regtools) for the batched path.
@@ -361,6 +363,135 @@ __global__ void __launch_bounds__(OA_THREADS) oa_update_kernel(int N, const doub
     }
 }
 
+// Two-sided FP64 Jacobi on the projected matrix S = X^H E X (N x N Hermitian,
+// nearly diagonal after the refinement steps), one CTA per frequency, S in
+// global memory, the rotations applied to the columns of X as well.  Only
+// pairs coupled above the rounding level of S (|S_ij| > 4 sqrt(N) eps
+// max|S_ii|) rotate, so the cost follows the clustered pairs the first-order
+// refinement cannot separate (near-degenerate eigenvalues of symmetric
+// geometries).  Round-robin ordering: in a round the pairs are disjoint, their
+// rotations are computed from the current S, then applied to all pair columns,
+// then to all pair rows (left and right rotations commute).  The rotation
+//   G = [[c, s e], [-s conj(e), c]],  e = S_ij/|S_ij|,  t = tan(theta) from
+//   zeta = (S_jj - S_ii) / (2 |S_ij|)   (Rutishauser's stable form)
+// zeroes S_ij; S <- G^H S G on the pair, X <- X G.  LAM <- diag(S).
+constexpr int HJ_THREADS = 512;
+
+__device__ __forceinline__ void hj_pair(int N2, int round, int k, int &i, int &j)
+{
+    if (k == 0) {
+        i = round;
+        j = N2 - 1;
+    } else {
+        i = (round + k) % (N2 - 1);
+        j = (round - k + N2 - 1) % (N2 - 1);
+    }
+    if (i > j) { int t = i; i = j; j = t; }
+}
+
+__global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 *S, double2 *X, double *LAM,
+                                                                  int max_sweeps, int *info)
+{
+    extern __shared__ __align__(16) double hj_sm[];
+    const int N2 = N + (N & 1), P = N2 / 2;
+    double *cs = hj_sm;                                   // P
+    double2 *se = reinterpret_cast<double2 *>(hj_sm + P + (P & 1));   // P, 16-byte aligned
+    int *pi = reinterpret_cast<int *>(se + P);            // P
+    int *pj = pi + P;                                     // P
+    __shared__ double red[HJ_THREADS / 32];
+    __shared__ int s_rot;
+    const int f = blockIdx.x;
+    S += (size_t)f * N * N;
+    X += (size_t)f * N * N;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    double lm = 0.0;
+    for (int i = tid; i < N; i += blockDim.x) lm = fmax(lm, fabs(S[i + (size_t)i * N].x));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    if (lane == 0) red[wid] = lm;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t = fmax(t, red[w]);
+        red[0] = t;
+    }
+    __syncthreads();
+    const double tol = 4.0 * sqrt((double)N) * 2.220446049250313e-16 * red[0];
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        if (tid == 0) s_rot = 0;
+        __syncthreads();
+        for (int round = 0; round < N2 - 1; ++round) {
+            int mine = 0;
+            for (int k = tid; k < P; k += blockDim.x) {
+                int i, j;
+                hj_pair(N2, round, k, i, j);
+                pi[k] = -1;
+                if (j >= N) continue;
+                const double2 s = S[i + (size_t)j * N];
+                const double g = sqrt(s.x * s.x + s.y * s.y);
+                if (!(g > tol)) continue;
+                const double a = S[i + (size_t)i * N].x, b = S[j + (size_t)j * N].x;
+                const double zeta = (b - a) / (2.0 * g);
+                const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t);
+                const double sn = t * c;
+                cs[k] = c;
+                se[k] = make_double2(sn * s.x / g, sn * s.y / g);   // s e
+                pi[k] = i;
+                pj[k] = j;
+                ++mine;
+            }
+            if (mine) atomicAdd(&s_rot, mine);
+            __syncthreads();
+            // columns of S and X: [u v] <- [u v] G
+            for (int k = wid; k < P; k += nw) {
+                const int i = pi[k];
+                if (i < 0) continue;
+                const int j = pj[k];
+                const double c = cs[k];
+                const double2 w = se[k];
+                for (int m = 0; m < 2; ++m) {
+                    double2 *M = m == 0 ? S : X;
+                    double2 *ci = M + (size_t)i * N, *cj = M + (size_t)j * N;
+                    for (int r = lane; r < N; r += 32) {
+                        const double2 u = ci[r], v = cj[r];
+                        double2 nu = zscale(u, c), nv = zscale(v, c);
+                        zfms(nu, zconj(w), v);                 // c u - conj(s e) v
+                        zfma(nv, w, u);                        // c v + s e u
+                        ci[r] = nu;
+                        cj[r] = nv;
+                    }
+                }
+            }
+            __syncthreads();
+            // rows of S: [u; v] <- G^H [u; v]
+            for (int k = wid; k < P; k += nw) {
+                const int i = pi[k];
+                if (i < 0) continue;
+                const int j = pj[k];
+                const double c = cs[k];
+                const double2 w = se[k];
+                for (int col = lane; col < N; col += 32) {
+                    double2 *a = S + i + (size_t)col * N, *b = S + j + (size_t)col * N;
+                    const double2 u = *a, v = *b;
+                    double2 nu = zscale(u, c), nv = zscale(v, c);
+                    zfms(nu, w, v);                            // c u - s e v
+                    zfma(nv, zconj(w), u);                     // c v + conj(s e) u
+                    *a = nu;
+                    *b = nv;
+                }
+            }
+            __syncthreads();
+        }
+        const int total = s_rot;
+        __syncthreads();
+        if (total == 0) break;
+    }
+    if (tid == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
+    for (int i = tid; i < N; i += blockDim.x) LAM[(size_t)f * N + i] = S[i + (size_t)i * N].x;
+}
+
 // s (sorted descending), beta = U^H b (sorted like s), rank of every column;
 // U = X, or conj(X) when conj_u.
 __global__ void eig_beta_kernel(int m, int N, const double *LAM, const double2 *X, int conj_u, int nrhs,
@@ -523,7 +654,28 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
         X = Xn;
         Xn = t;
     }
-    // 4. s, beta, GCV, back-projection
+    // 4. pairs of near-equal eigenvalues stay coupled through the first-order
+    // steps (the refinement treats them as a cluster): orthonormalise X
+    // (Newton-Schulz, X <- 1.5 X - 0.5 X X^H X), form S = X^H E X in FP64 and
+    // rotate the coupled pairs apart with two-sided Jacobi; lam_e <- diag(S)
+    if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
+    if ((st = zcopy2d_batched(ctx, N, N, X, N, sN, Xn, N, sN, false, batch))) return st;
+    if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, -0.5, X, N, sN, Rm, N, sN, 1.5, Xn, N, sN, batch))) return st;
+    {
+        double2 *t = X;
+        X = Xn;
+        Xn = t;
+    }
+    if ((st = zgemm_batched(ctx, OP_N, OP_N, N, N, N, one, E, N, sN, X, N, sN, zero, T1, N, sN, batch))) return st;
+    if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;
+    {
+        const int P = (N + (N & 1)) / 2;
+        const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P;
+        const int sweeps = cfg->svd_max_sweeps < 16 ? cfg->svd_max_sweeps : 16;
+        herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
+        IA_LAUNCH_CHECK(ctx);
+    }
+    // 5. s, beta, GCV, back-projection
     eig_beta_kernel<<<batch, 256, 0, ctx->stream>>>(m, N, lam_e, X, transposed ? 1 : 0, nrhs, b, s, beta, rank);
     IA_LAUNCH_CHECK(ctx);
     st = gcv_beta_batched(ctx, m, N, batch, s, nrhs, beta, nullptr, cfg, z, lam);

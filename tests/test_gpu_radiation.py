@@ -161,3 +161,24 @@ def test_plate_velocity_reconstruction(cuda, ctx, plate):
             assert relerr(q[f, 0], q_ref[f]) < tol
             wo = O.sound_power_R(O.sinc_resistance(x, k, C, RHO, area), q_ref[f])
             assert abs(W[f, 0] - wo) <= 10 * tol * abs(wo)
+
+
+def test_mixed_tsvd_symmetric_plate_all_bins(cuda, ctx, plate):
+    """The full 192-microphone grid is symmetric about the plate centre, so
+    G has near-equal singular pairs.  Mixed TSVD against the FP64 path at all
+    256 bins: the pairs the first-order eigen-refinement cannot separate are
+    rotated apart by the FP64 Jacobi on X^H E X."""
+    from inverseacoustics_gb300 import api
+    import torch
+    x, area, mics = plate.arrays["centres"], plate.params["area"], plate.arrays["mics"]
+    rng = np.random.default_rng(3)
+    vel = plate.params["vel"]
+    p = np.stack([g.add_noise(rng, g.rayleigh_pressure(mics, x, area, k, vel[f], C, RHO), 30.0)[None, :]
+                  for f, k in enumerate(plate.k)])
+    args = (T(mics, cuda), T(x, cuda), T(plate.k, cuda), T(p, cuda))
+    q0, _, _, i0 = api.esm_solve_batch(ctx, *args, api.default_config(method=1, tsvd_k=36))
+    q1, _, _, i1 = api.esm_solve_batch(ctx, *args, api.default_config(method=1, tsvd_k=36, precision=1))
+    torch.cuda.synchronize()
+    assert int(i0.abs().sum()) == 0 and int(i1.abs().sum()) == 0
+    err = ((q1 - q0).abs().pow(2).sum((1, 2)).sqrt() / q0.abs().pow(2).sum((1, 2)).sqrt()).cpu().numpy()
+    assert err.max() < 1e-9, (int(err.argmax()), float(err.max()))
