@@ -136,6 +136,43 @@ __global__ void build_raug_kernel(int N, int Mrows, int nrhs, const T *Y, const 
     }
 }
 
+// R^H (N x N) from the QR'd Y: R is the upper triangle of Y (all of Y when full)
+__global__ void build_rh_kernel(int N, int Mrows, const float2 *Y, int full, float2 *RH)
+{
+    const int f = blockIdx.y;
+    const long long total = (long long)N * N;
+    Y += (size_t)f * Mrows * N;
+    RH += (size_t)f * N * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % N), j = (int)(e / N);     // RH(i, j) = conj(R(j, i))
+        float2 v = make_float2(0.f, 0.f);
+        if (full || j <= i) {
+            const float2 r = Y[j + (size_t)i * Mrows];
+            v = make_float2(r.x, -r.y);
+        }
+        RH[e] = v;
+    }
+}
+
+// unit columns of Y (N x N per matrix); a zero column becomes e_j
+__global__ void normalize_cols_kernel(int N, const float2 *Y, float2 *X)
+{
+    const int f = blockIdx.x;
+    Y += (size_t)f * N * N;
+    X += (size_t)f * N * N;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = wid; j < N; j += nw) {
+        const float2 *y = Y + (size_t)j * N;
+        float a = 0.f;
+        for (int r = lane; r < N; r += 32) a += y[r].x * y[r].x + y[r].y * y[r].y;
+        a = warp_sum(a);
+        const float inv = a > 0.f ? rsqrtf(a) : 0.f;
+        for (int r = lane; r < N; r += 32)
+            X[r + (size_t)j * N] = a > 0.f ? make_float2(y[r].x * inv, y[r].y * inv) : make_float2(r == j ? 1.f : 0.f, 0.f);
+    }
+}
+
 // sigma (sorted, FP64 out), beta = conj(appended rows) (sorted, FP64 out),
 // U_R = R/sigma (sorted, element type T).
 template <class T>
@@ -625,11 +662,15 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
         long long total = (long long)N * N;
         int blocks = (int)((total + 255) / 256);
         if (blocks > 512) blocks = 512;
-        build_raug_kernel<float2><<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, 0, Y, b, qr ? 0 : 1, R32);
+        build_rh_kernel<<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, Y, qr ? 0 : 1, R32);
         IA_LAUNCH_CHECK(ctx);
     }
-    st = jacobi_rows_batched<float2>(ctx, N, N, N, R32, J32, batch, cfg->svd_max_sweeps, info);
+    // one-sided Jacobi on R^H: its columns end as U_E diag(sigma) with E = R^H R
+    // = H H^H, so no rotation accumulator is needed
+    st = jacobi_rows_batched<float2>(ctx, N, N, N, R32, nullptr, batch, cfg->svd_max_sweeps, info);
     if (st) return st;
+    normalize_cols_kernel<<<batch, 256, 0, ctx->stream>>>(N, R32, J32);
+    IA_LAUNCH_CHECK(ctx);
     // 2. E = H H^H (or its conjugate for H^T input).  E and S = X^H E X set
     // the accuracy of the eigenvectors as eps ||E|| / gap, so they are FP64
     // products; X^H X and X F only need double-float.
