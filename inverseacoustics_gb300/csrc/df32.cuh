@@ -4,12 +4,14 @@
 //
 // Building blocks are the error-free transformations: TwoSum (Knuth),
 // FastTwoSum (Dekker), TwoProd via fmaf; products and sums follow Dekker
-// (1971) and Hida, Li & Bailey (2001).  sin/cos: Cody-Waite reduction of an
-// FP64 argument by pi/2 (pi/2 held as two doubles), then the Taylor series of
-// sin and cos on [-pi/4, pi/4] evaluated by Horner in double-float; the
-// coefficients are (-1)^k / n! (exact rationals rounded to double, split).
+// (1971) and Hida, Li & Bailey (2001).  sin/cos: df_sincos_tab (below) for
+// double-float arguments, table plus short series, FP32 operations only; and
+// df_sincos for FP64 arguments, Cody-Waite reduction by pi/2 (pi/2 held as two
+// doubles) then the Taylor series on [-pi/4, pi/4] by Horner in double-float
+// with coefficients (-1)^k / n! (exact rationals rounded to double, split).
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 
 namespace ia {
 
@@ -125,6 +127,98 @@ __device__ __forceinline__ void df_sincos(double theta, const DfTrigCoef &C, dfl
     else if (q == 1) { s = pc; c = df_neg(ps); }
     else if (q == 2) { s = df_neg(ps); c = df_neg(pc); }
     else { s = df_neg(pc); c = ps; }
+}
+
+// ---- table-driven sin/cos of a double-float argument (no FP64 operations)
+//
+// theta = N pi/128 + u with N = rint(theta 128/pi) and |u| <= ~pi/256;
+// sin/cos(N pi/128) come from a 256-entry table (N mod 256) held in shared
+// memory as (sin hi, sin lo, cos hi, cos lo), filled by sincospi; sin u and
+// cos u by their Taylor series to u^7 and u^8 (terms below 1e-17 dropped);
+// then the angle-sum formulas.  pi/128 is carried as p0 + p1 + p2 + p3 with
+// p0..p2 of 12 significant bits, so N p_i is exact for |N| < 4096 and the
+// reduction is exact up to the last part (Cody & Waite 1980).  Larger
+// arguments take the FP64-reduced series above.
+struct DfTrigRed {
+    float p[4];            // pi/128 split
+    float s3h, s3l;        // -1/6
+    float c2h, c2l;        // 1/24
+};
+
+__host__ inline float df_round_bits(double x, int bits)
+{
+    if (x == 0.0) return 0.0f;
+    int e;
+    frexp(x, &e);                                   // x = m 2^e, 0.5 <= |m| < 1
+    const double scale = ldexp(1.0, bits - e);
+    return (float)(nearbyint(x * scale) / scale);
+}
+
+__host__ inline DfTrigRed df_trig_reduction_constants()
+{
+    // pi/2 as a double-double (hi exact to 53 bits, lo the next 53), / 64
+    const double hi = 1.5707963267948966 / 64.0, lo = 6.123233995736766e-17 / 64.0;
+    DfTrigRed r;
+    const float p0 = df_round_bits(hi, 12);
+    const double r1 = hi - (double)p0;
+    const float p1 = df_round_bits(r1, 12);
+    const double r2 = r1 - (double)p1;
+    const float p2 = df_round_bits(r2, 12);
+    const double r3 = (r2 - (double)p2) + lo;
+    r.p[0] = p0;
+    r.p[1] = p1;
+    r.p[2] = p2;
+    r.p[3] = (float)r3;
+    const double s3 = -1.0 / 6.0, c2 = 1.0 / 24.0;
+    r.s3h = (float)s3;
+    r.s3l = (float)(s3 - (double)r.s3h);
+    r.c2h = (float)c2;
+    r.c2l = (float)(c2 - (double)r.c2h);
+    return r;
+}
+
+// tab[j] = (sin, cos)(j pi / 128) as double-float pairs
+__device__ inline void df_trig_table_fill(float4 *tab, int tid, int nthreads)
+{
+    for (int j = tid; j < 256; j += nthreads) {
+        double s, c;
+        sincospi((double)j / 128.0, &s, &c);
+        const float sh = __double2float_rn(s), ch = __double2float_rn(c);
+        tab[j] = make_float4(sh, __double2float_rn(s - (double)sh), ch, __double2float_rn(c - (double)ch));
+    }
+}
+
+__device__ __forceinline__ dfl df_add_f(dfl a, float b)
+{
+    dfl s = two_sum(a.hi, b);
+    s.lo += a.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ void df_sincos_tab(dfl theta, const float4 *__restrict__ tab, const DfTrigRed &P,
+                                              const DfTrigCoef &C, dfl &s, dfl &c)
+{
+    const float N = rintf(theta.hi * 40.74366543152521f);     // 128 / pi
+    if (!(fabsf(N) < 4096.0f)) {                               // outside the exact reduction range
+        df_sincos(df_to_double(theta), C, s, c);
+        return;
+    }
+    // u = theta - N (p0 + p1 + p2 + p3); theta.hi - N p0 is exact
+    dfl u = two_sum(fmaf(-N, P.p[0], theta.hi), theta.lo);
+    u = df_add_f(u, -N * P.p[1]);
+    u = df_add_f(u, -N * P.p[2]);
+    u = df_add_f(u, -N * P.p[3]);
+    const dfl u2 = df_mul(u, u);
+    // sin u = u + u u2 (-1/6 + u2/120 - u2^2/5040)
+    const float ts = u2.hi * fmaf(u2.hi, -1.0f / 5040.0f, 1.0f / 120.0f);
+    const dfl su = df_add(u, df_mul(u, df_mul(u2, df_add_f(dfl{P.s3h, P.s3l}, ts))));
+    // cos u = 1 + u2 (-1/2 + u2 (1/24 - u2/720 + u2^2/40320))
+    const float tc = u2.hi * fmaf(u2.hi, 1.0f / 40320.0f, -1.0f / 720.0f);
+    const dfl cu = df_add_f(df_mul(u2, df_add_f(df_mul(u2, df_add_f(dfl{P.c2h, P.c2l}, tc)), -0.5f)), 1.0f);
+    const float4 t = tab[((int)N) & 255];
+    const dfl sj{t.x, t.y}, cj{t.z, t.w};
+    s = df_add(df_mul(sj, cu), df_mul(cj, su));
+    c = df_sub(df_mul(cj, cu), df_mul(sj, su));
 }
 
 }  // namespace ia

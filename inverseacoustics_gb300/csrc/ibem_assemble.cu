@@ -30,6 +30,7 @@
 // the FP64 path, double-float (dfl, df32.cuh) for the mixed path, which moves
 // the dominant work from GB300's FP64 pipe to its FP32 pipe at ~1e-14
 // relative accuracy.  The singular elements stay FP64 in both.
+#include <type_traits>
 #include "df32.cuh"
 #include "ia_common.cuh"
 #include "ia_internal.h"
@@ -50,7 +51,11 @@ __device__ __forceinline__ void r_mac(double &acc, double a, double b) { acc = f
 __device__ __forceinline__ double r_norm(double a) { return a; }
 __device__ __forceinline__ double r_rsqrt(double a) { return rsqrt(a); }
 __device__ __forceinline__ double r_zero(double) { return 0.0; }
-__device__ __forceinline__ void r_sincos(double theta, const DfTrigCoef &, double &s, double &c) { sincos(theta, &s, &c); }
+__device__ __forceinline__ void r_sincos(double theta, const float4 *, const DfTrigRed &, const DfTrigCoef &, double &s,
+                                         double &c)
+{
+    sincos(theta, &s, &c);
+}
 
 __device__ __forceinline__ dfl r_from(dfl x) { return x; }
 __device__ __forceinline__ double r_to_double(dfl x) { return df_to_double(x); }
@@ -61,7 +66,11 @@ __device__ __forceinline__ void r_mac(dfl &acc, dfl a, dfl b) { df_mac(acc, a, b
 __device__ __forceinline__ dfl r_norm(dfl a) { return df_norm(a); }
 __device__ __forceinline__ dfl r_rsqrt(dfl a) { return df_rsqrt(a); }
 __device__ __forceinline__ dfl r_zero(dfl) { return dfl{0.0f, 0.0f}; }
-__device__ __forceinline__ void r_sincos(double theta, const DfTrigCoef &C, dfl &s, dfl &c) { df_sincos(theta, C, s, c); }
+__device__ __forceinline__ void r_sincos(dfl theta, const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C, dfl &s,
+                                         dfl &c)
+{
+    df_sincos_tab(theta, tab, P, C, s, c);
+}
 
 template <class R> __device__ __forceinline__ R r_of_double(double x);
 template <> __device__ __forceinline__ double r_of_double<double>(double x) { return x; }
@@ -93,9 +102,9 @@ struct FreqBlock {
 // structure of arrays with stride n (elements) and 9 * n per point.
 template <class R>
 __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
-                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[IBEM_FB],
-                                                const DfTrigCoef &C, cx<R> (&a)[IBEM_FB][3], cx<R> (&b)[IBEM_FB][3],
-                                                R &ct)
+                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[IBEM_FB], R dkf,
+                                                const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C,
+                                                cx<R> (&a)[IBEM_FB][3], cx<R> (&b)[IBEM_FB][3], R &ct)
 {
     for (int q = 0; q < nq; ++q) {
         const R *p = qd + (size_t)q * 9 * n + e;
@@ -108,10 +117,9 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
         const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
         const R ft = r_mul(nd, r_mul(invr, invr));
         r_mac(ct, r_mul(r_add(r_add(wa[0], wa[1]), wa[2]), ft), r_sub(r_zero(R()), invr));
-        const double rd = r_to_double(r);
         cx<R> ph, step;
-        r_sincos(fb.k[0] * rd, C, ph.im, ph.re);
-        if (fb.uniform && fb.nf > 1) r_sincos(fb.dk * rd, C, step.im, step.re);
+        r_sincos(r_mul(kf[0], r), tab, P, C, ph.im, ph.re);
+        if (fb.uniform && fb.nf > 1) r_sincos(r_mul(dkf, r), tab, P, C, step.im, step.re);
         R sa[3];
 #pragma unroll
         for (int v = 0; v < 3; ++v) sa[v] = r_mul(wa[v], ft);
@@ -120,7 +128,7 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
             if (f >= fb.nf) break;
             if (f > 0) {
                 if (fb.uniform) ph = cx_mul(ph, step);
-                else r_sincos(fb.k[f] * rd, C, ph.im, ph.re);
+                else r_sincos(r_mul(kf[f], r), tab, P, C, ph.im, ph.re);
             }
             const R gr = r_mul(ph.re, invr), gi = r_mul(ph.im, invr);
             const R kr = r_mul(kf[f], r);
@@ -185,11 +193,13 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
-    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, double2 *__restrict__ At,
+    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, double2 *__restrict__ At,
     double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
 {
     extern __shared__ __align__(16) unsigned char ibem_smem[];
     cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // IBEM_FB x (A row, B row), m each
+    constexpr bool DF = std::is_same<R, dfl>::value;
+    float4 *tab = DF ? reinterpret_cast<float4 *>(rowbuf + 2 * IBEM_FB * (size_t)m) : nullptr;   // sin/cos table
     __shared__ double ct_red[IBEM_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int row = blockIdx.x;
@@ -207,7 +217,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     R kf[IBEM_FB];
 #pragma unroll
     for (int f = 0; f < IBEM_FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
+    const R dkf = r_of_double<R>(fb.dk);
     for (int j = tid; j < 2 * IBEM_FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
+    if (DF) df_trig_table_fill(tab, tid, blockDim.x);
     double xo, yo, zo;
     int self = -1;
     if (row < m) {
@@ -233,8 +245,8 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             for (int f = 0; f < IBEM_FB; ++f)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
-            regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, C,
-                               a, b, ctr);
+            regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, dkf,
+                               tab, P, C, a, b, ctr);
             ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
@@ -340,23 +352,24 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
     const int rows = m + n_ch + l;
-    const size_t smem = sizeof(double2) * 2 * (size_t)m * IBEM_FB;
+    const size_t smem = sizeof(double2) * 2 * (size_t)m * IBEM_FB + (df32 ? 256 * sizeof(float4) : 0);
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
     static const DfTrigCoef coef = df_trig_coefficients();
+    static const DfTrigRed red = df_trig_reduction_constants();
     dim3 g(rows, (F + IBEM_FB - 1) / IBEM_FB);
     if (df32) {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
-            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, At, Bt, Ahs_t, Bhs_t);
+            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, At, Bt, Ahs_t, Bhs_t);
     } else {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
             mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics,
-            cp, k, c, rho, coef, At, Bt, Ahs_t, Bhs_t);
+            cp, k, c, rho, coef, red, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;

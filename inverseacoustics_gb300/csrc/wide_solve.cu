@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(OA_THREADS) oa_update_kernel(int N, const doub
 // Two-sided FP64 Jacobi on the projected matrix S = X^H E X (N x N Hermitian,
 // nearly diagonal after the refinement steps), one CTA per frequency, S in
 // global memory, the rotations applied to the columns of X as well.  Only
-// pairs coupled above the rounding level of S (|S_ij| > 4 sqrt(N) eps
+// pairs coupled above the rounding level of S (|S_ij| > 2 N eps
 // max|S_ii|) rotate, so the cost follows the clustered pairs the first-order
 // refinement cannot separate (near-degenerate eigenvalues of symmetric
 // geometries).  Round-robin ordering: in a round the pairs are disjoint, their
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
         red[0] = t;
     }
     __syncthreads();
-    const double tol = 4.0 * sqrt((double)N) * 2.220446049250313e-16 * red[0];
+    const double tol = 2.0 * (double)N * 2.220446049250313e-16 * red[0];
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         if (tid == 0) s_rot = 0;
@@ -530,14 +530,33 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
 }
 
 // s (sorted descending), beta = U^H b (sorted like s), rank of every column;
-// U = X, or conj(X) when conj_u.
+// U = X, or conj(X) when conj_u.  Eigenvalues of the FP64 E = H H^H carry an
+// absolute error ~ N eps lambda_max, so singular values below
+// sqrt(N eps) s_1 are not resolved by this path: they are reported at that
+// floor (an exact 0 would otherwise extend the GCV grid, whose lower end is
+// max(s_p, 16 eps s_1), into a spurious lambda -> 0 minimum).  Filter factors
+// of such components are below (floor / lambda)^2 for any useful lambda.
 __global__ void eig_beta_kernel(int m, int N, const double *LAM, const double2 *X, int conj_u, int nrhs,
                                 const double2 *Bv, double *S, double2 *BETA, int *RANK)
 {
+    __shared__ double red[32];
     const int f = blockIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     LAM += (size_t)f * N;
     X += (size_t)f * N * N;
+    double lm = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) lm = fmax(lm, LAM[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    if (lane == 0) red[wid] = lm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t = fmax(t, red[w]);
+        red[0] = t;
+    }
+    __syncthreads();
+    const double floor2 = (double)N * 2.220446049250313e-16 * red[0];
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
         double li = LAM[i];
         int rk = 0;
@@ -546,7 +565,7 @@ __global__ void eig_beta_kernel(int m, int N, const double *LAM, const double2 *
             if (lj > li || (lj == li && j < i)) rk++;
         }
         RANK[(size_t)f * N + i] = rk;
-        S[(size_t)f * N + rk] = sqrt(fmax(li, 0.0));
+        S[(size_t)f * N + rk] = sqrt(fmax(li, floor2));
     }
     __syncthreads();
     for (int r = 0; r < nrhs; ++r) {
