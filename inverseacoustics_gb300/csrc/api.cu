@@ -312,6 +312,46 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
         color[i] = c;
         if (c == ncolors) ++ncolors;
     }
+    // balance: the assembly kernel walks a colour with IA_ASM_THREADS threads
+    // and a barrier after it, so a colour of 129..256 elements costs two
+    // rounds.  Move elements out of colours above that size into the smallest
+    // colour with no neighbour in it (at least ceil(n / IA_ASM_THREADS)
+    // colours), a few passes; greedy sizes like 177, 168, ..., 30, 2 become
+    // all 128 on the icospheres.
+    {
+        const int cap = IA_ASM_THREADS;
+        const int target = std::max(ncolors, (n + cap - 1) / cap);
+        std::vector<int> size(target, 0);
+        for (int i = 0; i < n; ++i) size[color[i]]++;
+        std::vector<char> nbc(target);
+        for (int pass = 0; pass < 20; ++pass) {
+            int moved = 0;
+            for (int i = 0; i < n; ++i) {
+                const int c = color[i];
+                if (size[c] <= cap) continue;
+                std::fill(nbc.begin(), nbc.end(), 0);
+                for (int s = 0; s < 3; ++s)
+                    for (int o : node_elems[elems[i + s * n]])
+                        if (o != i) nbc[color[o]] = 1;
+                int best = -1;
+                for (int d = 0; d < target; ++d)
+                    if (!nbc[d] && size[d] < cap && (best < 0 || size[d] < size[best])) best = d;
+                if (best >= 0) {
+                    color[i] = best;
+                    size[c]--;
+                    size[best]++;
+                    ++moved;
+                }
+            }
+            if (!moved) break;
+        }
+        // drop colours left empty
+        std::vector<int> remap(target, -1);
+        ncolors = 0;
+        for (int d = 0; d < target; ++d)
+            if (size[d] > 0) remap[d] = ncolors++;
+        for (int i = 0; i < n; ++i) color[i] = remap[color[i]];
+    }
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return color[a] < color[b]; });

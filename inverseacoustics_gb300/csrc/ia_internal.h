@@ -15,6 +15,9 @@ struct ia_context {
     int capturing;         // between ia_capture_begin and ia_capture_end
 };
 
+// threads per CTA of the IBEM assembly kernel; mesh colours are balanced to it
+#define IA_ASM_THREADS 128
+
 struct ia_mesh {
     ia_context *ctx;
     int m, n;              // nodes, triangles

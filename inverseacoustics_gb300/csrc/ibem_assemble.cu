@@ -38,7 +38,7 @@
 namespace ia {
 
 constexpr int IBEM_FB = 4;          // frequencies per CTA
-constexpr int IBEM_THREADS = 128;   // 4 warps
+constexpr int IBEM_THREADS = IA_ASM_THREADS;   // 4 warps; mesh colours are balanced to this
 constexpr int IBEM_MAX_NQ = 64;
 
 // ---- the real-type policy -------------------------------------------------
