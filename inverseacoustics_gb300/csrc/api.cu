@@ -523,7 +523,7 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
 
 static size_t transfer_mixed_ws_bytes(int m, int l, int F)
 {
-    return ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 2 * ws_round(16 * (size_t)m * l * F);
+    return ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F);
 }
 
 // Mixed transfer: FP32 LU of M = A^T; Y = M^-1 A_hs^T by FP32 solves refined
@@ -538,22 +538,28 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     float2 *Y32 = cur.take<float2>((size_t)m * l * F);
     double2 *Y = cur.take<double2>((size_t)m * l * F);
     double2 *R = cur.take<double2>((size_t)m * l * F);
-    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true);
+    float4 *Y4 = cur.take<float4>((size_t)m * l * F);
+    // A^T and B^T arrive as double-float pairs (float4, the size of double2)
+    float4 *At4 = reinterpret_cast<float4 *>(At), *Bt4 = reinterpret_cast<float4 *>(Bt);
+    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true);
     if (st) return st;
     const long long sMM = (long long)m * m, sML = (long long)m * l;
-    if ((st = copy2d_batched<double2, float2>(ctx, m, m, At, m, sMM, M32, m, sMM, false, F))) return st;
+    if ((st = df_hi_batched(ctx, (size_t)sMM * F, At4, M32))) return st;
     if ((st = getrf_batched<float2>(ctx, m, M32, m, sMM, ipiv, d_info, F))) return st;
     if ((st = copy2d_batched<double2, float2>(ctx, m, l, Ahs_t, m, sML, Y32, m, sML, false, F))) return st;
     if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
     if ((st = copy2d_batched<float2, double2>(ctx, m, l, Y32, m, sML, Y, m, sML, false, F))) return st;
     for (int it = 0; it < cfg->refine_steps; ++it) {
         if ((st = zcopy2d_batched(ctx, m, l, Ahs_t, m, sML, R, m, sML, false, F))) return st;
-        if ((st = dfgemm_batched(ctx, OP_N, OP_N, m, l, m, -1.0, At, m, sMM, Y, m, sML, 1.0, R, m, sML, F))) return st;
+        if ((st = split_df_batched(ctx, (size_t)sML * F, Y, Y4))) return st;
+        if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, l, m, -1.0, At4, m, sMM, Y4, m, sML, 1.0, R, m, sML, F)))
+            return st;
         if ((st = copy2d_batched<double2, float2>(ctx, m, l, R, m, sML, Y32, m, sML, false, F))) return st;
         if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
         if ((st = add2d_batched<float2>(ctx, m, l, Y32, m, sML, Y, m, sML, F))) return st;
     }
-    return dfgemm_batched(ctx, OP_N, OP_N, m, l, m, 1.0, Bt, m, sMM, Y, m, sML, -1.0, Ht, m, sML, F);
+    if ((st = split_df_batched(ctx, (size_t)sML * F, Y, Y4))) return st;
+    return dfgemm4_batched(ctx, OP_N, OP_N, m, l, m, 1.0, Bt4, m, sMM, Y4, m, sML, -1.0, Ht, m, sML, F);
 }
 
 int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,

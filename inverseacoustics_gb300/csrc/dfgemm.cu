@@ -12,6 +12,7 @@
 // autotuner picks per shape; all sum k in the same order), K tile 8, 256
 // threads, operands split to (hi, lo) on the way into shared memory.
 // op(A), op(B) in {N, C} (C = conjugate transpose).
+#include <type_traits>
 #include "ia_common.cuh"
 #include "ia_internal.h"
 #include "tune.h"
@@ -30,6 +31,19 @@ __device__ __forceinline__ float4 split_c(double2 v, bool conj)
     float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
     float rl = __double2float_rn(v.x - (double)rh), il = __double2float_rn(v.y - (double)ih);
     return make_float4(rh, ih, rl, il);
+}
+
+// an operand element as (re hi, im hi, re lo, im lo): split from FP64 on the
+// way in, or already split (float4 operands, no FP64 instructions)
+__device__ __forceinline__ float4 ld_df(const double2 *P, size_t i, bool conj) { return split_c(P[i], conj); }
+__device__ __forceinline__ float4 ld_df(const float4 *P, size_t i, bool conj)
+{
+    float4 v = P[i];
+    if (conj) {
+        v.y = -v.y;
+        v.w = -v.w;
+    }
+    return v;
 }
 
 // (ah, al) += (xh + xl)(yh + yl), low word renormalised later
@@ -53,10 +67,10 @@ __device__ __forceinline__ void df_norm(float &ah, float &al)
     ah = s;
 }
 
-template <int BM, int BN, int TM, int TN>
+template <int BM, int BN, int TM, int TN, class TA, class TB>
 __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, int N, int K, double alpha,
-                                                     const double2 *__restrict__ A, int lda, long long sA,
-                                                     const double2 *__restrict__ B, int ldb, long long sB,
+                                                     const TA *__restrict__ A, int lda, long long sA,
+                                                     const TB *__restrict__ B, int ldb, long long sB,
                                                      double beta, double2 *__restrict__ C, int ldc, long long sC)
 {
     constexpr int NTX = BN / TN, NTY = BM / TM;
@@ -84,7 +98,7 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
             int gr = m0 + r, gk = k0 + kk;
             float4 v = z4;
             if (gr < M && gk < K)
-                v = opa == OP_N ? split_c(A[gr + (size_t)gk * lda], false) : split_c(A[gk + (size_t)gr * lda], true);
+                v = opa == OP_N ? ld_df(A, gr + (size_t)gk * lda, false) : ld_df(A, gk + (size_t)gr * lda, true);
             As[kk][r] = v;
         }
 #pragma unroll
@@ -95,7 +109,7 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
             int gk = k0 + kk, gc = n0 + c;
             float4 v = z4;
             if (gk < K && gc < N)
-                v = opb == OP_N ? split_c(B[gk + (size_t)gc * ldb], false) : split_c(B[gc + (size_t)gk * ldb], true);
+                v = opb == OP_N ? ld_df(B, gk + (size_t)gc * ldb, false) : ld_df(B, gc + (size_t)gk * ldb, true);
             Bs[kk][c] = v;
         }
         __syncthreads();
@@ -148,22 +162,23 @@ __global__ void __launch_bounds__(256) dfgemm_kernel(int opa, int opb, int M, in
     }
 }
 
-template <int BM, int BN, int TM, int TN>
-static int dfgemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A,
-                         int lda, long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C,
-                         int ldc, long long sC, int batch)
+template <int BM, int BN, int TM, int TN, class TA, class TB>
+static int dfgemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const TA *A, int lda,
+                         long long sA, const TB *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                         long long sC, int batch)
 {
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
-    dfgemm_kernel<BM, BN, TM, TN>
+    dfgemm_kernel<BM, BN, TM, TN, TA, TB>
         <<<grid, 256, 0, ctx->stream>>>(opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
 
 // tile variants: 64x64 (4x4 per thread), 32x32 (2x2), 64x32 (4x2)
-int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
-                   long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
-                   long long sC, int batch)
+template <class TA, class TB>
+static int dfgemm_any(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const TA *A, int lda,
+                      long long sA, const TB *B, int ldb, long long sB, double beta, double2 *C, int ldc, long long sC,
+                      int batch)
 {
     if (M <= 0 || N <= 0 || batch <= 0) return IA_OK;
     if ((opa != OP_N && opa != OP_C) || (opb != OP_N && opb != OP_C)) return IA_ERR_ARG;
@@ -178,7 +193,7 @@ int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double 
         }
     };
     TuneKey key{};
-    key.kernel = TK_DFGEMM;
+    key.kernel = std::is_same<TA, float4>::value ? TK_DFGEMM4 : TK_DFGEMM;
     key.v[0] = opa;
     key.v[1] = opb;
     key.v[2] = M;
@@ -195,6 +210,59 @@ int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double 
         return launch(vv, (double2 *)scratch.p);
     });
     return launch(v, C);
+}
+
+int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
+                   long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                   long long sC, int batch)
+{
+    return dfgemm_any<double2, double2>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC,
+                                        batch);
+}
+
+int dfgemm4_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const float4 *A, int lda,
+                    long long sA, const float4 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                    long long sC, int batch)
+{
+    return dfgemm_any<float4, float4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
+}
+
+// out[e] = (re hi, im hi, re lo, im lo) of in[e]
+__global__ void split_df_kernel(size_t count, const double2 *__restrict__ in, float4 *__restrict__ out)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = split_c(in[e], false);
+}
+
+// out[e] = the high (FP32) parts of in[e]
+__global__ void df_hi_kernel(size_t count, const float4 *__restrict__ in, float2 *__restrict__ out)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = in[e];
+        out[e] = make_float2(v.x, v.y);
+    }
+}
+
+static int grid_for(ia_context *ctx, size_t count)
+{
+    const size_t want = (count + 255) / 256, cap = (size_t)ctx->sm_count * 16;
+    return (int)(want < cap ? want : cap);
+}
+
+int split_df_batched(ia_context *ctx, size_t count, const double2 *in, float4 *out)
+{
+    if (!count) return IA_OK;
+    split_df_kernel<<<grid_for(ctx, count), 256, 0, ctx->stream>>>(count, in, out);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+int df_hi_batched(ia_context *ctx, size_t count, const float4 *in, float2 *out)
+{
+    if (!count) return IA_OK;
+    df_hi_kernel<<<grid_for(ctx, count), 256, 0, ctx->stream>>>(count, in, out);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
 }
 
 }  // namespace ia

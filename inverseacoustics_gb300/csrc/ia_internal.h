@@ -132,6 +132,12 @@ int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, lon
 int dfgemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda,
                    long long sA, const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
                    long long sC, int batch);
+// the same with operands already split to float4 (re hi, im hi, re lo, im lo)
+int dfgemm4_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double alpha, const float4 *A, int lda,
+                    long long sA, const float4 *B, int ldb, long long sB, double beta, double2 *C, int ldc,
+                    long long sC, int batch);
+int split_df_batched(ia_context *ctx, size_t count, const double2 *in, float4 *out);
+int df_hi_batched(ia_context *ctx, size_t count, const float4 *in, float2 *out);
 
 // ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);
@@ -188,10 +194,11 @@ int monopole_batched(ia_context *ctx, int l, int m, int F, const double *mics, c
                      double2 *G);
 int esm_system(ia_context *ctx, int m, int l, const double *src, const double *mics, double r_i, double k, double c,
                double rho, double2 *DT, double2 *RHS);
-// df32: regular-element arithmetic in double-float (mixed path) instead of FP64
+// df32: regular-element arithmetic in double-float (mixed path) instead of FP64;
+// split_ab (with df32): At and Bt are written as float4 (re hi, im hi, re lo, im lo)
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
-              bool df32 = false);
+              bool df32 = false, bool split_ab = false);
 int hels_batched(ia_context *ctx, int npts, const double *pts, int order, int F, const double *k, double c,
                  double rho, double2 *Me, double2 *Qe);
 

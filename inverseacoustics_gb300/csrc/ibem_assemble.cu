@@ -187,13 +187,34 @@ __device__ __forceinline__ void singular_element(const double *__restrict__ eg, 
     }
 }
 
+__device__ __forceinline__ void write_split_rows(int m, int tid, const cx<double> *, const cx<double> *, double,
+                                                 float4 *, float4 *)
+{
+}
+
+__device__ __forceinline__ void write_split_rows(int m, int tid, const cx<dfl> *Ar, const cx<dfl> *Br, double s,
+                                                 float4 *arow, float4 *brow)
+{
+    const dfl sd = df_from_double(s);
+    for (int j = tid; j < m; j += IBEM_THREADS) {
+        if (arow) {
+            const dfl re = df_norm(Ar[j].re), im = df_norm(Ar[j].im);
+            arow[j] = make_float4(re.hi, im.hi, re.lo, im.lo);
+        }
+        if (brow) {
+            const dfl re = df_neg(df_mul(sd, Br[j].im)), im = df_mul(sd, Br[j].re);   // i s B
+            brow[j] = make_float4(re.hi, im.hi, re.lo, im.lo);
+        }
+    }
+}
+
 template <class R>
 __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
-    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, double2 *__restrict__ At,
+    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, int split_ab, double2 *__restrict__ At,
     double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
 {
     extern __shared__ __align__(16) unsigned char ibem_smem[];
@@ -337,6 +358,13 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             arow = Ahs_t ? Ahs_t + ((size_t)fg * l + (row - mt)) * m : nullptr;
             brow = Bhs_t ? Bhs_t + ((size_t)fg * l + (row - mt)) * m : nullptr;
         }
+        if (DF && split_ab && row < mt) {
+            // A and B rows of the surface system as (re hi, im hi, re lo, im lo)
+            // pairs for the double-float GEMMs (the normalised pair equals the
+            // split of the FP64 value)
+            write_split_rows(m, tid, Ar, Br, s, reinterpret_cast<float4 *>(arow), reinterpret_cast<float4 *>(brow));
+            continue;
+        }
         for (int j = tid; j < m; j += blockDim.x) {
             if (arow) arow[j] = make_double2(r_to_double(Ar[j].re), r_to_double(Ar[j].im));
             const double br = r_to_double(Br[j].re), bi = r_to_double(Br[j].im);
@@ -347,7 +375,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
 
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
-              bool df32)
+              bool df32, bool split_ab)
 {
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
@@ -362,14 +390,14 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
-            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, At, Bt, Ahs_t, Bhs_t);
+            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, split_ab ? 1 : 0, At, Bt, Ahs_t, Bhs_t);
     } else {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
             mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics,
-            cp, k, c, rho, coef, red, At, Bt, Ahs_t, Bhs_t);
+            cp, k, c, rho, coef, red, 0, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;

@@ -270,8 +270,9 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     if (nw < 1) nw = 1;
     // FP64: rotate while |y_i^H y_j| > sqrt(Mdot) eps |y_i||y_j|.  FP32 (the
     // mixed path, always followed by FP64 eigen-refinement): 8x that, above
-    // the rounding noise of FP32 dot products, so sweeps stop when the
-    // remaining rotations would only chase noise.
+    // the rounding noise of FP32 dot products.  A looser start (64x) cut the
+    // FP32 sweeps but left more coupled pairs for the FP64 Jacobi on X^H E X
+    // and made the whole solve slower.
     const double eps = sizeof(R) == 8 ? 2.220446049250313e-16 : 8.0 * 1.1920928955078125e-07;
     const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;

@@ -19,7 +19,15 @@ struct TuneKey {
     int v[8];        // shape / op parameters
 };
 
-enum TuneKernel { TK_GEMM_Z = 1, TK_GEMM_C = 2, TK_DFGEMM = 3, TK_RGEMM_D = 4, TK_RGEMM_S = 5, TK_RDFGEMM = 6 };
+enum TuneKernel {
+    TK_GEMM_Z = 1,
+    TK_GEMM_C = 2,
+    TK_DFGEMM = 3,
+    TK_RGEMM_D = 4,
+    TK_RGEMM_S = 5,
+    TK_RDFGEMM = 6,
+    TK_DFGEMM4 = 7
+};
 
 // Variant for key: the table entry, or (when absent) the result of timing
 // run(variant) for variant in [0, nvar) -- run must launch on scratch outputs --
