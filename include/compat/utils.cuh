@@ -7,7 +7,8 @@
 //   sphere       <- CUDA/utils.cuh:384   analytic pulsating sphere (input
 //                   preparation, host): p = (a/r) rho c u (ika/(ika-1)) e^{ik(r-a)}
 //   cartesian_2_spherical <- CUDA/utils.cuh:414  (az, el, r), same branch rules
-// The reference's debug printers/writers and gmsh reader are not part of it.
+//   geometry     <- CUDA/utils.cuh:291   gmsh v2.2 reader (ia_read_msh, host)
+// The reference's debug printers/writers are not part of it.
 #pragma once
 #include <cmath>
 #include "ia_compat_common.cuh"
@@ -64,4 +65,12 @@ inline void cartesian_2_spherical(int m, double *r_xx, double **azelr)
         (*azelr)[i] = std::atan2(y, x) + (y < 0 ? 2.0 * M_PI : 0.0);
         (*azelr)[i + m] = std::atan2(std::sqrt(xy), z) - (x < 0 ? 2.0 * M_PI : 0.0);
     }
+}
+
+// geometry <- CUDA/utils.cuh:291  gmsh v2.2 reader (ia_read_msh, host); throws
+// where the reference calls exit()
+inline void geometry(double **r_ms, double **r_lh, int **e_n, double k, double t, int *m_out, int *l_out, int *n_out,
+                     char *file)
+{
+    ia_compat_check(ia_read_msh(file, k, t, r_ms, r_lh, e_n, m_out, l_out, n_out), "geometry");
 }

@@ -101,6 +101,15 @@ const char *ia_version(void);
 int ia_last_cuda_error(void);
 void ia_free(void *p);
 
+/* gmsh v2.2 ASCII mesh reader; replaces geometry() (CUDA/utils.cuh:291).
+ * Nodes r_ms (3 x m SoA), triangles e_n (element type 2 with three distinct
+ * vertices, 0-based, 3 x n SoA, file order) and field points
+ * r_lh = r_ms (1 + (2 pi / k) t) (3 x m), all malloc'd by the callee (free
+ * with ia_free).  Host only, no GPU needed.  A missing or malformed file
+ * returns IA_ERR_ARG (the reference calls exit()). */
+int ia_read_msh(const char *file, double k, double t, double **r_ms, double **r_lh, int **e_n, int *m, int *l,
+                int *n);
+
 /* ---------------------------------------------------------------- layer 1 */
 
 /* ESM: Me = M_sq D^-1 (m x m), He = M_hq D^-1 (l x m), sources at r_ms*r_i.

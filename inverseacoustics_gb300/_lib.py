@@ -54,6 +54,7 @@ _SIGS = {
     "ia_version": (C.c_char_p, []),
     "ia_last_cuda_error": (_I, []),
     "ia_free": (None, [_P]),
+    "ia_read_msh": (_I, [C.c_char_p, _D, _D, _PP, _PP, _PP, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "ia_esm": (_I, [_I, _I, _P, _P, _PP, _PP, _D, _D, _P]),
     "ia_ibem": (_I, [_I, _I, _I, _P, _P, _P, _PP, _PP, _D, _I, _P, _P, _P]),
     "ia_hels": (_I, [_I, _I, _P, _P, _PP, _PP, _PP, _D, _I, _P]),

@@ -164,6 +164,20 @@ def sound_power(p, v, s):
     return w.value
 
 
+def read_msh(path, k, t=0.0):
+    """gmsh v2.2 mesh -- geometry() CUDA/utils.cuh:291.  Returns (nodes (3, m),
+    field points (3, m) = nodes (1 + 2 pi t / k), triangles (3, n) int32)."""
+    L = _lib.lib()
+    rm, rl, en = _P(), _P(), _P()
+    m, l, n = C.c_int(), C.c_int(), C.c_int()
+    check(L.ia_read_msh(str(path).encode(), float(k), float(t), C.byref(rm), C.byref(rl), C.byref(en), C.byref(m),
+                        C.byref(l), C.byref(n)), "ia_read_msh")
+    nodes = _take(rm, 3 * m.value, np.float64).reshape(3, m.value)
+    field = _take(rl, 3 * l.value, np.float64).reshape(3, l.value)
+    elems = _take(en, 3 * n.value, np.int32).reshape(3, n.value)
+    return nodes, field, elems
+
+
 # ------------------------------------------------------------- device layer
 def _dptr(t, dtype=None):
     import torch

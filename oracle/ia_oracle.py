@@ -531,3 +531,53 @@ def esm_design_grad(mics, surface, retreat, k, loglam, q, noise=None):
         gd += float((c[None] * D * unit[:, None, :]).sum())
         gl[f] = -2.0 * lam * lam * float(np.real(np.sum(z.conj() * y)))
     return gm, gd, gl
+
+
+# ---------------------------------------------------------------------------
+# gmsh v2.2 reader (CUDA/utils.cuh:291-382)
+# ---------------------------------------------------------------------------
+def read_msh(path, k, t):
+    """Nodes (3, m), field points (3, m) = nodes (1 + 2 pi t / k), triangles
+    (3, n) 0-based: element type 2 whose three vertices differ, in file order
+    (utils.cuh:331-357; the tag count is read from the line, the reference
+    assumes two)."""
+    lines = open(path).read().splitlines()
+    i = lines.index("$Nodes")
+    m = int(lines[i + 1])
+    nodes = np.array([[float(v) for v in lines[i + 2 + j].split()[1:4]] for j in range(m)]).T
+    j = lines.index("$Elements")
+    ne = int(lines[j + 1])
+    tris = []
+    for line in lines[j + 2:j + 2 + ne]:
+        f = [int(v) for v in line.split()]
+        if f[1] != 2:
+            continue
+        v = f[3 + f[2]:6 + f[2]]
+        v = [x - 1 for x in v]
+        if v[0] != v[1] and v[0] != v[2] and v[1] != v[2]:
+            tris.append(v)
+    elems = np.array(tris, dtype=np.int32).T.reshape(3, -1)
+    scale = 1.0 + (2.0 * math.pi / k) * t
+    return np.ascontiguousarray(nodes), np.ascontiguousarray(nodes * scale), np.ascontiguousarray(elems)
+
+
+def write_msh(path, nodes, elems, extra_points=0, degenerate=0):
+    """gmsh v2.2 ASCII file of the mesh (test input generator): optional point
+    elements (type 15) and degenerate triangles to exercise the filter."""
+    m, n = nodes.shape[1], elems.shape[1]
+    rows = []
+    for p in range(extra_points):
+        rows.append(f"15 2 0 {p + 1} {p + 1}")
+    for e in range(n):
+        a, b, c = (int(x) + 1 for x in elems[:, e])
+        rows.append(f"2 2 0 1 {a} {b} {c}")
+        if e < degenerate:
+            rows.append(f"2 2 0 1 {a} {a} {c}")
+    with open(path, "w") as fh:
+        fh.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % m)
+        for j in range(m):
+            fh.write("%d %.17g %.17g %.17g\n" % (j + 1, nodes[0, j], nodes[1, j], nodes[2, j]))
+        fh.write("$EndNodes\n$Elements\n%d\n" % len(rows))
+        for i, r in enumerate(rows):
+            fh.write(f"{i + 1} {r}\n")
+        fh.write("$EndElements\n")

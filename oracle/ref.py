@@ -47,6 +47,8 @@ def lib():
         _lib.ref_sphere.argtypes = [P, P, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.c_double, C.c_double,
                                     C.c_double, C.c_int, C.c_int]
         _lib.ref_cart2sph.argtypes = [C.c_int, P, C.POINTER(P)]
+        _lib.ref_geometry.argtypes = [C.c_char_p, C.c_double, C.c_double, C.POINTER(P), C.POINTER(P), C.POINTER(P),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib.ref_free.argtypes = [P]
         _lib.ref_c_air.restype = C.c_double
         _lib.ref_rho_air.restype = C.c_double
@@ -160,3 +162,18 @@ def read_reference_rules(ref_cuda_dir):
     sing = np.array(pages)
     assert sing.shape == (3, nsg, 3)
     return reg, sing
+
+
+def geometry(path, k, t):
+    """Reference geometry() (CUDA/utils.cuh:291): gmsh v2.2 nodes, triangles
+    and field points r (1 + 2 pi t / k).  Returns (r_ms (3, m), r_lh (3, l),
+    e_n (3, n))."""
+    P = C.c_void_p
+    rm, rl, en = P(), P(), P()
+    m, l, n = C.c_int(), C.c_int(), C.c_int()
+    lib().ref_geometry(str(path).encode(), float(k), float(t), C.byref(rm), C.byref(rl), C.byref(en), C.byref(m),
+                       C.byref(l), C.byref(n))
+    r_ms = _take(rm, 3 * m.value, np.float64).reshape(3, m.value)
+    r_lh = _take(rl, 3 * l.value, np.float64).reshape(3, l.value)
+    e_n = _take(en, 3 * n.value, np.int32).reshape(3, n.value)
+    return r_ms, r_lh, e_n

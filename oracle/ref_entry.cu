@@ -12,6 +12,7 @@
 // Exported (C linkage, thin adapters defined here):
 //   ref_sphere          -> sphere                CUDA/utils.cuh:384
 //   ref_cart2sph        -> cartesian_2_spherical CUDA/utils.cuh:414
+//   ref_geometry        -> geometry (gmsh v2.2)  CUDA/utils.cuh:291
 //   ref_free            -> free() for the callee-malloc'd outputs
 #include <cstdio>
 #include <cstdlib>
@@ -37,6 +38,12 @@ extern "C" void ref_sphere(double *r_ms, double *r_lh, cuDoubleComplex **p_s, cu
 }
 
 extern "C" void ref_cart2sph(int m, double *r_xx, double **azelr) { cartesian_2_spherical(m, r_xx, azelr); }
+
+extern "C" void ref_geometry(const char *file, double k, double t, double **r_ms, double **r_lh, int **e_n, int *m,
+                             int *l, int *n)
+{
+    geometry(r_ms, r_lh, e_n, k, t, m, l, n, const_cast<char *>(file));
+}
 
 extern "C" void ref_free(void *p) { free(p); }
 

@@ -16,6 +16,8 @@ cartesian_2_spherical(), built with C_AIR=343, RHO_AIR=1.21):
   esm_src (3, 42), esm_fld (3, 42), esm_k, esm_ri, esm_Me, esm_He   esm(), l == m
   kat_ps, kat_ph, kat_u, kat_a     sphere() analytic pressures at mesh nodes / mics
   sph_in (3, 12), sph_out (3, 12)  cartesian_2_spherical()
+  msh_k, msh_t, msh_nodes, msh_field, msh_elems   geometry() on tests/golden/sphere42.msh
+      (the mesh above as gmsh v2.2 text with 3 point elements and 2 degenerate triangles)
 """
 from __future__ import annotations
 
@@ -60,6 +62,14 @@ def main():
     out.update(kat_ps=ps, kat_ph=ph, kat_u=np.array(0.02), kat_a=np.array(0.10))
     P = rng.normal(size=(3, 12))
     out.update(sph_in=P, sph_out=ref.cart2sph(P))
+    # gmsh v2.2 file of the same mesh with point elements and degenerate
+    # triangles, read by the reference's geometry()
+    msh = os.path.join(HERE, "sphere42.msh")
+    from oracle import ia_oracle as O
+    O.write_msh(msh, nodes, elems, extra_points=3, degenerate=2)
+    msh_k, msh_t = 2 * np.pi * 500.0 / c, 0.3
+    rn, rl, en = ref.geometry(msh, msh_k, msh_t)
+    out.update(msh_k=np.array(msh_k), msh_t=np.array(msh_t), msh_nodes=rn, msh_field=rl, msh_elems=en)
     path = os.path.join(HERE, "ref_vectors.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes")
