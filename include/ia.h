@@ -60,7 +60,23 @@ typedef enum {
 
 enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
 enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };
-enum { IA_METHOD_TIKHONOV_GCV = 0, IA_METHOD_TSVD = 1, IA_METHOD_TIKHONOV_FIXED = 2 };
+/* Regularisation: filter and lambda selector.  Tikhonov filter s^2/(s^2+l^2)
+ * (MATLAB/regtools/tikhonovG.m), damped SVD s/(s+l) (dsvdG.m), TSVD
+ * (tsvdG.m); lambda by GCV (gcvG.m), the L-curve corner (l_curveG.m,
+ * lcfunG.m), the quasi-optimality criterion (quasioptG.m) or lambda_fixed.
+ * The grid-based selectors share gcv_points.  With IA_PREC_MIXED the damped-SVD
+ * methods run the FP64 solve (their 1/(s + lambda) weights keep the
+ * components of singular values the mixed path does not resolve). */
+enum {
+    IA_METHOD_TIKHONOV_GCV = 0,
+    IA_METHOD_TSVD = 1,
+    IA_METHOD_TIKHONOV_FIXED = 2,
+    IA_METHOD_TIKHONOV_LCURVE = 3,
+    IA_METHOD_TIKHONOV_QUASIOPT = 4,
+    IA_METHOD_DSVD_FIXED = 5,
+    IA_METHOD_DSVD_LCURVE = 6,
+    IA_METHOD_DSVD_QUASIOPT = 7
+};
 
 typedef struct {
     double c;              /* speed of sound [m/s]; reference C_AIR (CUDA/constants.cuh:2) */
@@ -70,7 +86,7 @@ typedef struct {
     int gcv_points;        /* grid size, 200 in gcvG.m:20 */
     double gcv_lo;         /* fixed log-spaced grid [gcv_lo, gcv_hi]; both 0 selects */
     double gcv_hi;         /*   regtools' grid max(s_p, 16 eps s_1) .. s_1 (gcvG.m:28-30) */
-    double lambda_fixed;   /* lambda for IA_METHOD_TIKHONOV_FIXED */
+    double lambda_fixed;   /* lambda for IA_METHOD_TIKHONOV_FIXED / IA_METHOD_DSVD_FIXED */
     int tsvd_k;            /* truncation index for IA_METHOD_TSVD, 1 <= k <= p */
     int precision;         /* IA_PREC_FP64 or IA_PREC_MIXED */
     int svd_max_sweeps;    /* Jacobi sweep cap (default 40) */

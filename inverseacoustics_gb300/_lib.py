@@ -20,6 +20,8 @@ IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE = 1, 2, 4
 IA_GCV_STANDARD, IA_GCV_REFERENCE = 0, 1
 IA_PREC_FP64, IA_PREC_MIXED = 0, 1
 IA_METHOD_TIKHONOV_GCV, IA_METHOD_TSVD, IA_METHOD_TIKHONOV_FIXED = 0, 1, 2
+IA_METHOD_TIKHONOV_LCURVE, IA_METHOD_TIKHONOV_QUASIOPT = 3, 4
+IA_METHOD_DSVD_FIXED, IA_METHOD_DSVD_LCURVE, IA_METHOD_DSVD_QUASIOPT = 5, 6, 7
 
 
 class IAError(RuntimeError):

@@ -617,11 +617,22 @@ int ia_regularize_batch(ia_context *ctx, int m, int n, int F, const ia_complex *
 }
 
 // SVD + regularisation on an operator given as A (m x n) or its transpose.
+// The mixed wide solve rebuilds x in data space, x = H^H U diag(phi / s) beta,
+// which needs s only where phi / s stays small for unresolved s (Tikhonov,
+// TSVD).  The damped SVD weights every component by 1/(s + lambda), so it
+// takes the FP64 wide solve in both precisions.
+static bool use_mixed_wide(int m, int n, const ia_config *cfg)
+{
+    const bool damped = cfg->method == IA_METHOD_DSVD_FIXED || cfg->method == IA_METHOD_DSVD_LCURVE ||
+                        cfg->method == IA_METHOD_DSVD_QUASIOPT;
+    return m <= n && cfg->precision == IA_PREC_MIXED && !damped;
+}
+
 static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bool transposed, int nrhs,
                       const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                       WsCursor &cur)
 {
-    if (m <= n && cfg->precision == IA_PREC_MIXED)
+    if (use_mixed_wide(m, n, cfg))
         return wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     const int p = m < n ? m : n;
@@ -638,7 +649,7 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
 
 static size_t solve_ws_bytes(int m, int n, int F, int nrhs, const ia_config *cfg)
 {
-    if (m <= n && cfg->precision == IA_PREC_MIXED) return wide_solve_mixed_ws_bytes(m, n, nrhs, F);
+    if (use_mixed_wide(m, n, cfg)) return wide_solve_mixed_ws_bytes(m, n, nrhs, F);
     if (m <= n) return wide_solve_ws_bytes(m, n, nrhs, F);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;

@@ -75,15 +75,17 @@ __device__ __forceinline__ double gcv_bisect(const GcvData &d, double lo, double
     return exp(0.5 * (a + b));
 }
 
-// Brent's bounded minimiser, fminbnd tolerances tol1 = sqrt(eps)|x| + tolx/3,
-// tolx = 1e-4; every lane runs the same control flow.
-__device__ __forceinline__ double fminbnd_dev(const GcvData &d, double ax, double bx, int lane)
+// Brent's bounded minimiser of obj(x) (a warp-uniform value), fminbnd
+// tolerances tol1 = sqrt(eps)|x| + tolx/3, tolx = 1e-4; every lane runs the
+// same control flow.
+template <class Obj>
+__device__ __forceinline__ double brent_min(const Obj &obj, double ax, double bx)
 {
     const double seps = 1.4901161193847656e-08, tolx = 1e-4;
     const double cg = 0.5 * (3.0 - sqrt(5.0));
     double a = ax, b = bx;
     double v = a + cg * (b - a), w = v, xf = v, dd = 0.0, e = 0.0;
-    double fx = gcv_value(d, xf, IA_GCV_REFERENCE, false, lane);
+    double fx = obj(xf);
     double fv = fx, fw = fx;
     double xm = 0.5 * (a + b);
     double tol1 = seps * fabs(xf) + tolx / 3.0, tol2 = 2.0 * tol1;
@@ -112,7 +114,7 @@ __device__ __forceinline__ double fminbnd_dev(const GcvData &d, double ax, doubl
             dd = cg * e;
         }
         double x = xf + (dd >= 0.0 ? 1.0 : -1.0) * fmax(fabs(dd), tol1);
-        double fu = gcv_value(d, x, IA_GCV_REFERENCE, false, lane);
+        double fu = obj(x);
         if (fu <= fx) {
             if (x >= xf) a = xf;
             else b = xf;
@@ -134,6 +136,65 @@ __device__ __forceinline__ double fminbnd_dev(const GcvData &d, double ax, doubl
         tol2 = 2.0 * tol1;
     }
     return xf;
+}
+
+__device__ __forceinline__ double fminbnd_dev(const GcvData &d, double ax, double bx, int lane)
+{
+    return brent_min([&](double x) { return gcv_value(d, x, IA_GCV_REFERENCE, false, lane); }, ax, bx);
+}
+
+// Filter factor f(lambda) and, for the L-curve, its use as written in
+// lcfunG.m: Tikhonov s^2/(s^2+l^2), damped SVD s/(s+l) (dsvdG.m).
+__device__ __forceinline__ double filt(double s, double lam, bool damped)
+{
+    return damped ? s / (s + lam) : (s * s) / (s * s + lam * lam);
+}
+
+// Negative curvature of the L-curve (log rho, log eta) at lambda, restating
+// lcfunG.m:12-49: xi = beta/s (0 where s = 0), rho^2 = sum (1-f)^2 |beta|^2
+// (+ the least-squares residual rho_ls2), eta^2 = sum f^2 |xi|^2, and the
+// derivative sums phi, psi, dphi, dpsi with f1 = -2 f (1-f)/l,
+// f2 = -f1 (3 - 4f)/l (lcfunG.m uses these for both filters).
+__device__ __forceinline__ double lcurve_value(const double *s, const double *b2, int p, double rho_ls2, double lam,
+                                               bool damped, int lane)
+{
+    double eta2 = 0, rho2 = 0, phi = 0, psi = 0, dphi = 0, dpsi = 0;
+    for (int j = lane; j < p; j += 32) {
+        const double sj = s[j], bb = b2[j];
+        const double xx = sj > 0.0 ? bb / (sj * sj) : 0.0;
+        const double f = filt(sj, lam, damped), cf = 1.0 - f;
+        const double f1 = -2.0 * f * cf / lam, f2 = -f1 * (3.0 - 4.0 * f) / lam;
+        eta2 = fma(f * f, xx, eta2);
+        rho2 = fma(cf * cf, bb, rho2);
+        phi = fma(f * f1, xx, phi);
+        psi = fma(cf * f1, bb, psi);
+        dphi = fma(f1 * f1 + f * f2, xx, dphi);
+        dpsi = fma(-f1 * f1 + cf * f2, bb, dpsi);
+    }
+    const double eta = sqrt(warp_sum(eta2)), rho = sqrt(warp_sum(rho2) + rho_ls2);
+    phi = warp_sum(phi);
+    psi = warp_sum(psi);
+    dphi = warp_sum(dphi);
+    dpsi = warp_sum(dpsi);
+    const double deta = phi / eta, drho = -psi / rho;
+    const double ddeta = dphi / eta - deta * (deta / eta), ddrho = -dpsi / rho - drho * (drho / rho);
+    const double dle = deta / eta, dlr = drho / rho;
+    const double ddle = ddeta / eta - dle * dle, ddlr = ddrho / rho - dlr * dlr;
+    return -(dlr * ddle - ddlr * dle) / pow(dlr * dlr + dle * dle, 1.5);
+}
+
+// Quasi-optimality function Q(lambda) = || (1-f) f xi || (quasioptG.m:31-37)
+__device__ __forceinline__ double quasiopt_value(const double *s, const double *b2, int p, double lam, bool damped,
+                                                 int lane)
+{
+    double q = 0.0;
+    for (int j = lane; j < p; j += 32) {
+        const double sj = s[j];
+        const double xx = sj > 0.0 ? b2[j] / (sj * sj) : 0.0;
+        const double f = filt(sj, lam, damped), g = (1.0 - f) * f;
+        q = fma(g * g, xx, q);
+    }
+    return sqrt(warp_sum(q));
 }
 
 __device__ __forceinline__ double gcv_grid_point(bool fixed, double lhi, double llo, double ratio, double rpm, int np,
@@ -190,10 +251,85 @@ static __device__ double select_lambda(const double *s, const double *b2, int p,
     return s_lam;
 }
 
-// filter factor times beta for the chosen method
+// Grid minimum, then Brent (fminbnd tolerances) on the bracket of the grid
+// points either side of it -- the scheme of l_curveG.m:42-53 and
+// quasioptG.m:24-41 -- over a descending geometric grid of np values from s1
+// down to rpm.  obj is warp-cooperative.  Returns lambda in every thread.
+template <class Obj>
+static __device__ double grid_brent(const Obj &obj, double s1, double rpm, int np, double *gval)
+{
+    __shared__ double s_lam;
+    __shared__ int s_jmin;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const double ratio = pow(s1 / rpm, 1.0 / (np - 1));
+    for (int t = wid; t < np; t += nw) {
+        const double g = obj(pow(ratio, (double)(np - 1 - t)) * rpm);
+        if (lane == 0) gval[t] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {   // first minimum; NaN never wins (MATLAB min)
+        int jm = 0;
+        double gm = gval[0];
+        for (int t = 1; t < np; ++t)
+            if (gval[t] < gm || !(gm == gm)) { gm = gval[t]; jm = t; }
+        s_jmin = jm;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int jm = s_jmin;
+        const int jl = jm + 1 < np ? jm + 1 : np - 1, jh = jm - 1 > 0 ? jm - 1 : 0;
+        const double lo = pow(ratio, (double)(np - 1 - jl)) * rpm, hi = pow(ratio, (double)(np - 1 - jh)) * rpm;
+        const double res = brent_min(obj, lo, hi);
+        if (lane == 0) s_lam = res;
+    }
+    __syncthreads();
+    return s_lam;
+}
+
+// lambda for cfg.method: GCV (select_lambda), L-curve corner (l_curveG.m;
+// grid down to max(s_p, 16 eps s_1), least-squares residual delta0 when
+// m > p), quasi-optimality (quasioptG.m; grid down to s_p), a fixed value, or
+// 0 for TSVD.
+static __device__ double choose_lambda(const double *s, const double *b2, int p, double delta0, double dof,
+                                       const ia_config &cfg, double *gval)
+{
+    const int mth = cfg.method;
+    if (mth == IA_METHOD_TIKHONOV_GCV) return select_lambda(s, b2, p, delta0, dof, cfg, gval);
+    if (mth == IA_METHOD_TIKHONOV_FIXED || mth == IA_METHOD_DSVD_FIXED) return cfg.lambda_fixed;
+    if (mth == IA_METHOD_TSVD) return 0.0;
+    const double s1 = s[0];
+    if (!(s1 > 0.0)) return 0.0;
+    const bool damped = mth == IA_METHOD_DSVD_LCURVE || mth == IA_METHOD_DSVD_QUASIOPT;
+    const int lane = threadIdx.x & 31;
+    const double floor = s1 * 16.0 * 2.220446049250313e-16;
+    if (mth == IA_METHOD_TIKHONOV_LCURVE || mth == IA_METHOD_DSVD_LCURVE) {
+        auto obj = [&](double lam) { return lcurve_value(s, b2, p, delta0, lam, damped, lane); };
+        return grid_brent(obj, s1, fmax(s[p - 1], floor), cfg.gcv_points, gval);
+    }
+    auto obj = [&](double lam) { return quasiopt_value(s, b2, p, lam, damped, lane); };
+    return grid_brent(obj, s1, s[p - 1] > 0.0 ? s[p - 1] : floor, cfg.gcv_points, gval);
+}
+
+// host-side validation of the regularisation settings for p singular values
+inline int check_method(const ia_config &cfg, int p)
+{
+    if (cfg.method < IA_METHOD_TIKHONOV_GCV || cfg.method > IA_METHOD_DSVD_QUASIOPT) return IA_ERR_ARG;
+    if (cfg.method == IA_METHOD_TSVD && (cfg.tsvd_k < 1 || cfg.tsvd_k > p)) return IA_ERR_ARG;
+    const bool grid = cfg.method == IA_METHOD_TIKHONOV_GCV || cfg.method == IA_METHOD_TIKHONOV_LCURVE ||
+                      cfg.method == IA_METHOD_TIKHONOV_QUASIOPT || cfg.method == IA_METHOD_DSVD_LCURVE ||
+                      cfg.method == IA_METHOD_DSVD_QUASIOPT;
+    if (grid && cfg.gcv_points < 2) return IA_ERR_ARG;
+    if ((cfg.method == IA_METHOD_TIKHONOV_FIXED || cfg.method == IA_METHOD_DSVD_FIXED) && !(cfg.lambda_fixed >= 0.0))
+        return IA_ERR_ARG;
+    return IA_OK;
+}
+
+// filter factor over s (x = V diag(phi) beta) for the chosen method
 __device__ __forceinline__ double filter_phi(int method, int j, double sj, double lam, int tsvd_k)
 {
     if (method == IA_METHOD_TSVD) return (j < tsvd_k) ? 1.0 / sj : 0.0;
+    if (method == IA_METHOD_DSVD_FIXED || method == IA_METHOD_DSVD_LCURVE || method == IA_METHOD_DSVD_QUASIOPT)
+        return (sj + lam) > 0.0 ? 1.0 / (sj + lam) : 0.0;       // damped SVD, dsvdG.m:26
     const double l2 = lam * lam;
     return (sj > 0.0 || l2 > 0.0) ? sj / (sj * sj + l2) : 0.0;
 }

@@ -61,9 +61,7 @@ __global__ void __launch_bounds__(REG_THREADS) regularize_kernel(int m, int n, i
         s_d0 = (m > p && d0 > 0.0) ? d0 : 0.0;
     }
     __syncthreads();
-    double lam = 0.0;
-    if (cfg.method == IA_METHOD_TIKHONOV_GCV) lam = select_lambda(s, b2, p, s_d0, (double)(m - p), cfg, gval);
-    else if (cfg.method == IA_METHOD_TIKHONOV_FIXED) lam = cfg.lambda_fixed;
+    const double lam = choose_lambda(s, b2, p, s_d0, (double)(m - p), cfg, gval);
     for (int j = threadIdx.x; j < p; j += blockDim.x) z[j] = zscale(z[j], filter_phi(cfg.method, j, s[j], lam, cfg.tsvd_k));
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -78,8 +76,7 @@ int regularize_batched(ia_context *ctx, int m, int n, int p, int batch, const do
                        const double2 *V, int nrhs, const double2 *b, const ia_config *cfg, double2 *x,
                        double *lambda)
 {
-    if (cfg->method == IA_METHOD_TSVD && (cfg->tsvd_k < 1 || cfg->tsvd_k > p)) return IA_ERR_ARG;
-    if (cfg->method == IA_METHOD_TIKHONOV_GCV && cfg->gcv_points < 2) return IA_ERR_ARG;
+    if (int st = check_method(*cfg, p)) return st;
     size_t smem = sizeof(double) * (size_t)p * 2 + sizeof(double2) * (size_t)p + sizeof(double) * (size_t)cfg->gcv_points;
     if (smem > 200 * 1024) return IA_ERR_TOO_LARGE;
     IA_CUDA_TRY(cudaFuncSetAttribute(regularize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -119,9 +116,7 @@ __global__ void __launch_bounds__(REG_THREADS) gcv_beta_kernel(int m, int p, con
         s_d0 = d0;
     }
     __syncthreads();
-    double lam = 0.0;
-    if (cfg.method == IA_METHOD_TIKHONOV_GCV) lam = select_lambda(s, b2, p, s_d0, (double)(m - p), cfg, gval);
-    else if (cfg.method == IA_METHOD_TIKHONOV_FIXED) lam = cfg.lambda_fixed;
+    const double lam = choose_lambda(s, b2, p, s_d0, (double)(m - p), cfg, gval);
     for (int j = threadIdx.x; j < p; j += blockDim.x) z[j] = zscale(beta[j], filter_phi(cfg.method, j, s[j], lam, cfg.tsvd_k));
     if (LAM && threadIdx.x == 0) LAM[(size_t)f * nrhs + r] = (cfg.method == IA_METHOD_TSVD) ? 0.0 : lam;
 }
@@ -129,8 +124,7 @@ __global__ void __launch_bounds__(REG_THREADS) gcv_beta_kernel(int m, int p, con
 int gcv_beta_batched(ia_context *ctx, int m, int p, int batch, const double *s, int nrhs, const double2 *beta,
                      const double *bnorm2, const ia_config *cfg, double2 *z, double *lambda)
 {
-    if (cfg->method == IA_METHOD_TSVD && (cfg->tsvd_k < 1 || cfg->tsvd_k > p)) return IA_ERR_ARG;
-    if (cfg->method == IA_METHOD_TIKHONOV_GCV && cfg->gcv_points < 2) return IA_ERR_ARG;
+    if (int st = check_method(*cfg, p)) return st;
     size_t smem = sizeof(double) * ((size_t)p * 2 + (size_t)cfg->gcv_points);
     if (smem > 200 * 1024) return IA_ERR_TOO_LARGE;
     IA_CUDA_TRY(cudaFuncSetAttribute(gcv_beta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

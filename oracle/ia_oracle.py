@@ -581,3 +581,93 @@ def write_msh(path, nodes, elems, extra_points=0, degenerate=0):
         for i, r in enumerate(rows):
             fh.write(f"{i + 1} {r}\n")
         fh.write("$EndElements\n")
+
+
+# ---------------------------------------------------------------------------
+# Other lambda selectors and the damped SVD (MATLAB/regtools/l_curveG.m,
+# lcfunG.m, quasioptG.m, dsvdG.m), filter 't' (Tikhonov) or 'd' (damped SVD)
+# ---------------------------------------------------------------------------
+def _filter(s, lam, method):
+    return s / (s + lam) if method == "d" else s * s / (s * s + lam * lam)
+
+
+def lcfun(lam, s, beta, xi, method, rho_ls2=0.0):
+    """Negative curvature of the L-curve at lam (lcfunG.m:12-49)."""
+    f = _filter(s, lam, method)
+    cf = 1.0 - f
+    xx, bb = np.abs(xi) ** 2, np.abs(beta) ** 2
+    eta = math.sqrt(float(np.sum(f * f * xx)))
+    rho = math.sqrt(float(np.sum(cf * cf * bb)) + rho_ls2)
+    f1 = -2.0 * f * cf / lam
+    f2 = -f1 * (3.0 - 4.0 * f) / lam
+    phi = float(np.sum(f * f1 * xx))
+    psi = float(np.sum(cf * f1 * bb))
+    dphi = float(np.sum((f1 ** 2 + f * f2) * xx))
+    dpsi = float(np.sum((-f1 ** 2 + cf * f2) * bb))
+    deta, drho = phi / eta, -psi / rho
+    ddeta = dphi / eta - deta * (deta / eta)
+    ddrho = -dpsi / rho - drho * (drho / rho)
+    dle, dlr = deta / eta, drho / rho
+    ddle, ddlr = ddeta / eta - dle ** 2, ddrho / rho - dlr ** 2
+    return -(dlr * ddle - ddlr * dle) / (dlr ** 2 + dle ** 2) ** 1.5
+
+
+def l_curve(U, s, b, method="t", npoints=200):
+    """L-curve corner (l_curveG.m:21-53): grid from s_1 down to
+    max(s_p, 16 eps s_1), grid minimum of the negative curvature, fminbnd on
+    the neighbouring grid points; the least-squares residual enters when m > p."""
+    m = U.shape[0]
+    p = s.size
+    beta = U[:, :p].conj().T @ b
+    rho_ls2 = gcv_delta0(b, beta, m, p)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        xi = np.where(s > 0, beta / np.where(s > 0, s, 1.0), 0.0)
+    lam = gcv_grid(s, npoints)
+    g = np.array([lcfun(la, s, beta, xi, method, rho_ls2) for la in lam])
+    gi = int(np.nanargmin(g))
+    return fminbnd(lambda la: lcfun(la, s, beta, xi, method, rho_ls2), lam[min(gi + 1, npoints - 1)],
+                   lam[max(gi - 1, 0)])
+
+
+def quasiopt(U, s, b, method="t", npoints=200):
+    """Quasi-optimality lambda (quasioptG.m:17-41): Q = ||(1-f) f xi|| on the
+    grid from s_1 down to s_p, then fminbnd around the grid minimum."""
+    p = s.size
+    xi = (U[:, :p].conj().T @ b) / s
+    rpm = s[-1] if s[-1] > 0 else s[0] * 16 * EPS
+    ratio = (s[0] / rpm) ** (1.0 / (npoints - 1))
+    lam = ratio ** np.arange(npoints - 1, -1, -1) * rpm
+
+    def Q(la):
+        f = _filter(s, la, method)
+        return float(np.linalg.norm((1.0 - f) * f * xi))
+
+    q = np.array([Q(la) for la in lam])
+    qi = int(np.nanargmin(q))
+    return fminbnd(Q, lam[min(qi + 1, npoints - 1)], lam[max(qi - 1, 0)])
+
+
+def dsvd(U, s, V, b, lam):
+    """Damped SVD x = V (beta / (s + lambda)) (dsvdG.m:21-26)."""
+    if lam < 0:
+        raise ValueError("Illegal regularization parameter lambda")
+    p = s.size
+    beta = U[:, :p].conj().T @ b
+    return V[:, :p] @ (beta / (s + lam))
+
+
+def solve_regularized(H, b, method, npoints=200, lam_fixed=None):
+    """csvd, then the filter and lambda of the library's IA_METHOD_* names:
+    'tikhonov-lcurve', 'tikhonov-quasiopt', 'dsvd-fixed', 'dsvd-lcurve',
+    'dsvd-quasiopt'.  Returns (x, lambda, s)."""
+    U, s, V = csvd(H)
+    filt, sel = method.split("-")
+    m = "d" if filt == "dsvd" else "t"
+    if sel == "lcurve":
+        lam = l_curve(U, s, b, m, npoints)
+    elif sel == "quasiopt":
+        lam = quasiopt(U, s, b, m, npoints)
+    else:
+        lam = lam_fixed
+    x = dsvd(U, s, V, b, lam) if m == "d" else tikhonov(U, s, V, b, lam)
+    return x, lam, s

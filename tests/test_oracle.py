@@ -196,3 +196,35 @@ def test_design_gradient_matches_central_differences():
     E = np.eye(len(k))
     fl = np.array([(L(LL=ll + h * E[f]) - L(LL=ll - h * E[f])) / (2 * h) for f in range(len(k))])
     assert np.max(np.abs(fl - gl)) <= 1e-6 * np.max(np.abs(gl))
+
+
+def test_lambda_selectors_restatement():
+    """L-curve corner and quasi-optimality restatements: the fminbnd result
+    sits at the minimum of the objective on a dense grid of its bracket, the
+    corner is inside the grid, and the damped SVD solves its diagonal system."""
+    rng = np.random.default_rng(4)
+    mics = g.planar_array(8, 8, 0.03, 0.10)
+    src, _ = g.icosphere(1, 0.05)
+    k = 2 * np.pi * 1200 / 343.0
+    G = O.monopole_matrix(mics, src, k)
+    b = g.add_noise(rng, G @ g.complex_normal(rng, src.shape[1]), 25.0)
+    U, s, V = O.csvd(G)
+    beta = U.conj().T @ b
+    xi = beta / s
+    rho_ls2 = O.gcv_delta0(b, beta, G.shape[0], s.size)      # m > p: least-squares residual term
+    assert rho_ls2 > 0
+    for method in ("t", "d"):
+        lc = O.l_curve(U, s, b, method)
+        dense = np.geomspace(lc / 1.2, lc * 1.2, 2001)
+        vals = [O.lcfun(la, s, beta, xi, method, rho_ls2) for la in dense]
+        assert abs(dense[int(np.argmin(vals))] - lc) <= 2e-3 * lc + 1e-4
+        assert s[-1] <= lc <= s[0]
+        qo = O.quasiopt(U, s, b, method)
+        f = O._filter(s, qo, method)
+        # within the bracket the grid minimum gives (here the grid's top end, s_1)
+        dense = np.geomspace(max(qo / 1.2, s[-1]), min(qo * 1.2, s[0]), 2001)
+        qv = [np.linalg.norm((1 - O._filter(s, la, method)) * O._filter(s, la, method) * xi) for la in dense]
+        assert abs(dense[int(np.argmin(qv))] - qo) <= 2e-3 * qo + 1e-4
+        assert np.isfinite(f).all()
+    x = O.dsvd(U, s, V, b, 0.3)
+    assert relerr(V.conj().T @ x * (s + 0.3), U.conj().T @ b) < 1e-12
