@@ -9,6 +9,7 @@
  *
  *      ia_esm   <- esm()   CUDA/esm.cuh:112   (and esmgpu() CUDA/esm.cuh:38)
  *      ia_ibem  <- ibem()  CUDA/ibem.cuh:424  (and ibemgpu() CUDA/ibem.cuh:263)
+ *      ia_invr  <- invr()  CUDA/invr.cuh:457  (and invrgpu() CUDA/invr.cuh:291)
  *      ia_hels  <- hels()  CUDA/hels.cuh:222  (and helsgpu() CUDA/hels.cuh:185)
  *      ia_csvd  <- csvd()  CUDA/tsvd.cuh:10
  *      ia_tsvd  <- tsvd()  CUDA/tsvd.cuh:122
@@ -140,6 +141,16 @@ int ia_esm(int m, int l, const double *r_ms, const double *r_lh, ia_complex **m_
  * Replaces ibem() CUDA/ibem.cuh:424 (which reads IPF.txt/IPFs.txt from the cwd). */
 int ia_ibem(int m, int l, int n, const double *r_ms, const int *e_n, const double *r_lh, ia_complex **m_e,
             ia_complex **h, double k, int n_ch, const double *cp, const ia_rules *rules, const ia_config *cfg);
+
+/* BEM radiation modes at one wavenumber: q_e (m x n_am) the leading left
+ * singular vectors of the complex G Z (phase as ia_bem_modes_complex_batch),
+ * h (l x n_am) = (A_hs Z - B_hs) q_e, m_e (m x n_am) = Z q_e; 1 <= n_am <= m.
+ * Replaces invr() CUDA/invr.cuh:457 and invrgpu() CUDA/invr.cuh:263 (whose
+ * GPU version computes these products for any n_am; the CPU version only for
+ * n_am = m, invr.cuh:904,907).  rules as ia_ibem. */
+int ia_invr(int m, int l, int n, const double *r_ms, const int *e_n, const double *r_lh, ia_complex **m_e,
+            ia_complex **h, ia_complex **q_e, double k, int n_ch, const double *cp, int n_am, const ia_rules *rules,
+            const ia_config *cfg);
 
 /* HELS: Me (m x nt), He (l x nt), Qe (m x nt), nt = (n_sh+1)^2, column
  * i = n^2 + n + m.  Points in (az, el, r) structure-of-arrays.
@@ -302,6 +313,35 @@ int ia_sinc_resistance_batch(ia_context *ctx, int n, const double *d_x, int F, c
  * matrix, MATLAB/invrV.m:65-119). */
 int ia_radiation_modes_batch(ia_context *ctx, int n, int F, const double *d_R, int nmodes, const ia_config *cfg,
                              double *d_lambda, double *d_modes, int *d_info);
+
+/* BEM radiation modes of a closed surface, F wavenumbers; replaces invr()
+ * (CUDA/invr.cuh:457), specified by MATLAB/invrS.m:18-170.  Z = A \ B (the
+ * IBEM surface system; least squares when n_ch > 0 CHIEF points d_cp 3 x n_ch
+ * add rows, as invr.cuh:860 zgels and invrS.m:159), G the surface mass matrix,
+ * R = Re(G Z), U_r the nmodes leading left singular vectors of R (d_Ur
+ * F x (m x nmodes), real, each column's first component within 1e-6 of its
+ * largest magnitude positive; d_sr F x nmodes, descending), H_r =
+ * (A_hs Z - B_hs) U_r at the field points d_mics (d_Hr F x (l x nmodes)),
+ * P_r = Z U_r the modal surface pressures (d_Pr F x (m x nmodes), or NULL).
+ * The outputs have the sizes invrS.m gives for any n_am (invr.cuh:904,907 use
+ * n_am as the inner dimension, which is H U and Z U only for n_am = m).
+ * Singular vectors by subspace iteration on R R^T (cfg->mode_iters,
+ * mode_oversample; FP32 iterations with IA_PREC_MIXED, which also assembles
+ * in double-float). */
+int ia_bem_modes_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                       const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg, double *d_Ur,
+                       double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info);
+
+/* As ia_bem_modes_batch, with the modes of the complex G Z itself, as the
+ * C++ invr() takes them (CUDA/invr.cuh:868-889 zgesvd of G Z): d_Ur
+ * F x (m x nmodes) complex, each column's phase fixed so that its first
+ * component within 1e-6 of its largest magnitude is real and positive (the
+ * phase of a singular vector is arbitrary; zgesvd's is not reproduced).
+ * FP64 one-sided Jacobi SVD of the full G Z (cfg->svd_max_sweeps);
+ * IA_PREC_MIXED assembles in double-float. */
+int ia_bem_modes_complex_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                               const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg,
+                               ia_complex *d_Ur, double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info);
 
 /* Sound power W_f,r = 1/2 Re(v^H R_f v) of F x nrhs velocity fields
  * d_v F x (n x nrhs) (the reference's 1/2 Re(v^H p), CUDA/utils.cuh:265-280,

@@ -59,6 +59,7 @@ _SIGS = {
     "ia_read_msh": (_I, [C.c_char_p, _D, _D, _PP, _PP, _PP, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "ia_esm": (_I, [_I, _I, _P, _P, _PP, _PP, _D, _D, _P]),
     "ia_ibem": (_I, [_I, _I, _I, _P, _P, _P, _PP, _PP, _D, _I, _P, _P, _P]),
+    "ia_invr": (_I, [_I, _I, _I, _P, _P, _P, _PP, _PP, _PP, _D, _I, _P, _I, _P, _P]),
     "ia_hels": (_I, [_I, _I, _P, _P, _PP, _PP, _PP, _D, _I, _P]),
     "ia_csvd": (_I, [_I, _I, _P, _PP, _PP, _PP]),
     "ia_tsvd": (_I, [_I, _I, _I, _I, _P, _P, _P, _P, _PP]),
@@ -93,6 +94,8 @@ _SIGS = {
     "ia_sinc_resistance_batch": (_I, [_P, _I, _P, _I, _P, _D, _P, _P]),
     "ia_radiation_modes_batch": (_I, [_P, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ia_sound_power_batch": (_I, [_P, _I, _I, _P, _I, _P, _P]),
+    "ia_bem_modes_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "ia_bem_modes_complex_batch": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "ia_esm_design_batch": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 }
 

@@ -94,6 +94,28 @@ def ibem(r_ms, e_n, r_lh, k, n_ch=0, cp=None, rules=None, c=None, rho=None, cfg=
     return _take(me, m * m).reshape(m, m, order="F"), _take(h, l * m).reshape(l, m, order="F")
 
 
+def invr(r_ms, e_n, r_lh, k, n_am, n_ch=0, cp=None, rules=None, c=None, rho=None, cfg=None):
+    """(m_e = Z q_e m x n_am, h = H q_e l x n_am, q_e m x n_am) -- invr()
+    CUDA/invr.cuh:457; q_e the leading left singular vectors of G Z."""
+    L = _lib.lib()
+    r_ms, r_lh = _f64(r_ms).ravel(), _f64(r_lh).ravel()
+    e = np.ascontiguousarray(np.asarray(e_n, dtype=np.int32)).ravel()
+    m, l, n = r_ms.size // 3, r_lh.size // 3, e.size // 3
+    cpa = _f64(cp).ravel() if n_ch else np.zeros(3)
+    cfg = _cfg(cfg, c, rho)
+    keep = None
+    rp = None
+    if rules is not None:
+        rs, keep = rules_struct(*rules)
+        rp = C.byref(rs)
+    me, h, qe = _P(), _P(), _P()
+    check(L.ia_invr(m, l, n, r_ms.ctypes.data, e.ctypes.data, r_lh.ctypes.data, C.byref(me), C.byref(h),
+                    C.byref(qe), float(k), int(n_ch), cpa.ctypes.data, int(n_am), rp, C.byref(cfg)), "ia_invr")
+    del keep
+    return (_take(me, m * n_am).reshape(m, n_am, order="F"), _take(h, l * n_am).reshape(l, n_am, order="F"),
+            _take(qe, m * n_am).reshape(m, n_am, order="F"))
+
+
 def hels(r_ms_s, r_lh_s, k, n_sh, c=None, rho=None, cfg=None):
     """(Me m x nt, He l x nt, Qe m x nt) -- hels() CUDA/hels.cuh:222."""
     L = _lib.lib()
@@ -469,6 +491,32 @@ def radiation_modes_batch(ctx, R, nmodes, cfg=None):
     check(_lib.lib().ia_radiation_modes_batch(ctx.handle, n, F, _dptr(R, torch.float64), int(nmodes), C.byref(cfg),
                                               _dptr(lam), _dptr(modes), _dptr(info)), "ia_radiation_modes_batch")
     return lam, modes, info
+
+
+def bem_modes_batch(ctx, mesh, mics, k, nmodes, cfg=None, pressures=True, cp=None, complex_modes=False):
+    """BEM radiation modes of mesh at wavenumbers k (F,): (s (F, nmodes)
+    descending singular values, Ur (F, nmodes, m) left singular vectors -- mode
+    j of frequency f is Ur[f, j] --, Hr (F, nmodes, l) modal transfer columns
+    at mics (3, l), Pr (F, nmodes, m) modal surface pressures or None, info
+    (F,)).  Modes of the resistance Re(G Z) (real Ur, MATLAB invrS.m), or with
+    complex_modes of G Z itself (complex Ur, the C++ invr()).  cp (3, n_ch):
+    CHIEF points."""
+    import torch
+    cfg = cfg or default_config()
+    l, F, m = mics.shape[-1], k.numel(), mesh.m
+    n_ch = 0 if cp is None else cp.shape[-1]
+    dev = k.device
+    s = torch.empty((F, nmodes), dtype=torch.float64, device=dev)
+    Ur = torch.empty((F, nmodes, m), dtype=torch.complex128 if complex_modes else torch.float64, device=dev)
+    Hr = torch.empty((F, nmodes, l), dtype=torch.complex128, device=dev)
+    Pr = torch.empty((F, nmodes, m), dtype=torch.complex128, device=dev) if pressures else None
+    info = torch.zeros(F, dtype=torch.int32, device=dev)
+    fn = _lib.lib().ia_bem_modes_complex_batch if complex_modes else _lib.lib().ia_bem_modes_batch
+    check(fn(ctx.handle, mesh._h, l, _dptr(mics, torch.float64), n_ch, _dptr(cp, torch.float64) if n_ch else None, F,
+             _dptr(k, torch.float64), int(nmodes), C.byref(cfg), _dptr(Ur), _dptr(s), _dptr(Hr),
+             _dptr(Pr) if Pr is not None else None, _dptr(info)),
+          "ia_bem_modes_complex_batch" if complex_modes else "ia_bem_modes_batch")
+    return s, Ur, Hr, Pr, info
 
 
 def sound_power_batch(ctx, R, v):

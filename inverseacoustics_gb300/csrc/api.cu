@@ -449,6 +449,25 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
     up((void **)&M->d_qnrm, qnrm.data(), sizeof(double) * qnrm.size());
     up((void **)&M->d_qdat_f, qdat_f.data(), sizeof(float) * qdat_f.size());
     up((void **)&M->d_qnrm_f, qnrm_f.data(), sizeof(float) * qnrm_f.size());
+    // node-node pattern (nodes sharing an element, the node itself included),
+    // CSR with sorted columns: the sparsity of the surface mass matrix
+    {
+        std::vector<int> gptr(m + 1, 0), gidx;
+        std::vector<int> row;
+        for (int i = 0; i < m; ++i) {
+            row.clear();
+            row.push_back(i);
+            for (int el : node_elems[i])
+                for (int s2 = 0; s2 < 3; ++s2) row.push_back(elems[el + s2 * n]);
+            std::sort(row.begin(), row.end());
+            row.erase(std::unique(row.begin(), row.end()), row.end());
+            gidx.insert(gidx.end(), row.begin(), row.end());
+            gptr[i + 1] = (int)gidx.size();
+        }
+        M->gnnz = (int)gidx.size();
+        up((void **)&M->d_gptr, gptr.data(), sizeof(int) * gptr.size());
+        up((void **)&M->d_gidx, gidx.data(), sizeof(int) * gidx.size());
+    }
     if (e != cudaSuccess) {
         ia_mesh_destroy(M);
         return cuda_status(e);
@@ -466,6 +485,8 @@ int ia_mesh_destroy(ia_mesh *M)
     cudaFree(M->d_color_ptr);
     cudaFree(M->d_adj_ptr);
     cudaFree(M->d_adj);
+    cudaFree(M->d_gptr);
+    cudaFree(M->d_gidx);
     cudaFree(M->d_reg);
     cudaFree(M->d_sing);
     cudaFree(M->d_qdat);
@@ -773,6 +794,38 @@ int ia_esm_design_batch(ia_context *ctx, int l, int m, int F, int nrhs, const do
     return esm_design_batched(ctx, l, m, F, nrhs, d_mics, d_surface, d_retreat, d_k, d_loglam, (const double2 *)d_q,
                               (const double2 *)d_noise, d_err, d_grad_mics, d_grad_retreat, d_grad_loglam, d_info,
                               cur);
+}
+
+static int bem_modes_entry(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                           const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg, bool cplx,
+                           void *d_Ur, double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info)
+{
+    if (!ctx || !mesh || !cfg || l < 1 || n_ch < 0 || (n_ch > 0 && !d_cp) || F < 1 || nmodes < 1 ||
+        nmodes > mesh->m || !d_mics || !d_k || !d_Ur || !d_sr || !d_Hr || !d_info || cfg->mode_iters < 0 ||
+        cfg->mode_oversample < 0)
+        return IA_ERR_ARG;
+    int st = ws_reserve(ctx, bem_modes_ws_bytes(mesh, l, n_ch, F, nmodes, cfg, cplx));
+    if (!st) st = clear_info(ctx, d_info, F);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return bem_modes_batched(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, nmodes, cfg, cplx, d_Ur, d_sr,
+                             (double2 *)d_Hr, (double2 *)d_Pr, d_info, cur);
+}
+
+int ia_bem_modes_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                       const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg, double *d_Ur,
+                       double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info)
+{
+    return bem_modes_entry(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, nmodes, cfg, false, d_Ur, d_sr, d_Hr, d_Pr,
+                           d_info);
+}
+
+int ia_bem_modes_complex_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
+                               const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg,
+                               ia_complex *d_Ur, double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info)
+{
+    return bem_modes_entry(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, nmodes, cfg, true, d_Ur, d_sr, d_Hr, d_Pr,
+                           d_info);
 }
 
 int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,

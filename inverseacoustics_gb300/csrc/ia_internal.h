@@ -35,6 +35,8 @@ struct ia_mesh {
     double *d_qnrm;        // element normals [3][element]
     float *d_qdat_f;       // d_qdat as double-float (hi, lo) pairs
     float *d_qnrm_f;       // d_qnrm as double-float (hi, lo) pairs
+    int *d_gptr, *d_gidx;  // node-node pattern, CSR (m + 1, gnnz): nodes sharing an element
+    int gnnz;
 };
 
 namespace ia {
@@ -206,9 +208,17 @@ int hels_batched(ia_context *ctx, int npts, const double *pts, int order, int F,
 // R (F x n x n FP64) and optionally an FP32 copy R32
 int sinc_resistance_batched(ia_context *ctx, int n, const double *x, int F, const double *k, double area, double c,
                             double rho, double *R, float *R32);
-size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg);
+// leading eigenpairs of the symmetric R, or (gram) of R R^T for a general R:
+// left singular vectors, lambda = squared singular values
+size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg, bool gram = false);
 int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int nm, const ia_config *cfg,
-                            double *lambda, double *modes, int *info, WsCursor &cur);
+                            double *lambda, double *modes, int *info, WsCursor &cur, bool gram = false);
+// BEM radiation modes (bem_modes.cu)
+// (cplx: Ur is double2 m x nm per frequency, modes of G Z; else double, of Re(G Z))
+size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, const ia_config *cfg, bool cplx);
+int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp,
+                      int F, const double *k, int nm, const ia_config *cfg, bool cplx, void *Ur, double *sr,
+                      double2 *Hr, double2 *Pr, int *info, WsCursor &cur);
 size_t sound_power_ws_bytes(int n, int F);
 
 // ---- differentiable ESM design (adjoint.cu); gm == nullptr: forward only

@@ -501,19 +501,22 @@ __global__ void mode_sign_kernel(int n, int nm, double *__restrict__ X, const do
     if (threadIdx.x == 0 && info && bad) info[f] |= IA_INFO_NONFINITE;
 }
 
-size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg)
+size_t radiation_modes_ws_bytes(int n, int F, int nm, const ia_config *cfg, bool gram)
 {
     const size_t b = (size_t)min(n, nm + max(0, cfg->mode_oversample));
     const size_t nb = (size_t)n * b * F, bb = b * b * F;
-    size_t s = 3 * ws_round(8 * nb) + ws_round(8 * b * F) + ws_round(8 * bb) + 4 * ws_round(16 * bb) +
+    size_t s = 4 * ws_round(8 * nb) + ws_round(8 * b * F) + ws_round(8 * bb) + 4 * ws_round(16 * bb) +
                ws_round(8 * b * F) + ws_round(8 * b * (size_t)nm * F);
     if (cfg->precision == IA_PREC_MIXED)
-        s += ws_round(4 * (size_t)n * n * F) + 2 * ws_round(4 * nb) + ws_round(4 * b * F);
+        s += ws_round(4 * (size_t)n * n * F) + 3 * ws_round(4 * nb) + ws_round(4 * b * F);
+    (void)gram;
     return s + 4096;
 }
 
+// gram: the operator is R R^T (R general, n x n): its eigenpairs are the left
+// singular vectors and the squared singular values of R
 int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int nm, const ia_config *cfg,
-                            double *lambda, double *modes, int *info, WsCursor &cur)
+                            double *lambda, double *modes, int *info, WsCursor &cur, bool gram)
 {
     const int b = min(n, nm + max(0, cfg->mode_oversample));
     const bool mixed = cfg->precision == IA_PREC_MIXED;
@@ -521,6 +524,13 @@ int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int 
     double *Q = cur.take<double>(nb * F);
     double *Y = cur.take<double>(nb * F);
     double *Y2 = cur.take<double>(nb * F);
+    double *Tg = cur.take<double>(nb * F);
+    // Yo = op Qi at FP64 accuracy, op = R or R R^T
+    auto apply64 = [&](const double *Qi, double *Yo) -> int {
+        if (!gram) return prod64(ctx, mixed, OP_N, n, b, n, R, n, nn, Qi, n, nb, Yo, n, nb, F);
+        int s2 = prod64(ctx, mixed, OP_T, n, b, n, R, n, nn, Qi, n, nb, Tg, n, nb, F);
+        return s2 ? s2 : prod64(ctx, mixed, OP_N, n, b, n, R, n, nn, Tg, n, nb, Yo, n, nb, F);
+    };
     double *tau = cur.take<double>((size_t)b * F);
     double *B = cur.take<double>(bb * F);
     double2 *Bc = cur.take<double2>(bb * F);
@@ -537,11 +547,18 @@ int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int 
         float *Q32 = cur.take<float>(nb * F);
         float *Y32 = cur.take<float>(nb * F);
         float *tau32 = cur.take<float>((size_t)b * F);
+        float *T32 = cur.take<float>(nb * F);
         if ((st = convert(ctx, (size_t)nn * F, R, R32))) return st;
         start_block_kernel<float><<<blocks, 256, 0, ctx->stream>>>(n, b, Q32, F);
         IA_LAUNCH_CHECK(ctx);
         for (int t = 0; t < cfg->mode_iters; ++t) {
-            if ((st = rgemm_batched<float>(ctx, OP_N, n, b, n, 1.f, R32, n, nn, Q32, n, nb, 0.f, Y32, n, nb, F)))
+            const float *src = Q32;
+            if (gram) {
+                if ((st = rgemm_batched<float>(ctx, OP_T, n, b, n, 1.f, R32, n, nn, Q32, n, nb, 0.f, T32, n, nb, F)))
+                    return st;
+                src = T32;
+            }
+            if ((st = rgemm_batched<float>(ctx, OP_N, n, b, n, 1.f, R32, n, nn, src, n, nb, 0.f, Y32, n, nb, F)))
                 return st;
             if ((st = orthonormalise<float>(ctx, n, b, Y32, tau32, Q32, F))) return st;
         }
@@ -552,11 +569,11 @@ int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int 
         IA_LAUNCH_CHECK(ctx);
     }
     for (int t = 0; t < steps64; ++t) {
-        if ((st = prod64(ctx, mixed, OP_N, n, b, n, R, n, nn, Q, n, nb, Y, n, nb, F))) return st;
+        if ((st = apply64(Q, Y))) return st;
         if ((st = orthonormalise<double>(ctx, n, b, Y, tau, Q, F))) return st;
     }
-    // Rayleigh-Ritz: B = Q^T R Q, eigenpairs of B, modes = Q W
-    if ((st = prod64(ctx, mixed, OP_N, n, b, n, R, n, nn, Q, n, nb, Y2, n, nb, F))) return st;
+    // Rayleigh-Ritz: B = Q^T op Q, eigenpairs of B, modes = Q W
+    if ((st = apply64(Q, Y2))) return st;
     if ((st = prod64(ctx, mixed, OP_T, b, b, n, Q, n, nb, Y2, n, nb, B, b, bb, F))) return st;
     sym_complex_kernel<<<blocks, 256, 0, ctx->stream>>>(b, B, Bc, F);
     IA_LAUNCH_CHECK(ctx);

@@ -243,6 +243,64 @@ def sound_power_R(R, v):
 
 
 # ---------------------------------------------------------------------------
+# BEM radiation modes  (MATLAB/invrS.m:18-170; CUDA/invr.cuh:457-909)
+# ---------------------------------------------------------------------------
+def mass_matrix(nodes, elems, regular):
+    """Surface mass matrix G (m x m) accumulated element by element with the
+    regular rule: G[e_a, e_b] += |n_e| sum_q w_q N_a(q) N_b(q), N = (x1, x2,
+    1 - x1 - x2) on the element's vertices in order, |n_e| = |(v0 - v2) x
+    (v1 - v2)| (MATLAB/invrS.m:54-65; CUDA/invr.cuh:590-624)."""
+    P = _soa(nodes)
+    E = np.asarray(elems, dtype=np.int64)
+    rule = np.asarray(regular, dtype=np.float64)
+    N = np.stack([rule[:, 0], rule[:, 1], 1.0 - rule[:, 0] - rule[:, 1]])
+    Me = (N * rule[:, 2]) @ N.T
+    v = P[:, E]                                    # (3 coords, 3 slots, n)
+    an = np.linalg.norm(np.cross((v[:, 0] - v[:, 2]).T, (v[:, 1] - v[:, 2]).T), axis=1)
+    m = P.shape[1]
+    G = np.zeros((m, m))
+    for a in range(3):
+        for b in range(3):
+            np.add.at(G, (E[a], E[b]), an * Me[a, b])
+    return G
+
+
+def bem_modes(nodes, elems, mics, k, regular, singular, c, rho, nmodes):
+    """invrS.m:159-169: Z = A \\ B, R = real(G Z), [U, ~] = svd(R),
+    U_r = U(:, 1:n_ma), H_r = (A_hs Z - B_hs) U_r, and the modal surface
+    pressures Z U_r.  Returns (s_r, U_r, H_r, P_r, Z, G); each column of U_r
+    has its first component within 1e-6 of the largest magnitude positive,
+    the sign convention of the device path."""
+    Z, H = ibem(nodes, elems, mics, k, regular, singular, c, rho)
+    G = mass_matrix(nodes, elems, regular)
+    R = (G @ Z).real
+    U, s, _ = np.linalg.svd(R)
+    Ur = U[:, :nmodes].copy()
+    for j in range(nmodes):
+        a = np.abs(Ur[:, j])
+        i = int(np.argmax(a >= a.max() * (1.0 - 1e-6)))
+        if Ur[i, j] < 0:
+            Ur[:, j] = -Ur[:, j]
+    return s[:nmodes].copy(), Ur, H @ Ur, Z @ Ur, Z, G
+
+
+def bem_modes_complex(nodes, elems, mics, k, regular, singular, c, rho, nmodes, chief=None):
+    """The C++ invr()/invrgpu() form (CUDA/invr.cuh:392-440, 860-907): U from
+    the SVD of the complex G Z, h = (A_hs Z - B_hs) U(:, 1:n), m_e = Z U(:, 1:n).
+    Each column's phase is fixed so that its first component within 1e-6 of
+    the largest magnitude is real and positive.  Returns (s, U, h, m_e, Z, G)."""
+    Z, H = ibem(nodes, elems, mics, k, regular, singular, c, rho, chief)
+    G = mass_matrix(nodes, elems, regular)
+    U, s, _ = np.linalg.svd(G @ Z)
+    U = U[:, :nmodes].copy()
+    for j in range(nmodes):
+        a = np.abs(U[:, j])
+        i = int(np.argmax(a >= a.max() * (1.0 - 1e-6)))
+        U[:, j] *= np.conj(U[i, j]) / a[i]
+    return s[:nmodes].copy(), U, H @ U, Z @ U, Z, G
+
+
+# ---------------------------------------------------------------------------
 # products and sound power (CUDA/utils.cuh:199-289)
 # ---------------------------------------------------------------------------
 def to_pressure(Me, x):

@@ -123,6 +123,31 @@ def ibem(nodes, elems, mics, k, regular, singular, chief=None):
     return Z, H
 
 
+def invr(nodes, elems, mics, k, regular, singular, n_am):
+    """Reference invr() with n_ch = 0: returns (q_e m x n_am, the left singular
+    vectors of G Z; h l x n_am; m_e m x n_am).  Its output products take n_am
+    as the inner dimension (CUDA/invr.cuh:904,907), so only n_am = m gives
+    H U and Z U."""
+    r_ms, r_lh = _soa(nodes), _soa(mics)
+    e_n = np.ascontiguousarray(np.asarray(elems, dtype=np.int32)).ravel()
+    m, l, n = r_ms.size // 3, r_lh.size // 3, e_n.size // 3
+    me, h, qe = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    cp = np.zeros(3)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        write_rules(d, regular, singular)
+        os.chdir(d)
+        try:
+            lib().invr(m, l, n, r_ms.ctypes.data, e_n.ctypes.data, r_lh.ctypes.data, C.byref(me), C.byref(h),
+                       C.byref(qe), float(k), 0, cp.ctypes.data, int(n_am))
+        finally:
+            os.chdir(cwd)
+    Q = _take(qe, m * n_am).reshape(m, n_am, order="F")
+    Hh = _take(h, l * n_am).reshape(l, n_am, order="F")
+    Me = _take(me, m * n_am).reshape(m, n_am, order="F")
+    return Q, Hh, Me
+
+
 def sphere(nodes, mics, k, u, a):
     r_ms, r_lh = _soa(nodes), _soa(mics)
     m, l = r_ms.size // 3, r_lh.size // 3

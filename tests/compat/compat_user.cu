@@ -1,19 +1,21 @@
 // A "user program" written against the reference's call surface: it includes
-// the drop-in headers of include/compat/ and calls esm, ibem, hels, csvd,
-// tsvd, to_pressure and sound_power exactly as reference code would.  The
+// the drop-in headers of include/compat/ and calls esm, ibem, invr, hels,
+// csvd, tsvd, to_pressure and sound_power exactly as reference code would.  The
 // test suite compiles it against libia.so, runs it on the GPU and compares
 // what it writes with the oracle.
 //
 // usage: compat_user <in.bin> <out.bin>
 //   in.bin : int32 m, l, n; double k, r_i; double r_ms[3m], r_lh[3l]; int32 e_n[3n]
 //   out.bin: esm Me (m*m), He (l*m); ibem Z (m*m), H (l*m); hels Me, He, Qe (order 3);
-//            csvd s (min(l,m)); tsvd x (m, k = 5); to_pressure p (l); sound_power w (1 double)
+//            csvd s (min(l,m)); tsvd x (m, k = 5); to_pressure p (l); sound_power w (1 double);
+//            invr q_e (m*9), h (l*9), m_e (m*9)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 #include "esm.cuh"
 #include "hels.cuh"
 #include "ibem.cuh"
+#include "invr.cuh"
 #include "tsvd.cuh"
 #include "utils.cuh"
 
@@ -73,6 +75,14 @@ int main(int argc, char **argv)
         put(fo, p, (size_t)l);
         sound_power(l, p, b.data(), &w, 0.3);
         put(fo, &w, 1);
+        cuDoubleComplex *rq, *rh, *rm;
+        invr(m, l, n, r_ms.data(), e_n.data(), r_lh.data(), &rm, &rh, &rq, k, 0, nullptr, 9);
+        put(fo, rq, (size_t)m * 9);
+        put(fo, rh, (size_t)l * 9);
+        put(fo, rm, (size_t)m * 9);
+        std::free(rq);
+        std::free(rh);
+        std::free(rm);
         for (void *q : {(void *)z, (void *)h, (void *)sph_s, (void *)sph_h, (void *)hm, (void *)hh, (void *)hq,
                         (void *)u, (void *)s, (void *)v, (void *)x, (void *)p})
             std::free(q);

@@ -13,6 +13,8 @@ cartesian_2_spherical(), built with C_AIR=343, RHO_AIR=1.21):
   mics (3, 30), chief (3, 2), ks (2,)
   ibem_Z_{0,1}, ibem_H_{0,1}        ibem() at ks[0], ks[1], no CHIEF points
   ibem_chief_Z, ibem_chief_H        ibem() at ks[0] with the 2 CHIEF points
+  invr_q, invr_h, invr_m            invr() at ks[1], n_am = m: left singular
+      vectors of G Z, (A_hs Z - B_hs) q, Z q
   esm_src (3, 42), esm_fld (3, 42), esm_k, esm_ri, esm_Me, esm_He   esm(), l == m
   kat_ps, kat_ph, kat_u, kat_a     sphere() analytic pressures at mesh nodes / mics
   sph_in (3, 12), sph_out (3, 12)  cartesian_2_spherical()
@@ -53,6 +55,10 @@ def main():
         out[f"ibem_Z_{i}"], out[f"ibem_H_{i}"] = Z, H
     Z, H = ref.ibem(nodes, elems, mics, ks[0], reg, sing, chief)
     out["ibem_chief_Z"], out["ibem_chief_H"] = Z, H
+    # invr() with n_am = m, the one size at which its output products are H U
+    # and Z U
+    q_e, h_r, m_e = ref.invr(nodes, elems, mics, ks[1], reg, sing, nodes.shape[1])
+    out.update(invr_q=q_e, invr_h=h_r, invr_m=m_e)
     src = nodes.copy()
     fld = nodes * 1.8
     esm_k = 2 * np.pi * 800.0 / c

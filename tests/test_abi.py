@@ -63,3 +63,10 @@ def test_bad_arguments_rejected_before_device_work():
     with pytest.raises(_lib.IAError) as e:
         api.esm(bad, np.ones((3, 4)), 1.0, 0.5)
     assert e.value.code == 6
+    # invr: n_am outside [1, m]
+    from inverseacoustics_gb300 import geometry as g
+    nodes, elems = g.icosphere(0, 0.1)
+    for n_am in (0, nodes.shape[1] + 1):
+        with pytest.raises(_lib.IAError) as e:
+            api.invr(nodes, elems, np.ones((3, 2)), 1.0, n_am)
+        assert e.value.code == 1

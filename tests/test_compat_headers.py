@@ -84,3 +84,12 @@ def test_compat_program_matches_oracle(tmp_path, cuda):
     assert relerr(pr, H @ x) < 1e-12
     w = take(1, np.float64)[0]
     assert abs(w - O.sound_power(H @ x, b, 0.3)) < 1e-10 * abs(w)
+    # invr, n_am = 9: the sphere's singular values of G Z come in multiplets
+    # (1, 3, 5, ...), so the 9 leading vectors are compared as a subspace
+    rq = take(m * 9).reshape(m, 9, order="F")
+    rh = take(l * 9).reshape(l, 9, order="F")
+    rm = take(m * 9).reshape(m, 9, order="F")
+    _, Uo, _, _, Zr, Gr = O.bem_modes_complex(nodes, elems, mics, k, reg, sing, c, rho, 9)
+    assert np.max(np.abs(rq.conj().T @ rq - np.eye(9))) < 1e-12
+    assert np.linalg.norm(rq @ rq.conj().T - Uo @ Uo.conj().T) < 1e-9
+    assert relerr(rh, Hio @ rq) < 1e-10 and relerr(rm, Zo @ rq) < 1e-10

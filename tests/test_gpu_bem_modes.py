@@ -1,0 +1,179 @@
+"""GPU suite: BEM radiation modes (ia_bem_modes_batch, ia_bem_modes_complex_batch,
+ia_invr) against the oracle's restatement of MATLAB/invrS.m and the C++
+invr() (CUDA/invr.cuh:457-909), and against the reference invr()'s own
+outputs (golden fixture).
+
+Geometry: an icosphere (162 nodes) scaled to an ellipsoid (0.1, 0.08, 0.06 m)
+so that few singular values are degenerate, 24 field points at 0.3 m.
+
+Bounds.  Real variant (singular vectors of R = Re(G Z) as eigenvectors of
+R R^T): s^2 within 1e-12 s_1^2 (FP64) / 1e-10 s_1^2 (mixed); vectors of modes
+with s_j > 1e-3 s_1 and a relative gap in s^2 above 1e-3, 1e-8 (FP64) / 1e-6
+(mixed), up to sign, and the device sign convention exactly; residual
+||R R^T U - U s^2|| within 1e-11 s_1^2.  Complex variant (FP64 Jacobi SVD of
+G Z): s within 1e-11 s_1; vectors with a relative gap above 1e-4 within 1e-9
+after the phase convention.  Both: H_r = H U and P_r = Z U with the oracle's
+H and Z and the device U, 1e-11 relative (FP64) / 1e-8 (mixed)."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from inverseacoustics_gb300 import geometry as g
+from inverseacoustics_gb300 import quadrature as Q
+from oracle import ia_oracle as O
+
+pytestmark = pytest.mark.gpu
+C, RHO = 343.0, 1.21
+
+
+def T(a, dev):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), device=dev)
+
+
+@pytest.fixture(scope="module")
+def ellipsoid():
+    nodes, elems = g.icosphere(2, 1.0)
+    nodes = np.ascontiguousarray(nodes * np.array([[0.1], [0.08], [0.06]]))
+    mics = g.hemisphere_array(np.random.default_rng(7), 24, 0.3)
+    ks = 2 * np.pi * np.array([120.0, 700.0, 1600.0]) / C
+    return nodes, elems, mics, ks
+
+
+def _run(ctx, cuda, ellipsoid, nm, precision, complex_modes, cp=None):
+    from inverseacoustics_gb300 import api
+    import torch
+    nodes, elems, mics, ks = ellipsoid
+    mesh = api.Mesh(ctx, nodes, elems)
+    cfg = api.default_config(precision=precision)
+    out = api.bem_modes_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), nm, cfg, cp=None if cp is None else T(cp, cuda),
+                              complex_modes=complex_modes)
+    torch.cuda.synchronize()
+    s, U, Hr, Pr, info = (None if a is None else a.cpu().numpy() for a in out)
+    mesh.close()
+    return s, U, Hr, Pr, info
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_bem_modes_real_match_oracle(cuda, ctx, ellipsoid, precision):
+    nodes, elems, mics, ks = ellipsoid
+    nm = 12
+    s, U, Hr, Pr, info = _run(ctx, cuda, ellipsoid, nm, precision, False)
+    assert int(np.abs(info).sum()) == 0
+    reg, sing = Q.builtin()
+    s2_tol, vec_tol, prod_tol = (1e-12, 1e-8, 1e-11) if precision == 0 else (1e-10, 1e-6, 1e-8)
+    checked = 0
+    for f, k in enumerate(ks):
+        so, Uo, _, _, Zo, Go = O.bem_modes(nodes, elems, mics, k, reg, sing, C, RHO, nm + 1)
+        _, Ho = O.ibem(nodes, elems, mics, k, reg, sing, C, RHO)
+        X = U[f].T                                          # m x nm
+        s1 = so[0]
+        assert np.max(np.abs(s[f] ** 2 - so[:nm] ** 2)) <= s2_tol * s1 ** 2
+        assert np.all(np.diff(s[f]) <= 0)
+        assert np.max(np.abs(X.T @ X - np.eye(nm))) < 1e-12
+        R = (Go @ Zo).real
+        assert np.linalg.norm(R @ (R.T @ X) - X * s[f] ** 2) <= 1e-11 * s1 ** 2
+        for j in range(nm):
+            if so[j] < 1e-3 * s1:
+                continue
+            gap = min(so[j - 1] ** 2 - so[j] ** 2 if j > 0 else np.inf, so[j] ** 2 - so[j + 1] ** 2) / s1 ** 2
+            if gap < 1e-3:
+                continue
+            assert np.linalg.norm(X[:, j] - Uo[:, j]) <= vec_tol, (f, j)
+            checked += 1
+        for j in range(nm):
+            a = np.abs(X[:, j])
+            assert X[int(np.argmax(a >= a.max() * (1 - 1e-6))), j] > 0
+        assert relerr(Hr[f].T, Ho @ X) < prod_tol
+        assert relerr(Pr[f].T, Zo @ X) < prod_tol
+    assert checked >= 12
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_bem_modes_complex_match_oracle(cuda, ctx, ellipsoid, precision):
+    nodes, elems, mics, ks = ellipsoid
+    nm = 10
+    s, U, Hr, Pr, info = _run(ctx, cuda, ellipsoid, nm, precision, True)
+    assert int(np.abs(info).sum()) == 0
+    reg, sing = Q.builtin()
+    s_tol, vec_tol, prod_tol = (1e-11, 1e-9, 1e-11) if precision == 0 else (1e-9, 1e-7, 1e-8)
+    checked = 0
+    for f, k in enumerate(ks):
+        so, Uo, _, _, Zo, _ = O.bem_modes_complex(nodes, elems, mics, k, reg, sing, C, RHO, nm + 1)
+        _, Ho = O.ibem(nodes, elems, mics, k, reg, sing, C, RHO)
+        X = U[f].T
+        assert np.max(np.abs(s[f] - so[:nm])) <= s_tol * so[0]
+        assert np.max(np.abs(X.conj().T @ X - np.eye(nm))) < 1e-12
+        for j in range(nm):
+            gap = min(so[j - 1] - so[j] if j > 0 else np.inf, so[j] - so[j + 1]) / so[0]
+            if gap < 1e-4:
+                continue
+            assert np.linalg.norm(X[:, j] - Uo[:, j]) <= vec_tol, (f, j)
+            checked += 1
+        assert relerr(Hr[f].T, Ho @ X) < prod_tol
+        assert relerr(Pr[f].T, Zo @ X) < prod_tol
+    assert checked >= 20
+
+
+def test_bem_modes_chief_least_squares(cuda, ctx, ellipsoid):
+    """Two CHIEF points inside the surface: Z by least squares (invr.cuh:860
+    zgels, invrS.m:159 backslash)."""
+    nodes, elems, mics, ks = ellipsoid
+    cp = np.array([[0.01, 0.02, -0.01], [-0.03, 0.0, 0.015]]).T.copy()
+    nm = 8
+    s, U, Hr, Pr, info = _run(ctx, cuda, ellipsoid, nm, 0, True, cp=cp)
+    assert int(np.abs(info).sum()) == 0
+    reg, sing = Q.builtin()
+    for f, k in enumerate(ks):
+        so, Uo, _, _, Zo, _ = O.bem_modes_complex(nodes, elems, mics, k, reg, sing, C, RHO, nm, chief=cp)
+        _, Ho = O.ibem(nodes, elems, mics, k, reg, sing, C, RHO, cp)
+        X = U[f].T
+        assert np.max(np.abs(s[f] - so)) <= 1e-11 * so[0]
+        assert np.linalg.norm(X @ X.conj().T - Uo @ Uo.conj().T) < 1e-8
+        assert relerr(Hr[f].T, Ho @ X) < 1e-11 and relerr(Pr[f].T, Zo @ X) < 1e-11
+
+
+def test_bem_modes_batch_is_per_frequency(cuda, ctx, ellipsoid):
+    """A frequency's modes do not depend on the rest of the batch: bitwise equal
+    alone and inside a batch."""
+    nodes, elems, mics, ks = ellipsoid
+    full = _run(ctx, cuda, ellipsoid, 6, 0, False)
+    one = _run(ctx, cuda, (nodes, elems, mics, ks[1:2]), 6, 0, False)
+    for a, b in zip(full[:4], one[:4]):
+        assert np.array_equal(a[1], b[0])
+
+
+def _clusters(s, rel=1e-6):
+    out, start = [], 0
+    for j in range(1, len(s) + 1):
+        if j == len(s) or s[j - 1] - s[j] > rel * s[0]:
+            out.append((start, j))
+            start = j
+    return out
+
+
+def test_invr_matches_reference_golden(cuda, golden):
+    """ia_invr with n_am = m against the reference invr() itself: the sphere's
+    singular values of G Z come in multiplets, so q is compared through the
+    projector onto each cluster; h q^H and m_e q^H (= H and Z) directly."""
+    from inverseacoustics_gb300 import api
+    nodes, elems, mics, k = golden["mesh_nodes"], golden["mesh_elems"], golden["mics"], golden["ks"][1]
+    rules = (golden["rule_regular"], golden["rule_singular"])
+    c, rho = float(golden["c"]), float(golden["rho"])
+    m = nodes.shape[1]
+    me, h, q = api.invr(nodes, elems, mics, k, m, rules=rules, c=c, rho=rho)
+    Qr = golden["invr_q"]
+    assert np.max(np.abs(q.conj().T @ q - np.eye(m))) < 1e-12
+    assert relerr(me @ q.conj().T, golden["invr_m"] @ Qr.conj().T) < 1e-10
+    assert relerr(h @ q.conj().T, golden["invr_h"] @ Qr.conj().T) < 1e-10
+    so = O.bem_modes_complex(nodes, elems, mics, k, *rules, c, rho, m)[0]
+    for a, b in _clusters(so):
+        if so[a] < 1e-8 * so[0]:
+            break
+        P = q[:, a:b] @ q[:, a:b].conj().T
+        Pr = Qr[:, a:b] @ Qr[:, a:b].conj().T
+        assert np.linalg.norm(P - Pr) < 1e-8, (a, b)
+    # n_am < m: the leading columns of the same modes
+    me8, h8, q8 = api.invr(nodes, elems, mics, k, 9, rules=rules, c=c, rho=rho)
+    assert np.array_equal(q8, q[:, :9])
+    assert relerr(h8, h[:, :9]) < 1e-14 and relerr(me8, me[:, :9]) < 1e-14

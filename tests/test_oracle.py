@@ -42,6 +42,60 @@ def test_oracle_transfer_equals_ibem_H(golden):
     assert relerr(H, golden["ibem_H_1"]) < 1e-12
 
 
+def _invr_golden_problem(golden):
+    return (golden["mesh_nodes"], golden["mesh_elems"], golden["mics"], golden["ks"][1], golden["rule_regular"],
+            golden["rule_singular"], float(golden["c"]), float(golden["rho"]))
+
+
+def test_oracle_mass_matrix_properties(golden):
+    """G symmetric, sparse on the node-node pattern, and its entries sum to
+    sum_e |n_e| sum_q w_q (the polyhedral area when the weights sum to 1/2)."""
+    nodes, elems, reg = golden["mesh_nodes"], golden["mesh_elems"], golden["rule_regular"]
+    G = O.mass_matrix(nodes, elems, reg)
+    assert np.max(np.abs(G - G.T)) <= 1e-15 * np.max(G)
+    v = nodes[:, elems]
+    an = np.linalg.norm(np.cross((v[:, 0] - v[:, 2]).T, (v[:, 1] - v[:, 2]).T), axis=1)
+    assert abs(G.sum() - an.sum() * reg[:, 2].sum()) < 1e-14 * G.sum()
+    pattern = np.zeros_like(G, dtype=bool)
+    for a in range(3):
+        for b in range(3):
+            pattern[elems[a], elems[b]] = True
+    assert np.all(G[~pattern] == 0) and np.all(G[pattern] > 0)
+
+
+def test_oracle_bem_modes_pinned_to_reference_invr(golden):
+    """The reference invr() (n_am = m) returns q = U, h = H U and m_e = Z U
+    with U the left singular vectors of G Z: Z and H recovered from them match
+    the oracle's, and U diagonalises the oracle's (G Z)(G Z)^H with its
+    singular values -- which pins the oracle's mass matrix G."""
+    prob = _invr_golden_problem(golden)
+    Q = golden["invr_q"]
+    m = Q.shape[0]
+    assert np.max(np.abs(Q.conj().T @ Q - np.eye(m))) < 1e-13
+    s, U, h, me, Z, G = O.bem_modes_complex(*prob, m)
+    assert relerr(Z, golden["invr_m"] @ Q.conj().T) < 1e-13
+    assert relerr(h @ U.conj().T, golden["invr_h"] @ Q.conj().T) < 1e-13
+    M = G @ Z
+    D = Q.conj().T @ M @ M.conj().T @ Q
+    assert np.max(np.abs(D - np.diag(np.diag(D)))) < 1e-13 * np.abs(D).max()
+    assert np.max(np.abs(np.sqrt(np.diag(D).real) - s)) < 1e-13 * s[0]
+
+
+def test_oracle_bem_modes_real_variant(golden):
+    """invrS.m: U_r are the left singular vectors of Re(G Z); H_r = H U_r and
+    P_r = Z U_r; sign convention of the device path."""
+    prob = _invr_golden_problem(golden)
+    s, Ur, Hr, Pr, Z, G = O.bem_modes(*prob, 12)
+    R = (G @ Z).real
+    assert np.max(np.abs(Ur.T @ Ur - np.eye(12))) < 1e-13
+    assert np.linalg.norm(R @ R.T @ Ur - Ur * s**2) < 1e-12 * s[0] ** 2
+    Zo, Ho = O.ibem(*prob)
+    assert relerr(Hr, Ho @ Ur) < 1e-14 and relerr(Pr, Zo @ Ur) < 1e-14
+    for j in range(12):
+        a = np.abs(Ur[:, j])
+        assert Ur[int(np.argmax(a >= a.max() * (1 - 1e-6))), j] > 0
+
+
 def test_oracle_esm_matches_reference(golden):
     Me, He = O.esm(golden["esm_src"], golden["esm_fld"], float(golden["esm_k"]), float(golden["esm_ri"]),
                    float(golden["c"]), float(golden["rho"]))
