@@ -110,7 +110,22 @@ typedef struct {
     const double *singular;  /* 9*nqs  : page0, page1, page2 */
 } ia_rules;
 
+/* ADMM sparse / regularised inversion (MATLAB/ADMMG.m:1-90; its arguments
+ * rho, gamma, epsilon, Nm, nor and, for nor = 3, p and N). */
+enum { IA_ADMM_L1 = 1, IA_ADMM_L2 = 2, IA_ADMM_LP = 3 };
+typedef struct {
+    int norm;         /* IA_ADMM_L1 (soft threshold), IA_ADMM_L2, IA_ADMM_LP (generalised soft threshold) */
+    int max_iters;    /* Nm: iterations per continuation stage (L1, Lp) or in all (L2) */
+    double rho;       /* augmented-Lagrangian weight, > 0 */
+    double gamma;     /* dual step factor */
+    double epsilon;   /* stop when ||c - c_old||, ||c - x|| and ||u - u_old|| are all <= epsilon */
+    double p;         /* Lp exponent, 0 < p <= 1 (IA_ADMM_LP) */
+    int gst_iters;    /* N: fixed-point steps of the generalised soft threshold (IA_ADMM_LP) */
+} ia_admm_config;
+
 void ia_config_default(ia_config *cfg);
+/* norm L1, max_iters 200, rho 1, gamma 1, epsilon 1e-6, p 0.5, gst_iters 5 */
+void ia_admm_config_default(ia_admm_config *cfg);
 /* sizeof(ia_config), for bindings that mirror the struct */
 int ia_config_size(void);
 const char *ia_status_string(int status);
@@ -342,6 +357,18 @@ int ia_bem_modes_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double
 int ia_bem_modes_complex_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
                                const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg,
                                ia_complex *d_Ur, double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info);
+
+/* ADMM inversion of F independent systems H_f c = p_f, each with nrhs
+ * right-hand sides: d_H F x (l x m), d_p F x (l x nrhs), d_lambda0 F x nrhs
+ * (lambda_0 of each system), d_x0 F x (m x nrhs) the starting x or NULL for
+ * A \ b (least squares when m <= l; the minimum-norm solution when m > l,
+ * where MATLAB's backslash gives a pivoting-dependent basic solution).
+ * Returns d_c F x (m x nrhs) (ADMMG.m's output c), d_iters F x nrhs (c-updates
+ * run, or NULL) and d_info (IA_INFO_NOCONV: no stage met epsilon).  FP64.
+ * Replaces MATLAB/ADMMG.m:1-90 (function ADMM). */
+int ia_admm_batch(ia_context *ctx, int l, int m, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_p,
+                  const double *d_lambda0, const ia_admm_config *acfg, const ia_complex *d_x0, ia_complex *d_c,
+                  int *d_iters, int *d_info);
 
 /* Sound power W_f,r = 1/2 Re(v^H R_f v) of F x nrhs velocity fields
  * d_v F x (n x nrhs) (the reference's 1/2 Re(v^H p), CUDA/utils.cuh:265-280,

@@ -38,6 +38,14 @@ class Config(C.Structure):
                 ("mode_oversample", C.c_int)]
 
 
+IA_ADMM_L1, IA_ADMM_L2, IA_ADMM_LP = 1, 2, 3
+
+
+class AdmmConfig(C.Structure):
+    _fields_ = [("norm", C.c_int), ("max_iters", C.c_int), ("rho", C.c_double), ("gamma", C.c_double),
+                ("epsilon", C.c_double), ("p", C.c_double), ("gst_iters", C.c_int)]
+
+
 class Rules(C.Structure):
     _fields_ = [("nq", C.c_int), ("regular", C.c_void_p), ("nqs", C.c_int), ("singular", C.c_void_p)]
 
@@ -51,6 +59,8 @@ _PP = C.POINTER(C.c_void_p)
 
 _SIGS = {
     "ia_config_default": (None, [_P]),
+    "ia_admm_config_default": (None, [_P]),
+    "ia_admm_batch": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "ia_config_size": (_I, []),
     "ia_status_string": (C.c_char_p, [_I]),
     "ia_version": (C.c_char_p, []),
@@ -127,6 +137,14 @@ def check(code: int, where: str):
 def default_config(**kw) -> Config:
     cfg = Config()
     lib().ia_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def default_admm_config(**kw) -> AdmmConfig:
+    cfg = AdmmConfig()
+    lib().ia_admm_config_default(C.byref(cfg))
     for k, v in kw.items():
         setattr(cfg, k, v)
     return cfg

@@ -18,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import IA_OK, IAError, check, default_config  # noqa: F401
+from ._lib import IA_OK, IAError, check, default_admm_config, default_config  # noqa: F401
 
 _P = C.c_void_p
 
@@ -517,6 +517,28 @@ def bem_modes_batch(ctx, mesh, mics, k, nmodes, cfg=None, pressures=True, cp=Non
              _dptr(Pr) if Pr is not None else None, _dptr(info)),
           "ia_bem_modes_complex_batch" if complex_modes else "ia_bem_modes_batch")
     return s, Ur, Hr, Pr, info
+
+
+def admm_batch(ctx, H, p, lambda0, acfg=None, x0=None, out=None):
+    """ADMM inversion (MATLAB/ADMMG.m): H (F, m, l) complex128 -- torch's
+    row-major view of F column-major l x m matrices, as elsewhere here -- p
+    (F, nrhs, l), lambda0 (F, nrhs) float64, x0 (F, nrhs, m) or None.  Returns
+    (c (F, nrhs, m), iters (F, nrhs), info (F,))."""
+    import torch
+    acfg = acfg or default_admm_config()
+    F, m, l = H.shape
+    nrhs = p.shape[1]
+    dev = H.device
+    if out is not None:
+        c, its, info = out
+    else:
+        c = torch.empty((F, nrhs, m), dtype=torch.complex128, device=dev)
+        its = torch.empty((F, nrhs), dtype=torch.int32, device=dev)
+        info = torch.zeros(F, dtype=torch.int32, device=dev)
+    check(_lib.lib().ia_admm_batch(ctx.handle, l, m, F, _dptr(H), nrhs, _dptr(p), _dptr(lambda0, torch.float64),
+                                   C.byref(acfg), _dptr(x0) if x0 is not None else None, _dptr(c), _dptr(its),
+                                   _dptr(info)), "ia_admm_batch")
+    return c, its, info
 
 
 def sound_power_batch(ctx, R, v):

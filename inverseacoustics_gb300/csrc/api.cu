@@ -189,6 +189,19 @@ void ia_config_default(ia_config *cfg)
     cfg->mode_oversample = 16;
 }
 
+void ia_admm_config_default(ia_admm_config *cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->norm = IA_ADMM_L1;
+    cfg->max_iters = 200;
+    cfg->rho = 1.0;
+    cfg->gamma = 1.0;
+    cfg->epsilon = 1e-6;
+    cfg->p = 0.5;
+    cfg->gst_iters = 5;
+}
+
 const char *ia_status_string(int status)
 {
     switch (status) {
@@ -826,6 +839,24 @@ int ia_bem_modes_complex_batch(ia_context *ctx, const ia_mesh *mesh, int l, cons
 {
     return bem_modes_entry(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, nmodes, cfg, true, d_Ur, d_sr, d_Hr, d_Pr,
                            d_info);
+}
+
+int ia_admm_batch(ia_context *ctx, int l, int m, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_p,
+                  const double *d_lambda0, const ia_admm_config *acfg, const ia_complex *d_x0, ia_complex *d_c,
+                  int *d_iters, int *d_info)
+{
+    if (!ctx || !acfg || l < 1 || m < 1 || F < 1 || nrhs < 1 || !d_H || !d_p || !d_lambda0 || !d_c || !d_info)
+        return IA_ERR_ARG;
+    if (acfg->norm < IA_ADMM_L1 || acfg->norm > IA_ADMM_LP || acfg->max_iters < 0 || !(acfg->rho > 0.0) ||
+        !isfinite(acfg->rho) || !isfinite(acfg->gamma) || !(acfg->epsilon >= 0.0))
+        return IA_ERR_ARG;
+    if (acfg->norm == IA_ADMM_LP && (!(acfg->p > 0.0 && acfg->p <= 1.0) || acfg->gst_iters < 0)) return IA_ERR_ARG;
+    int st = ws_reserve(ctx, admm_ws_bytes(l, m, F, nrhs));
+    if (!st) st = clear_info(ctx, d_info, F);
+    if (st) return st;
+    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+    return admm_batched(ctx, l, m, F, (const double2 *)d_H, nrhs, (const double2 *)d_p, d_lambda0, acfg,
+                        (const double2 *)d_x0, (double2 *)d_c, d_iters, d_info, cur);
 }
 
 int ia_sound_power_batch(ia_context *ctx, int n, int F, const double *d_R, int nrhs, const ia_complex *d_v,

@@ -221,6 +221,12 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
                       double2 *Hr, double2 *Pr, int *info, WsCursor &cur);
 size_t sound_power_ws_bytes(int n, int F);
 
+// ---- ADMM (admm.cu)
+size_t admm_ws_bytes(int l, int m, int F, int nrhs);
+int admm_batched(ia_context *ctx, int l, int m, int F, const double2 *H, int nrhs, const double2 *P,
+                 const double *lam0, const ia_admm_config *acfg, const double2 *x0, double2 *c, int *iters,
+                 int *info, WsCursor &cur);
+
 // ---- differentiable ESM design (adjoint.cu); gm == nullptr: forward only
 size_t esm_design_ws_bytes(int l, int m, int F, int R);
 int esm_design_batched(ia_context *ctx, int l, int m, int F, int R, const double *mics, const double *surf,

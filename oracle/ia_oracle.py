@@ -11,7 +11,11 @@ Each function cites the reference code it restates.  Parity pins:
   * hels against scipy's spherical Bessel and Legendre functions (the
     reference's CPU hels() needs GSL, which is absent);
   * gcv / tikhonov / tsvd / csvd restate MATLAB/regtools/*G.m (MATLAB is
-    absent); sinc-R has no reference code and is unpinned.
+    absent); sinc-R has no reference code and is unpinned;
+  * bem_modes / mass_matrix against the reference's own invr() output;
+  * admm restates MATLAB/ADMMG.m; with MATLAB absent it is pinned by its
+    fixed points only (L2: the Tikhonov solution; L1: the lasso optimality
+    conditions), not by reference outputs.
 """
 from __future__ import annotations
 
@@ -729,3 +733,93 @@ def solve_regularized(H, b, method, npoints=200, lam_fixed=None):
         lam = lam_fixed
     x = dsvd(U, s, V, b, lam) if m == "d" else tikhonov(U, s, V, b, lam)
     return x, lam, s
+
+
+# ---------------------------------------------------------------------------
+# ADMM  (MATLAB/ADMMG.m:1-90)
+# ---------------------------------------------------------------------------
+def admm_x0(A, b):
+    """The starting point x = A \\ b (ADMMG.m:6,32,50): the least-squares
+    solution for square and tall A; for wide A the minimum-norm solution
+    (MATLAB's backslash returns a basic solution there, which depends on its
+    column pivoting)."""
+    l, m = A.shape
+    if l >= m:
+        return np.linalg.lstsq(A, b, rcond=None)[0]
+    Q, R = np.linalg.qr(A.conj().T)
+    return Q @ np.linalg.solve(R.conj().T, b)
+
+
+def admm_gst_threshold(lam_p, p):
+    """tpgst of ADMMG.m:59, the generalised soft-threshold of |y|."""
+    t = 2.0 * lam_p * (1.0 - p)
+    return t ** (1.0 / (2.0 - p)) + lam_p * p * t ** ((p - 1.0) / (2.0 - p))
+
+
+def admm(A, b, lambda_0, rho, gamma, epsilon, Nm, nor, p=None, N=None, x0=None):
+    """ADMMG.m:1-90, one right-hand side.  nor 1: L1 (soft threshold,
+    continuation lambda = 5 lambda_0 * 0.75^j while above lambda_0 / 10);
+    2: L2; 3: Lp (generalised soft threshold, N fixed-point steps).  Every
+    c-update solves (2 A^H A + rho I) c = 2 A^H b + rho x - u; the first time
+    all three of ||c - c_old||, ||c - x||, ||u - u_old|| are <= epsilon ends
+    the whole run.  Returns (c, iterations, converged)."""
+    A = np.asarray(A, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    n = A.shape[1]
+    x = admm_x0(A, b) if x0 is None else np.array(x0, dtype=np.complex128)
+    aa21 = 2.0 * (A.conj().T @ A) + rho * np.eye(n)
+    from scipy.linalg import lu_factor, lu_solve
+    lu = lu_factor(aa21)          # aa21 \ (...) every iteration, factored once
+    aa22 = 2.0 * (A.conj().T @ b)
+    c = np.zeros(n, dtype=np.complex128)
+    its = 0
+
+    def conv(c, cold, x, u, uold):
+        return (np.linalg.norm(c - cold) <= epsilon and np.linalg.norm(c - x) <= epsilon
+                and np.linalg.norm(u - uold) <= epsilon)
+
+    if nor == 2:
+        u = np.zeros(n, dtype=np.complex128)
+        dlr = 2.0 * lambda_0 + rho
+        for _ in range(Nm):
+            cold = c
+            c = lu_solve(lu, aa22 + rho * x - u)
+            its += 1
+            x = (rho * c + u) / dlr
+            uold = u
+            u = u + gamma * rho * (c - x)
+            if conv(c, cold, x, u, uold):
+                return c, its, True
+        return c, its, False
+    lambda_e = lambda_0 / 10.0
+    lam = lambda_0 * 5.0
+    u = np.zeros(n, dtype=np.complex128) if nor == 1 else x.copy()
+    while lam > lambda_e:
+        if nor == 1:
+            lr = lam / rho
+        else:
+            lam_p = 2.0 * lam / rho
+            tau = admm_gst_threshold(lam_p, p)
+        for _ in range(Nm):
+            cold = c
+            c = lu_solve(lu, aa22 + rho * x - u)
+            its += 1
+            y = c + u / rho
+            ay = np.abs(y)
+            if nor == 1:
+                # max(0, |y| - lr) exp(i wrapTo2Pi(angle(y))), ADMMG.m:18
+                x = np.maximum(0.0, ay - lr) * np.exp(1j * np.angle(y))
+            else:
+                keep = ~(ay <= tau)
+                s = ay.astype(np.complex128)
+                for _d in range(N):
+                    s = ay - lam_p * p * np.power(s, complex(p - 1.0, 0.0))
+                with np.errstate(invalid="ignore", divide="ignore"):
+                    sgn = np.where(ay > 0, y / np.where(ay > 0, ay, 1.0), 0.0)
+                x = sgn * s * keep
+            uold = u
+            u = u + gamma * rho * (c - x)
+            if conv(c, cold, x, u, uold):
+                return c, its, True
+        lam = max(0.75 * lam, lambda_e)
+    return c, its, False

@@ -282,3 +282,54 @@ def test_lambda_selectors_restatement():
         assert np.isfinite(f).all()
     x = O.dsvd(U, s, V, b, 0.3)
     assert relerr(V.conj().T @ x * (s + 0.3), U.conj().T @ b) < 1e-12
+
+
+def _admm_problem(seed, l, m, k=3, noise=1e-3):
+    rng = np.random.default_rng(seed)
+    A = (rng.normal(size=(l, m)) + 1j * rng.normal(size=(l, m))) / np.sqrt(l)
+    xt = np.zeros(m, complex)
+    idx = rng.choice(m, k, replace=False)
+    xt[idx] = rng.normal(size=k) + 1j * rng.normal(size=k)
+    b = A @ xt + noise * (rng.normal(size=l) + 1j * rng.normal(size=l))
+    return A, b, xt
+
+
+def test_admm_l2_fixed_point_is_tikhonov():
+    """ADMMG.m case 2 converges to argmin ||Ac - b||^2 + lambda_0 ||c||^2."""
+    for l, m in ((20, 60), (40, 12)):
+        A, b, _ = _admm_problem(1, l, m)
+        c, its, conv = O.admm(A, b, 0.3, 5.0, 1.0, 1e-12, 5000, 2)
+        assert conv
+        ct = np.linalg.solve(A.conj().T @ A + 0.3 * np.eye(m), A.conj().T @ b)
+        assert relerr(c, ct) < 1e-10
+
+
+def test_admm_l1_fixed_point_is_lasso():
+    """ADMMG.m case 1 stops at a lasso point of its current stage lambda:
+    2 [A^H (b - A c)]_j = lambda c_j / |c_j| on the support, |.| <= lambda off it."""
+    A, b, xt = _admm_problem(2, 30, 80)
+    lam0, Nm = 0.5, 2000
+    c, its, conv = O.admm(A, b, lam0, 5.0, 1.0, 1e-10, Nm, 1)
+    assert conv
+    lam = 5 * lam0 * 0.75 ** ((its - 1) // Nm)
+    g_ = 2 * A.conj().T @ (b - A @ c)
+    on = np.abs(c) > 1e-8
+    assert on.sum() >= 3
+    assert np.max(np.abs(g_[on] - lam * c[on] / np.abs(c[on]))) < 1e-6
+    assert np.max(np.abs(g_[~on])) <= lam * (1 + 1e-6)
+
+
+def test_admm_gst_threshold_and_x0():
+    # p = 1: the generalised soft threshold is the soft threshold lambda_p
+    assert O.admm_gst_threshold(0.7, 1.0) == 0.7
+    # p = 1/2: tau = (lambda_p)^(2/3) + (lambda_p / 2) (lambda_p)^(-1/3), the
+    # point where the thresholded value would reach its fixed point
+    lp = 0.4
+    assert abs(O.admm_gst_threshold(lp, 0.5) - (lp ** (2 / 3) + 0.5 * lp * lp ** (-1 / 3))) < 1e-15
+    # x0: minimum norm for wide A (in the range of A^H), least squares for tall
+    A, b, _ = _admm_problem(3, 10, 30)
+    x0 = O.admm_x0(A, b)
+    assert relerr(A @ x0, b) < 1e-12
+    assert relerr(x0, np.linalg.pinv(A) @ b) < 1e-12
+    A, b, _ = _admm_problem(4, 30, 10)
+    assert relerr(O.admm_x0(A, b), np.linalg.lstsq(A, b, rcond=None)[0]) < 1e-12
