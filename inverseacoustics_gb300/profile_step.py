@@ -2,13 +2,16 @@
 (ncu launch lists and kernel captures); prints nothing but a checksum.  Same
 workloads and code paths as bench.py's timed steps.
 
-    python -m inverseacoustics_gb300.profile_step [--workload ibem|radiation|design]
-        [--precision mixed|fp64] [--reps 2] [--freqs 64] [--subdiv 3]
+    python -m inverseacoustics_gb300.profile_step [--workload ibem|radiation|design|bemmodes|admm]
+        [--precision mixed|fp64] [--reps 2] [--freqs 64] [--subdiv 3] [--admm-iters 50]
 
 ibem: the IBEM sphere pipeline (642 nodes / 1280 triangles / 120 mics).
 radiation: the baffled plate (1280 elements, 192 mics): sinc R, 32 radiation
 modes, ESM TSVD reconstruction (k = 36), sound power.
 design: ESM array design (128 mics, 642 sources, 16 fields), forward + adjoint.
+bemmodes: BEM radiation modes of the IBEM sphere, 32 modes of Re(G Z).
+admm: L1 ADMM on the sphere's monopole transfer matrices (120 mics, 642
+sources), epsilon = 0: all 14 continuation stages of --admm-iters iterations.
 """
 from __future__ import annotations
 
@@ -76,6 +79,41 @@ def _design(a, dev, api, g):
     return float(out[0].sum()), int(out[4].abs().sum())
 
 
+def _bemmodes(a, dev, api, g):
+    import torch
+    w = g.ibem_sphere(n_freq=a.freqs, subdiv=a.subdiv)
+    ctx = api.Context(0)
+    mesh = api.Mesh(ctx, w.arrays["nodes"], w.arrays["elems"])
+    md, kd = (torch.as_tensor(np.ascontiguousarray(x), device=dev) for x in (w.arrays["mics"], w.k))
+    cfg = api.default_config(precision=1 if a.precision == "mixed" else 0)
+    out = None
+    for _ in range(a.reps):
+        out = api.bem_modes_batch(ctx, mesh, md, kd, 32, cfg)
+    torch.cuda.synchronize()
+    return float(out[0].sum()), int(out[4].abs().sum())
+
+
+def _admm(a, dev, api, g):
+    import torch
+    w = g.ibem_sphere(n_freq=a.freqs, subdiv=a.subdiv)
+    mics, src = w.arrays["mics"], w.arrays["nodes"] * 0.7
+    ctx = api.Context(0)
+    l, m, F = mics.shape[1], src.shape[1], a.freqs
+    H = api.monopole_batch(ctx, torch.as_tensor(mics, device=dev), torch.as_tensor(src, device=dev),
+                           torch.as_tensor(w.k, device=dev))
+    H /= torch.linalg.vector_norm(H, dim=(1, 2), keepdim=True) / math.sqrt(l)
+    x = torch.zeros((F, m, 1), dtype=torch.complex128, device=dev)
+    x[:, [5, 77, 140, 400], 0] = torch.tensor([1.0, 0.7j, -0.5, 0.3 + 0.3j], dtype=torch.complex128, device=dev)
+    p = torch.matmul(H.transpose(1, 2), x).transpose(1, 2).contiguous()
+    lam = torch.full((F, 1), 0.01, dtype=torch.float64, device=dev)
+    acfg = api.default_admm_config(norm=1, max_iters=a.admm_iters, rho=2.0, epsilon=0.0)
+    out = None
+    for _ in range(a.reps):
+        out = api.admm_batch(ctx, H, p, lam, acfg)
+    torch.cuda.synchronize()
+    return float(out[0].abs().sum()), int(out[1].sum())
+
+
 def main():
     import torch
 
@@ -83,16 +121,18 @@ def main():
     from . import geometry as g
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="ibem", choices=["ibem", "radiation", "design"])
+    ap.add_argument("--workload", default="ibem", choices=["ibem", "radiation", "design", "bemmodes", "admm"])
+    ap.add_argument("--admm-iters", type=int, default=50, help="ADMM: Nm (iterations per continuation stage)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--freqs", type=int, default=None)
     ap.add_argument("--subdiv", type=int, default=3)
     a = ap.parse_args()
     if a.freqs is None:
-        a.freqs = {"ibem": 64, "radiation": 256, "design": 128}[a.workload]
+        a.freqs = {"ibem": 64, "radiation": 256, "design": 128, "bemmodes": 16, "admm": 64}[a.workload]
     dev = torch.device("cuda:0")
-    fn = {"ibem": _ibem, "radiation": _radiation, "design": _design}[a.workload]
+    fn = {"ibem": _ibem, "radiation": _radiation, "design": _design, "bemmodes": _bemmodes,
+          "admm": _admm}[a.workload]
     chk, info = fn(a, dev, api, g)
     print("checksum", chk, "info", info)
 
