@@ -286,8 +286,8 @@ def _bench_admm(ctx, dev, stream, flush, w, fp64_peak, reps=2):
     """ADMM L1 inversion (MATLAB/ADMMG.m) of the sphere's monopole transfer
     matrices: 120 microphones, 642 equivalent sources, 64 frequencies, Nm = 50
     iterations per continuation stage and epsilon = 0, i.e. all 14 stages
-    (700 c-updates per system).  The iteration kernel is FP64-issue bound:
-    per c-update and cluster CTA, (2 l m / cs + l^2) complex multiply-adds."""
+    (700 c-updates per system).  Per c-update 2 l m + l^2 complex
+    multiply-adds (A r, K2 y, A^H z); FP64 and double-float timed."""
     import numpy as np
     import torch
 
@@ -303,23 +303,29 @@ def _bench_admm(ctx, dev, stream, flush, w, fp64_peak, reps=2):
     x[:, [5, 77, 140, 400], 0] = torch.tensor([1.0, 0.7j, -0.5, 0.3 + 0.3j], dtype=torch.complex128, device=dev)
     pd = torch.matmul(Hd.transpose(1, 2), x).transpose(1, 2).contiguous()   # (F, 1, l)
     lam = torch.full((F, 1), 0.01, dtype=torch.float64, device=dev)
-    acfg = api.default_admm_config(norm=1, max_iters=Nm, rho=2.0, epsilon=0.0)
-    out = api.admm_batch(ctx, Hd, pd, lam, acfg)
-    times = []
-    for _ in range(reps):
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        api.admm_batch(ctx, Hd, pd, lam, acfg, out=out)
-        b.record(stream)
-        b.synchronize()
-        times.append(a.elapsed_time(b))
-    ms = sum(times) / reps
+    res, outs = {}, {}
+    for prec in (1, 0):
+        acfg = api.default_admm_config(norm=1, max_iters=Nm, rho=2.0, epsilon=0.0, precision=prec)
+        out = api.admm_batch(ctx, Hd, pd, lam, acfg)
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            api.admm_batch(ctx, Hd, pd, lam, acfg, out=out)
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        res[prec], outs[prec] = sum(times) / reps, out
+    ms, ms64 = res[1], res[0]
+    out = outs[1]
+    c1, c0 = outs[1][0], outs[0][0]
+    err = float(((c1 - c0).abs().pow(2).sum((1, 2)).sqrt() / c0.abs().pow(2).sum((1, 2)).sqrt()).max())
     its = int(out[1][0, 0])
     cs = 1
     while cs < 8 and (m + 2 * cs - 1) // (2 * cs) >= 128:
         cs *= 2
-    flops = 8.0 * its * F * cs * (2 * l * ((m + cs - 1) // cs) + l * l)
+    flops = 8.0 * its * F * (2 * l * m + l * l)
     # CPU baseline: the oracle's restatement on one system for 5 of the 14
     # stages, scaled to the full run
     from oracle import ia_oracle as O
@@ -329,9 +335,13 @@ def _bench_admm(ctx, dev, stream, flush, w, fp64_peak, reps=2):
     c5 = O.admm(H0, p0, 0.01, 2.0, 1.0, 0.0, 5, 1)
     cpu_s = (time.perf_counter() - t0) * (its / c5[1])
     return {"workload": f"admm_l1_monopole_{l}mic_{m}src_F{F}_Nm{Nm}", "systems": F, "c_updates_per_system": its,
-            "ms": ms, "value": F * its / (ms / 1000.0), "unit": "c-updates/s (all systems)",
-            "fp64": {"achieved_tflops": flops / (ms / 1000.0) / 1e12, "peak_dgemm_measured": fp64_peak,
-                     "cluster_ctas": cs, "note": "includes the setup (A^H b, K inverse, x0) in the timed call"},
+            "ms": ms, "value": F * its / (ms / 1000.0), "unit": "c-updates/s (all systems), double-float products",
+            "fp64_ms": ms64, "fp64_value": F * its / (ms64 / 1000.0), "mixed_speedup": ms64 / ms,
+            "accuracy": {"c_mixed_vs_fp64_rel": err},
+            "flops": {"fp64_achieved_tflops": flops / (ms64 / 1000.0) / 1e12, "peak_dgemm_measured": fp64_peak,
+                      "mixed_equivalent_tflops": flops / (ms / 1000.0) / 1e12, "cluster_ctas": cs,
+                      "note": "8 flops per complex multiply-add; the timed call includes the setup "
+                              "(A^H b, the c-update inverse, x0)"},
             "cpu_baseline": {"value": its / cpu_s, "unit": "c-updates/s (one system)", "cores": "numpy BLAS",
                              "kind": "port", "sample": "oracle restatement, 70 c-updates of system 0, scaled"},
             "info_noconv_expected": int(out[2].ne(0).all())}

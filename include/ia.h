@@ -121,10 +121,12 @@ typedef struct {
     double epsilon;   /* stop when ||c - c_old||, ||c - x|| and ||u - u_old|| are all <= epsilon */
     double p;         /* Lp exponent, 0 < p <= 1 (IA_ADMM_LP) */
     int gst_iters;    /* N: fixed-point steps of the generalised soft threshold (IA_ADMM_LP) */
+    int precision;    /* IA_PREC_FP64, or IA_PREC_MIXED: the iteration's matrix-vector products in
+                         double-float (FP32 pairs, ~48-bit significand); setup, shrink and norms FP64 */
 } ia_admm_config;
 
 void ia_config_default(ia_config *cfg);
-/* norm L1, max_iters 200, rho 1, gamma 1, epsilon 1e-6, p 0.5, gst_iters 5 */
+/* norm L1, max_iters 200, rho 1, gamma 1, epsilon 1e-6, p 0.5, gst_iters 5, FP64 */
 void ia_admm_config_default(ia_admm_config *cfg);
 /* sizeof(ia_config), for bindings that mirror the struct */
 int ia_config_size(void);

@@ -43,7 +43,7 @@ IA_ADMM_L1, IA_ADMM_L2, IA_ADMM_LP = 1, 2, 3
 
 class AdmmConfig(C.Structure):
     _fields_ = [("norm", C.c_int), ("max_iters", C.c_int), ("rho", C.c_double), ("gamma", C.c_double),
-                ("epsilon", C.c_double), ("p", C.c_double), ("gst_iters", C.c_int)]
+                ("epsilon", C.c_double), ("p", C.c_double), ("gst_iters", C.c_int), ("precision", C.c_int)]
 
 
 class Rules(C.Structure):

@@ -200,6 +200,7 @@ void ia_admm_config_default(ia_admm_config *cfg)
     cfg->epsilon = 1e-6;
     cfg->p = 0.5;
     cfg->gst_iters = 5;
+    cfg->precision = IA_PREC_FP64;
 }
 
 const char *ia_status_string(int status)
@@ -851,6 +852,7 @@ int ia_admm_batch(ia_context *ctx, int l, int m, int F, const ia_complex *d_H, i
         !isfinite(acfg->rho) || !isfinite(acfg->gamma) || !(acfg->epsilon >= 0.0))
         return IA_ERR_ARG;
     if (acfg->norm == IA_ADMM_LP && (!(acfg->p > 0.0 && acfg->p <= 1.0) || acfg->gst_iters < 0)) return IA_ERR_ARG;
+    if (acfg->precision != IA_PREC_FP64 && acfg->precision != IA_PREC_MIXED) return IA_ERR_ARG;
     int st = ws_reserve(ctx, admm_ws_bytes(l, m, F, nrhs));
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;

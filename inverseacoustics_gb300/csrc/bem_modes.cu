@@ -124,6 +124,17 @@ __global__ void modes_phase_kernel(int m, int nm, const double2 *__restrict__ U,
     }
 }
 
+// out = hi + lo of double-float complex pairs
+__global__ void df_join_kernel(size_t count, const float4 *__restrict__ in, double2 *__restrict__ out)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = in[e];
+        out[e] = make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+    }
+}
+
+static bool bem_mixed_solve(const ia_config *cfg, int n_ch) { return cfg->precision == IA_PREC_MIXED && n_ch == 0; }
+
 size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, const ia_config *cfg, bool cplx)
 {
     const size_t M = mesh->m, MT = M + n_ch, L = l, FF = F;
@@ -131,7 +142,54 @@ size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, c
                ws_round(8 * (size_t)mesh->gnnz) + ws_round(16 * M * nm * FF);
     if (cplx) b += ws_round(16 * M * M * FF) + ws_round(8 * M * FF);
     else b += ws_round(8 * M * M * FF) + ws_round(8 * nm * FF) + radiation_modes_ws_bytes(mesh->m, F, nm, cfg, true);
+    if (bem_mixed_solve(cfg, n_ch)) b += 2 * ws_round(8 * M * M * FF) + ws_round(16 * M * M * FF);
     return b + 4096;
+}
+
+// Mixed Z = A^-1 B and H = A_hs Z - B_hs: A and B arrive as double-float row
+// blocks (A^T, B^T as float4); FP32 LU of A and FP32 solves for Z, refined
+// with double-float residuals B - A Z (max(1, refine_steps) times); H by the
+// double-float GEMM.  On exit Z (FP64, m x m) is in At's storage.
+static int bem_mixed_z(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int F, const double *k,
+                       const ia_config *cfg, double2 *At, double2 *Bt, double2 *A, double2 *B, double2 *Ahs_t,
+                       double2 *Bhs_t, double2 *Ahs, double2 *H, int *ipiv, int *info, WsCursor &cur)
+{
+    const int m = mesh->m;
+    const long long mm = (long long)m * m, ml = (long long)m * l;
+    int st;
+    if ((st = ibem_rows(ctx, mesh, l, mics, 0, nullptr, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t, true, true)))
+        return st;
+    // A, B column-major as float4 pairs (16-byte moves through the double2 view)
+    if ((st = ztranspose_batched(ctx, m, m, At, m, mm, A, m, mm, false, F))) return st;
+    if ((st = ztranspose_batched(ctx, m, m, Bt, m, mm, B, m, mm, false, F))) return st;
+    if ((st = ztranspose_batched(ctx, m, l, Ahs_t, m, ml, Ahs, l, ml, false, F))) return st;
+    if ((st = ztranspose_batched(ctx, m, l, Bhs_t, m, ml, H, l, ml, false, F))) return st;
+    float4 *A4 = reinterpret_cast<float4 *>(A), *B4 = reinterpret_cast<float4 *>(B);
+    float2 *A32 = cur.take<float2>((size_t)mm * F);
+    float2 *Z32 = cur.take<float2>((size_t)mm * F);
+    float4 *Z4 = cur.take<float4>((size_t)mm * F);
+    double2 *Z = At, *R = Bt;
+    if ((st = df_hi_batched(ctx, (size_t)mm * F, A4, A32))) return st;
+    if ((st = getrf_batched<float2>(ctx, m, A32, m, mm, ipiv, info, F))) return st;
+    if ((st = df_hi_batched(ctx, (size_t)mm * F, B4, Z32))) return st;
+    if ((st = getrs_batched<float2>(ctx, m, m, A32, m, mm, ipiv, Z32, m, mm, F))) return st;
+    if ((st = copy2d_batched<float2, double2>(ctx, m, m, Z32, m, mm, Z, m, mm, false, F))) return st;
+    const int steps = cfg->refine_steps > 1 ? cfg->refine_steps : 1;
+    const size_t n4 = (size_t)mm * F;
+    for (int it = 0; it < steps; ++it) {
+        df_join_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(n4, B4, R);
+        IA_LAUNCH_CHECK(ctx);
+        if ((st = split_df_batched(ctx, n4, Z, Z4))) return st;
+        if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, m, m, -1.0, A4, m, mm, Z4, m, mm, 1.0, R, m, mm, F))) return st;
+        if ((st = copy2d_batched<double2, float2>(ctx, m, m, R, m, mm, Z32, m, mm, false, F))) return st;
+        if ((st = getrs_batched<float2>(ctx, m, m, A32, m, mm, ipiv, Z32, m, mm, F))) return st;
+        if ((st = add2d_batched<float2>(ctx, m, m, Z32, m, mm, Z, m, mm, F))) return st;
+    }
+    // H = A_hs Z - B_hs (A_hs split into A_hs^T's storage)
+    float4 *Ahs4 = reinterpret_cast<float4 *>(Ahs_t);
+    if ((st = split_df_batched(ctx, n4, Z, Z4))) return st;
+    if ((st = split_df_batched(ctx, (size_t)ml * F, Ahs, Ahs4))) return st;
+    return dfgemm4_batched(ctx, OP_N, OP_N, l, m, m, 1.0, Ahs4, l, ml, Z4, m, mm, -1.0, H, l, ml, F);
 }
 
 int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp,
@@ -149,27 +207,33 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
     double *gval = cur.take<double>((size_t)mesh->gnnz);
     double2 *Uc = cplx ? static_cast<double2 *>(Ur) : cur.take<double2>((size_t)m * nm * F);
     const double2 one = make_double2(1.0, 0.0), mone = make_double2(-1.0, 0.0), zero = make_double2(0.0, 0.0);
-    // collocation rows, then A, B (mt x m), A_hs, B_hs (l x m) column-major
-    if ((st = ibem_rows(ctx, mesh, l, mics, n_ch, cp, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t,
-                        cfg->precision == IA_PREC_MIXED)))
-        return st;
-    if ((st = ztranspose_batched(ctx, m, mt, At, m, tm, A, mt, tm, false, F))) return st;
-    if ((st = ztranspose_batched(ctx, m, mt, Bt, m, tm, B, mt, tm, false, F))) return st;
-    if ((st = ztranspose_batched(ctx, m, l, Ahs_t, m, ml, Ahs, l, ml, false, F))) return st;
-    if ((st = ztranspose_batched(ctx, m, l, Bhs_t, m, ml, H, l, ml, false, F))) return st;
-    // Z = A \ B (B's storage, leading dimension mt)
-    if (n_ch == 0) {
-        if ((st = zgetrf_batched(ctx, m, A, mt, tm, ipiv, info, F))) return st;
-        if ((st = zgetrs_batched(ctx, m, m, A, mt, tm, ipiv, B, mt, tm, F))) return st;
-    } else {
-        if ((st = zgeqrs_batched(ctx, mt, m, A, mt, tm, m, B, mt, tm, F))) return st;
-        if ((st = zbacksolve_upper_batched(ctx, m, m, A, mt, tm, B, mt, tm, F))) return st;
-    }
-    // compact Z (ld mt -> m) into At's storage
+    const bool mixed_z = bem_mixed_solve(cfg, n_ch);
     double2 *Z = At;
-    if ((st = zcopy2d_batched(ctx, m, m, B, mt, tm, Z, m, mm, false, F))) return st;
-    // H = A_hs Z - B_hs
-    if ((st = zgemm_batched(ctx, OP_N, OP_N, l, m, m, one, Ahs, l, ml, Z, m, mm, mone, H, l, ml, F))) return st;
+    if (mixed_z) {
+        if ((st = bem_mixed_z(ctx, mesh, l, mics, F, k, cfg, At, Bt, A, B, Ahs_t, Bhs_t, Ahs, H, ipiv, info, cur)))
+            return st;
+    } else {
+        // collocation rows, then A, B (mt x m), A_hs, B_hs (l x m) column-major
+        if ((st = ibem_rows(ctx, mesh, l, mics, n_ch, cp, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t,
+                            cfg->precision == IA_PREC_MIXED)))
+            return st;
+        if ((st = ztranspose_batched(ctx, m, mt, At, m, tm, A, mt, tm, false, F))) return st;
+        if ((st = ztranspose_batched(ctx, m, mt, Bt, m, tm, B, mt, tm, false, F))) return st;
+        if ((st = ztranspose_batched(ctx, m, l, Ahs_t, m, ml, Ahs, l, ml, false, F))) return st;
+        if ((st = ztranspose_batched(ctx, m, l, Bhs_t, m, ml, H, l, ml, false, F))) return st;
+        // Z = A \ B (B's storage, leading dimension mt)
+        if (n_ch == 0) {
+            if ((st = zgetrf_batched(ctx, m, A, mt, tm, ipiv, info, F))) return st;
+            if ((st = zgetrs_batched(ctx, m, m, A, mt, tm, ipiv, B, mt, tm, F))) return st;
+        } else {
+            if ((st = zgeqrs_batched(ctx, mt, m, A, mt, tm, m, B, mt, tm, F))) return st;
+            if ((st = zbacksolve_upper_batched(ctx, m, m, A, mt, tm, B, mt, tm, F))) return st;
+        }
+        // compact Z (ld mt -> m) into At's storage
+        if ((st = zcopy2d_batched(ctx, m, m, B, mt, tm, Z, m, mm, false, F))) return st;
+        // H = A_hs Z - B_hs
+        if ((st = zgemm_batched(ctx, OP_N, OP_N, l, m, m, one, Ahs, l, ml, Z, m, mm, mone, H, l, ml, F))) return st;
+    }
     mass_matrix_kernel<<<(m + 127) / 128, 128, 0, ctx->stream>>>(m, mesh->d_gptr, mesh->d_gidx, mesh->d_adj_ptr,
                                                                   mesh->d_adj, mesh->d_evert, mesh->d_egeo,
                                                                   mesh->d_reg, mesh->nq, gval);
@@ -198,13 +262,18 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
         modes_finish_kernel<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>((size_t)nm * F, lam, sr, nu, Urr, Uc);
         IA_LAUNCH_CHECK(ctx);
     }
-    // H_r = H U_r, P_r = Z U_r
-    if ((st = zgemm_batched(ctx, OP_N, OP_N, l, nm, m, one, H, l, ml, Uc, m, (long long)m * nm, zero, Hr, l,
-                            (long long)l * nm, F)))
+    // H_r = H U_r, P_r = Z U_r (double-float products on the mixed path)
+    const long long mn = (long long)m * nm;
+    if (mixed_z) {
+        if ((st = dfgemm_batched(ctx, OP_N, OP_N, l, nm, m, 1.0, H, l, ml, Uc, m, mn, 0.0, Hr, l, (long long)l * nm,
+                                 F)))
+            return st;
+        if (Pr) st = dfgemm_batched(ctx, OP_N, OP_N, m, nm, m, 1.0, Z, m, mm, Uc, m, mn, 0.0, Pr, m, mn, F);
         return st;
-    if (Pr)
-        st = zgemm_batched(ctx, OP_N, OP_N, m, nm, m, one, Z, m, mm, Uc, m, (long long)m * nm, zero, Pr, m,
-                           (long long)m * nm, F);
+    }
+    if ((st = zgemm_batched(ctx, OP_N, OP_N, l, nm, m, one, H, l, ml, Uc, m, mn, zero, Hr, l, (long long)l * nm, F)))
+        return st;
+    if (Pr) st = zgemm_batched(ctx, OP_N, OP_N, m, nm, m, one, Z, m, mm, Uc, m, mn, zero, Pr, m, mn, F);
     return st;
 }
 

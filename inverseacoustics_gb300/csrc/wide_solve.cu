@@ -13,11 +13,11 @@
 // Neither U_H nor V_H is formed.
 //
 // Mixed path (wide_solve_mixed_batched): QR of H^H and one-sided Jacobi on R
-// in FP32 give X ~ U_H (eigenvectors of E = H H^H) to ~1e-5; E is formed in
-// FP64; Ogita-Aishima refinement steps (X^H E X in FP64, X^H X and the update
-// in double-float) bring separated eigenpairs to FP64 accuracy; a two-sided
-// FP64 Jacobi on S = X^H E X separates the near-equal pairs those steps leave
-// coupled; then s = sqrt(eig E), beta = U^H b, GCV in FP64, and
+// in FP32 give X ~ U_H (eigenvectors of E = H H^H) to ~1e-5; E is formed by
+// the double-float GEMM; Ogita-Aishima refinement steps (all products in
+// double-float) bring separated eigenpairs to that level; a two-sided FP64
+// Jacobi on S = X^H E X (an FP64 product) separates the near-equal pairs
+// those steps leave coupled; then s = sqrt(eig E), beta = U^H b, GCV in FP64, and
 // x = H^H U diag(phi / s) beta against the FP64 operator.
 //
 // Both replace the reference's csvd + gcvG + tikhonovG / tsvd chain
@@ -690,21 +690,23 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     if (st) return st;
     normalize_cols_kernel<<<batch, 256, 0, ctx->stream>>>(N, R32, J32);
     IA_LAUNCH_CHECK(ctx);
-    // 2. E = H H^H (or its conjugate for H^T input).  E and S = X^H E X set
-    // the accuracy of the eigenvectors as eps ||E|| / gap, so they are FP64
-    // products; X^H X and X F only need double-float.
+    // 2. E = H H^H (or its conjugate for H^T input) by the double-float GEMM:
+    // H reaches this path from the double-float transfer (~1e-13 relative), so
+    // an FP64 product would not make E more accurate.
     const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
-    if (transposed) st = zgemm_batched(ctx, OP_C, OP_N, N, N, n, one, A, n, sA, A, n, sA, zero, E, N, sN, batch);
-    else st = zgemm_batched(ctx, OP_N, OP_C, N, N, n, one, A, m, sA, A, m, sA, zero, E, N, sN, batch);
+    if (transposed) st = dfgemm_batched(ctx, OP_C, OP_N, N, N, n, 1.0, A, n, sA, A, n, sA, 0.0, E, N, sN, batch);
+    else st = dfgemm_batched(ctx, OP_N, OP_C, N, N, n, 1.0, A, m, sA, A, m, sA, 0.0, E, N, sN, batch);
     if (st) return st;
     // 3. eigen-refinement from X = J (conj(J) for H^T input)
     if ((st = copy2d_batched<float2, double2>(ctx, N, N, J32, N, sN, X, N, sN, transposed, batch))) return st;
     // the FP32 Jacobi leaves X accurate to ~1e-5 (its stopping threshold sits
-    // above FP32 rounding noise); two quadratic steps reach FP64 level
+    // above FP32 rounding noise); two quadratic steps reach the double-float
+    // level of their products, and step 4's FP64 S = X^H E X with the
+    // two-sided Jacobi finishes at FP64 level
     const int steps = cfg->refine_steps > 2 ? cfg->refine_steps : 2;
     for (int it = 0; it < steps; ++it) {
-        if ((st = zgemm_batched(ctx, OP_N, OP_N, N, N, N, one, E, N, sN, X, N, sN, zero, T1, N, sN, batch))) return st;
-        if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;
+        if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
+        if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, T1, N, sN, 0.0, Sm, N, sN, batch))) return st;
         if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
         oa_update_kernel<<<batch, OA_THREADS, sizeof(double) * (size_t)N, ctx->stream>>>(N, Sm, Rm, Fc, lam_e);
         IA_LAUNCH_CHECK(ctx);

@@ -106,7 +106,8 @@ def _admm(a, dev, api, g):
     x[:, [5, 77, 140, 400], 0] = torch.tensor([1.0, 0.7j, -0.5, 0.3 + 0.3j], dtype=torch.complex128, device=dev)
     p = torch.matmul(H.transpose(1, 2), x).transpose(1, 2).contiguous()
     lam = torch.full((F, 1), 0.01, dtype=torch.float64, device=dev)
-    acfg = api.default_admm_config(norm=1, max_iters=a.admm_iters, rho=2.0, epsilon=0.0)
+    acfg = api.default_admm_config(norm=1, max_iters=a.admm_iters, rho=2.0, epsilon=0.0,
+                                   precision=1 if a.precision == "mixed" else 0)
     out = None
     for _ in range(a.reps):
         out = api.admm_batch(ctx, H, p, lam, acfg)

@@ -3,9 +3,10 @@ of MATLAB/ADMMG.m, all three norms, wide (dual / Woodbury form, one CTA and
 thread-block clusters) and tall (primal form) systems.
 
 Bounds.  With epsilon = 0 every run takes the same number of iterations on
-both sides and c agrees to 1e-10 relative (the c-update inverse is formed
-once and applied as a product here, solved every iteration in the oracle);
-with a finite epsilon the iteration counts agree exactly and c to 1e-9."""
+both sides and c agrees to 1e-10 relative in FP64, 1e-9 with double-float
+products (the c-update inverse is formed once and applied as a product here,
+solved every iteration in the oracle); with a finite epsilon the iteration
+counts agree exactly and c to 1e-9 (FP64) / 1e-8 (double-float)."""
 import numpy as np
 import pytest
 
@@ -43,37 +44,43 @@ def _run(ctx, cuda, A, B, lam0, acfg, x0=None):
     return c.cpu().numpy(), its.cpu().numpy(), info.cpu().numpy()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("norm", [1, 2, 3])
-@pytest.mark.parametrize("shape", [(24, 80), (40, 16), (32, 300)])
-def test_admm_fixed_iterations_match_oracle(cuda, ctx, norm, shape):
+@pytest.mark.parametrize("shape", [(24, 80), (40, 16), (32, 300), (120, 642)])
+def test_admm_fixed_iterations_match_oracle(cuda, ctx, norm, shape, precision):
     """epsilon = 0: MATLAB's loops run to the end (14 continuation stages x
-    Nm for L1 / Lp, Nm for L2)."""
+    Nm for L1 / Lp, Nm for L2).  (120, 642) is the benchmark's shape (clusters
+    of 4 CTAs)."""
     from inverseacoustics_gb300 import api
     l, m = shape
-    F, nrhs, Nm = 3, 2, 25
+    F, nrhs, Nm = (3, 2, 25) if m < 600 else (2, 1, 10)
     A, B, lam0 = _problems(10 + norm, F, nrhs, l, m)
-    acfg = api.default_admm_config(norm=norm, max_iters=Nm, rho=4.0, gamma=1.0, epsilon=0.0, p=0.5, gst_iters=4)
+    acfg = api.default_admm_config(norm=norm, max_iters=Nm, rho=4.0, gamma=1.0, epsilon=0.0, p=0.5, gst_iters=4,
+                                   precision=precision)
     c, its, info = _run(ctx, cuda, A, B, lam0, acfg)
+    tol = 1e-10 if precision == 0 else 1e-9
     for f in range(F):
         for r in range(nrhs):
             co, ito, conv = O.admm(A[f], B[f, r], lam0[f, r], 4.0, 1.0, 0.0, Nm, norm, p=0.5, N=4)
             assert not conv and its[f, r] == ito
-            assert relerr(c[f, r], co) < 1e-10, (f, r)
+            assert relerr(c[f, r], co) < tol, (f, r)
     assert np.all(info == 1)      # IA_INFO_NOCONV: no stage met epsilon = 0
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("norm", [1, 2, 3])
-def test_admm_converged_match_oracle(cuda, ctx, norm):
+def test_admm_converged_match_oracle(cuda, ctx, norm, precision):
     from inverseacoustics_gb300 import api
     l, m = 24, 80
     F, nrhs, Nm = 4, 1, 3000
     A, B, lam0 = _problems(20 + norm, F, nrhs, l, m)
-    acfg = api.default_admm_config(norm=norm, max_iters=Nm, rho=6.0, gamma=1.0, epsilon=1e-8, p=0.7, gst_iters=6)
+    acfg = api.default_admm_config(norm=norm, max_iters=Nm, rho=6.0, gamma=1.0, epsilon=1e-8, p=0.7, gst_iters=6,
+                                   precision=precision)
     c, its, info = _run(ctx, cuda, A, B, lam0, acfg)
     for f in range(F):
         co, ito, conv = O.admm(A[f], B[f, 0], lam0[f, 0], 6.0, 1.0, 1e-8, Nm, norm, p=0.7, N=6)
         assert conv and its[f, 0] == ito
-        assert relerr(c[f, 0], co) < 1e-9
+        assert relerr(c[f, 0], co) < (1e-9 if precision == 0 else 1e-8)
     assert np.all(info == 0)
 
 
