@@ -162,6 +162,21 @@ static bool all_finite(const double *p, size_t n)
     return true;
 }
 
+int ensure_side_stream(ia_context *ctx)
+{
+    if (ctx->side) return IA_OK;
+    cudaStream_t s;
+    IA_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaError_t e = cudaEventCreateWithFlags(&ctx->ev_split[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_split[1], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return cuda_status(e);
+    }
+    ctx->side = s;
+    return IA_OK;
+}
+
 }  // namespace ia
 
 using namespace ia;
@@ -245,9 +260,15 @@ int ia_create(ia_context **out, int device, void *stream)
 int ia_destroy(ia_context *ctx)
 {
     if (!ctx) return IA_OK;
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->ws) {
         cudaFreeAsync(ctx->ws, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
+    }
+    if (ctx->side) {
+        cudaEventDestroy(ctx->ev_split[0]);
+        cudaEventDestroy(ctx->ev_split[1]);
+        cudaStreamDestroy(ctx->side);
     }
     free(ctx);
     return IA_OK;
@@ -540,11 +561,12 @@ int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
 // H^T (m x l per frequency) into Ht, given workspace for A^T, B^T, pivots.
 static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                            const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
-                           double2 *Ahs_t, double2 *Ht, int *d_info)
+                           double2 *Ahs_t, double2 *Ht, int *d_info, cudaEvent_t ev_rows = nullptr)
 {
     const int m = mesh->m;
     int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
     if (st) return st;
+    if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
     const long long sMM = (long long)m * m, sML = (long long)m * l;
     // LU of M = A^T; solve M Y = A_hs^T  ->  Y = W^T, W = A_hs A^-1
     st = zgetrf_batched(ctx, m, At, m, sMM, ipiv, d_info, F);
@@ -566,7 +588,8 @@ static size_t transfer_mixed_ws_bytes(int m, int l, int F)
 // H^T = B^T Y - B_hs^T by the double-float GEMM.  Matrices in, H^T out in FP64.
 static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                                  const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
-                                 double2 *Ahs_t, double2 *Ht, int *d_info, WsCursor &cur)
+                                 double2 *Ahs_t, double2 *Ht, int *d_info, WsCursor &cur,
+                                 cudaEvent_t ev_rows = nullptr)
 {
     const int m = mesh->m;
     float2 *M32 = cur.take<float2>((size_t)m * m * F);
@@ -578,6 +601,7 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     float4 *At4 = reinterpret_cast<float4 *>(At), *Bt4 = reinterpret_cast<float4 *>(Bt);
     int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true);
     if (st) return st;
+    if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
     const long long sMM = (long long)m * m, sML = (long long)m * l;
     if ((st = df_hi_batched(ctx, (size_t)sMM * F, At4, M32))) return st;
     if ((st = getrf_batched<float2>(ctx, m, M32, m, sMM, ipiv, d_info, F))) return st;
@@ -705,6 +729,34 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
                       d_lambda, d_s, d_info, cur);
 }
 
+static size_t ibem_solve_ws_bytes(int m, int l, int F, int nrhs, const ia_config *cfg)
+{
+    const bool mixed = cfg->precision == IA_PREC_MIXED;
+    return ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
+           ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
+           (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
+}
+
+// the whole IBEM pipeline for F bins on ctx->stream; ev_rows (if given) is
+// recorded when the assembly has been issued
+static int ibem_solve_part(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
+                           const double *d_k, int nrhs, const double2 *p, const ia_config *cfg, double2 *x,
+                           double *lambda, double *s, int *info, WsCursor &cur, cudaEvent_t ev_rows)
+{
+    const int m = mesh->m;
+    double2 *At = cur.take<double2>((size_t)m * m * F);
+    double2 *Bt = cur.take<double2>((size_t)m * m * F);
+    int *ipiv = cur.take<int>((size_t)m * F);
+    double2 *Ahs = cur.take<double2>((size_t)m * l * F);
+    double2 *Ht = cur.take<double2>((size_t)m * l * F);
+    int st;
+    if (cfg->precision == IA_PREC_MIXED)
+        st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, info, cur, ev_rows);
+    else st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, info, ev_rows);
+    if (st) return st;
+    return solve_core(ctx, l, m, F, Ht, true, nrhs, p, cfg, x, lambda, s, info, cur);
+}
+
 int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                         const double *d_k, int nrhs, const ia_complex *d_p, const ia_config *cfg, ia_complex *d_x,
                         double *d_lambda, double *d_s, int *d_info)
@@ -712,24 +764,43 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     if (!ctx || !mesh || !cfg || l < 1 || F < 1 || nrhs < 1 || !d_mics || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
     const int m = mesh->m;
-    const bool mixed = cfg->precision == IA_PREC_MIXED;
-    size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
-                  (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
-    int st = ws_reserve(ctx, need);
+    // Staggered halves: with F a multiple of 8 the bins are solved as two
+    // halves on two streams, the second starting when the first one's
+    // assembly is done, so that the latency-bound stages of one half (LU
+    // panels, Jacobi, QR, one CTA per frequency) run beside the
+    // throughput-bound stages of the other.  Frequencies stay in blocks of 4
+    // in the assembly and every later kernel works per frequency, so the
+    // results are bitwise those of one F-bin pass.
+    const bool split = F >= 16 && F % 8 == 0;
+    const int Fh = split ? F / 2 : F;
+    const size_t need = ibem_solve_ws_bytes(m, l, Fh, nrhs, cfg);
+    int st = ws_reserve(ctx, split ? 2 * need : need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
-    WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
-    double2 *At = cur.take<double2>((size_t)m * m * F);
-    double2 *Bt = cur.take<double2>((size_t)m * m * F);
-    int *ipiv = cur.take<int>((size_t)m * F);
-    double2 *Ahs = cur.take<double2>((size_t)m * l * F);
-    double2 *Ht = cur.take<double2>((size_t)m * l * F);
-    if (mixed) st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info, cur);
-    else st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, d_info);
+    if (!split) {
+        WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
+        return ibem_solve_part(ctx, mesh, l, d_mics, F, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x,
+                               d_lambda, d_s, d_info, cur, nullptr);
+    }
+    if ((st = ensure_side_stream(ctx))) return st;
+    const int p = l < m ? l : m;
+    WsCursor ca{(char *)ctx->ws, 0, need}, cb{(char *)ctx->ws + need, 0, need};
+    st = ibem_solve_part(ctx, mesh, l, d_mics, Fh, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda,
+                         d_s, d_info, ca, ctx->ev_split[0]);
     if (st) return st;
-    return solve_core(ctx, l, m, F, Ht, true, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
-                      cur);
+    if (ca.off > need) return IA_ERR_ALLOC;    // workspace accounting broken: the halves would overlap
+    cudaStream_t main = ctx->stream;
+    IA_CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->ev_split[0], 0));
+    ctx->stream = ctx->side;
+    st = ibem_solve_part(ctx, mesh, l, d_mics, Fh, d_k + Fh, nrhs, (const double2 *)d_p + (size_t)Fh * nrhs * l, cfg,
+                         (double2 *)d_x + (size_t)Fh * nrhs * m, d_lambda ? d_lambda + (size_t)Fh * nrhs : nullptr,
+                         d_s ? d_s + (size_t)Fh * p : nullptr, d_info + Fh, cb, nullptr);
+    cudaError_t e = cudaEventRecord(ctx->ev_split[1], ctx->side);
+    ctx->stream = main;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, ctx->ev_split[1], 0);
+    if (st) return st;
+    if (cb.off > need) return IA_ERR_ALLOC;
+    return e == cudaSuccess ? IA_OK : cuda_status(e);
 }
 
 int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, const double *d_src, int F,

@@ -15,7 +15,8 @@ namespace ia {
 // --------------------------------------------------------------------------
 // GEMM: C = alpha op(A) op(B) + beta C.  A BM x BN tile per CTA of 256
 // threads, each thread a TM x TN block of outputs strided by BM/TM rows and
-// BN/TN columns so shared-memory reads are conflict free; K in steps of 8.
+// BN/TN columns so shared-memory reads are conflict free; K in steps of 8
+// (a step of 16 measured slower for the FP32 LU updates).
 // Every variant sums k in the same order (0..K-1, one thread per output), so
 // the autotuner's choice of tile does not change results.
 // --------------------------------------------------------------------------
@@ -40,8 +41,9 @@ __global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int 
 {
     constexpr int NTX = BN / TN, NTY = BM / TM;
     static_assert(NTX * NTY == 256, "256 threads per tile");
-    __shared__ T As[GB_K][BM];
-    __shared__ T Bs[GB_K][BN];
+    constexpr int KC = GB_K;
+    __shared__ T As[KC][BM];
+    __shared__ T Bs[KC][BN];
     const int f = blockIdx.z;
     A += f * sA;
     B += f * sB;
@@ -54,24 +56,24 @@ __global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int 
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = ctraits<T>::make(0, 0);
 
-    for (int k0 = 0; k0 < K; k0 += GB_K) {
+    for (int k0 = 0; k0 < K; k0 += KC) {
 #pragma unroll
-        for (int e = threadIdx.x; e < GB_K * BM; e += 256) {
+        for (int e = threadIdx.x; e < KC * BM; e += 256) {
             int r, kk;
             if (opa == OP_N) { r = e % BM; kk = e / BM; }
-            else { kk = e % GB_K; r = e / GB_K; }
+            else { kk = e % KC; r = e / KC; }
             As[kk][r] = ld_op(A, lda, m0 + r, k0 + kk, M, K, opa);
         }
 #pragma unroll
-        for (int e = threadIdx.x; e < GB_K * BN; e += 256) {
+        for (int e = threadIdx.x; e < KC * BN; e += 256) {
             int kk, c;
-            if (opb == OP_N) { kk = e % GB_K; c = e / GB_K; }
+            if (opb == OP_N) { kk = e % KC; c = e / KC; }
             else { c = e % BN; kk = e / BN; }
             Bs[kk][c] = ld_op(B, ldb, k0 + kk, n0 + c, K, N, opb);
         }
         __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < GB_K; ++kk) {
+        for (int kk = 0; kk < KC; ++kk) {
             T a[TM], b[TN];
 #pragma unroll
             for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + NTY * i];
@@ -229,6 +231,117 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, T *A, in
     }
 }
 
+// The same panel factorisation with the panel (rows k0..n-1 of columns
+// k0..kend-1) held in shared memory: identical arithmetic in the same order,
+// so the factors are bitwise those of lu_panel_kernel.  Row interchanges are
+// applied inside the panel only; lu_laswp_kernel applies them to the other
+// columns afterwards.
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *A, int lda, long long sA, int *ipiv,
+                                                                        int k0, int kend, int *info)
+{
+    typedef typename ctraits<T>::R R;
+    extern __shared__ unsigned char lu_smem[];
+    T *P = reinterpret_cast<T *>(lu_smem);          // P[c * pr + (i - k0)]
+    __shared__ R sval[PANEL_THREADS / 32];
+    __shared__ int sidx[PANEL_THREADS / 32];
+    __shared__ int s_piv;
+    const int f = blockIdx.x;
+    A += f * sA;
+    ipiv += (size_t)f * n;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int pr = n - k0, nb = kend - k0;
+    for (int e = tid; e < pr * nb; e += PANEL_THREADS) {
+        const int i = e % pr, c = e / pr;
+        P[e] = A[k0 + i + (size_t)(k0 + c) * lda];
+    }
+    __syncthreads();
+    // A(i, c) of the panel is P[(c - k0) * pr + i - k0]
+    for (int j = k0; j < kend; ++j) {
+        const T *col = P + (size_t)(j - k0) * pr;           // col[i - k0] = A(i, j)
+        R best = -1;
+        int bi = n;
+        for (int i = j + tid; i < n; i += PANEL_THREADS) {
+            T a = col[i - k0];
+            R v = fabs(a.x) + fabs(a.y);
+            if (v > best) { best = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            R ov = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { sval[wid] = best; sidx[wid] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            R bv = sval[0];
+            int bidx = sidx[0];
+            for (int w = 1; w < PANEL_THREADS / 32; ++w)
+                if (sval[w] > bv || (sval[w] == bv && sidx[w] < bidx)) { bv = sval[w]; bidx = sidx[w]; }
+            if (!(bv > 0)) {
+                if (!(bv == 0)) info[f] |= IA_INFO_NONFINITE;
+                else info[f] |= IA_INFO_SINGULAR;
+                bidx = j;
+            }
+            s_piv = bidx;
+            ipiv[j] = bidx;
+        }
+        __syncthreads();
+        const int piv = s_piv;
+        if (piv != j) {
+            for (int c = tid; c < nb; c += PANEL_THREADS) {
+                T *pc = P + (size_t)c * pr;
+                T t = pc[j - k0];
+                pc[j - k0] = pc[piv - k0];
+                pc[piv - k0] = t;
+            }
+        }
+        __syncthreads();
+        T *cj = P + (size_t)(j - k0) * pr;
+        T d = cj[j - k0];
+        if (d.x != 0 || d.y != 0) {
+            T inv = zdiv(ctraits<T>::make(1, 0), d);
+            for (int i = j + 1 + tid; i < n; i += PANEL_THREADS) cj[i - k0] = zmul(cj[i - k0], inv);
+        }
+        __syncthreads();
+        const int rows = n - j - 1, ncols = kend - j - 1;
+        for (int idx = tid; idx < rows * ncols; idx += PANEL_THREADS) {
+            int r = j + 1 + idx % rows;
+            int c = j + 1 + idx / rows;
+            T *pc = P + (size_t)(c - k0) * pr;
+            T v = pc[r - k0];
+            zfms(v, cj[r - k0], pc[j - k0]);
+            pc[r - k0] = v;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < pr * nb; e += PANEL_THREADS) {
+        const int i = e % pr, c = e / pr;
+        A[k0 + i + (size_t)(k0 + c) * lda] = P[e];
+    }
+}
+
+// apply the interchanges ipiv[k0..kend) to every column outside [k0, kend)
+template <class T>
+__global__ void lu_laswp_kernel(int n, T *A, int lda, long long sA, const int *ipiv, int k0, int kend)
+{
+    const int f = blockIdx.y;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n - (kend - k0)) return;
+    if (c >= k0) c += kend - k0;
+    T *a = A + f * sA + (size_t)c * lda;
+    const int *pv = ipiv + (size_t)f * n;
+    for (int j = k0; j < kend; ++j) {
+        const int p = pv[j];
+        if (p != j) {
+            T t = a[j];
+            a[j] = a[p];
+            a[p] = t;
+        }
+    }
+}
+
 // Solve T X = X in place for an nbk x nbk diagonal block T (lower unit or
 // upper non-unit) and X = nbk x ncols; one thread per column.
 template <class T, bool UPPER>
@@ -280,11 +393,27 @@ template <class T>
 int getrf_batched(ia_context *ctx, int n, T *A, int lda, long long sA, int *ipiv, int *info, int batch)
 {
     const T one = ctraits<T>::make(1, 0), mone = ctraits<T>::make(-1, 0);
+    constexpr size_t kPanelSmemMax = 200 * 1024;
+    const bool smem_panel = (size_t)n * LU_NB * sizeof(T) <= kPanelSmemMax;
+    if (smem_panel)
+        IA_CUDA_TRY(cudaFuncSetAttribute(lu_panel_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kPanelSmemMax));
     for (int k0 = 0; k0 < n; k0 += LU_NB) {
         int kend = k0 + LU_NB < n ? k0 + LU_NB : n;
         int nb = kend - k0;
-        lu_panel_kernel<T><<<batch, PANEL_THREADS, 0, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend, info);
-        IA_LAUNCH_CHECK(ctx);
+        if (smem_panel) {
+            const size_t smem = (size_t)(n - k0) * nb * sizeof(T);
+            lu_panel_smem_kernel<T><<<batch, PANEL_THREADS, smem, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend, info);
+            IA_LAUNCH_CHECK(ctx);
+            if (n > nb) {
+                dim3 gs((n - nb + 127) / 128, batch);
+                lu_laswp_kernel<T><<<gs, 128, 0, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend);
+                IA_LAUNCH_CHECK(ctx);
+            }
+        } else {
+            lu_panel_kernel<T><<<batch, PANEL_THREADS, 0, ctx->stream>>>(n, A, lda, sA, ipiv, k0, kend, info);
+            IA_LAUNCH_CHECK(ctx);
+        }
         int rest = n - kend;
         if (rest <= 0) break;
         dim3 g((rest + 127) / 128, batch);

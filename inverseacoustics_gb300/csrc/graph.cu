@@ -19,6 +19,9 @@ int ia_capture_begin(ia_context *ctx)
     if (!ctx || ctx->capturing) return IA_ERR_ARG;
     if (ctx->stream == nullptr || ctx->stream == cudaStreamLegacy || ctx->stream == cudaStreamPerThread)
         return IA_ERR_ARG;
+    // the side stream of split pipelines exists before the capture starts
+    int st = ensure_side_stream(ctx);
+    if (st) return st;
     IA_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->capturing = 1;
     return IA_OK;

@@ -13,7 +13,15 @@ struct ia_context {
     long long launches;    // kernels launched through this context
     int sm_count;
     int capturing;         // between ia_capture_begin and ia_capture_end
+    // second stream and events of the staggered two-half IBEM pipeline,
+    // created at its first use or by ia_capture_begin (ensure_side_stream)
+    cudaStream_t side;
+    cudaEvent_t ev_split[2];
 };
+
+namespace ia {
+int ensure_side_stream(ia_context *ctx);
+}
 
 // threads per CTA of the IBEM assembly kernel; mesh colours are balanced to it
 #define IA_ASM_THREADS 128
