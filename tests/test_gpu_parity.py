@@ -242,6 +242,31 @@ def test_ibem_pipeline_matches_oracle_and_is_deterministic(cuda, ctx):
         assert relerr(x[f, 0].cpu().numpy(), xo) < 1e-9
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision):
+    """F = 16 runs as two staggered halves of 8 on two streams; each half
+    equals a plain 8-bin call bit for bit (bins stay in assembly blocks of 4,
+    later kernels work per bin)."""
+    from inverseacoustics_gb300 import api
+    import torch
+    nodes, elems = g.icosphere(2, 0.1)
+    rng = np.random.default_rng(19)
+    mics = g.hemisphere_array(rng, 40, 0.3)
+    ks = 2 * np.pi * np.linspace(200.0, 1800.0, 16) / 343.0
+    p = np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0), 30.0)[None, :] for k in ks])
+    mesh = api.Mesh(ctx, nodes, elems)
+    cfg = api.default_config(precision=precision)
+    md, kd, pd = T(mics, cuda), T(ks, cuda), T(p, cuda)
+    x, lam, s, info = api.ibem_solve_batch(ctx, mesh, md, kd, pd, cfg)
+    parts = [api.ibem_solve_batch(ctx, mesh, md, kd[h:h + 8].contiguous(), pd[h:h + 8].contiguous(), cfg)
+             for h in (0, 8)]
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0
+    for h, (xh, lh, sh, ih) in zip((0, 8), parts):
+        assert torch.equal(x[h:h + 8], xh) and torch.equal(lam[h:h + 8], lh) and torch.equal(s[h:h + 8], sh)
+        assert torch.equal(info[h:h + 8], ih)
+
+
 def test_hels_pipeline_matches_oracle(cuda, ctx):
     from inverseacoustics_gb300 import api
     import torch
