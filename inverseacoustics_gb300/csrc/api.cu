@@ -484,6 +484,23 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
     up((void **)&M->d_qnrm, qnrm.data(), sizeof(double) * qnrm.size());
     up((void **)&M->d_qdat_f, qdat_f.data(), sizeof(float) * qdat_f.size());
     up((void **)&M->d_qnrm_f, qnrm_f.data(), sizeof(float) * qnrm_f.size());
+    {
+        // (sin, cos)(j pi / 128) as double-float pairs, evaluated in long
+        // double (x86 extended or Arm quad) so the argument carries more
+        // bits than the FP64 result
+        const long double pi_l = 3.14159265358979323846264338327950288L;
+        std::vector<float> tab(4 * 256);
+        for (int j = 0; j < 256; ++j) {
+            const long double t = (long double)j * pi_l / 128.0L;
+            const double s = (double)sinl(t), c = (double)cosl(t);
+            const float sh = (float)s, ch = (float)c;
+            tab[4 * j] = sh;
+            tab[4 * j + 1] = (float)(s - (double)sh);
+            tab[4 * j + 2] = ch;
+            tab[4 * j + 3] = (float)(c - (double)ch);
+        }
+        up((void **)&M->d_dftab, tab.data(), sizeof(float) * tab.size());
+    }
     // node-node pattern (nodes sharing an element, the node itself included),
     // CSR with sorted columns: the sparsity of the surface mass matrix
     {
@@ -528,6 +545,7 @@ int ia_mesh_destroy(ia_mesh *M)
     cudaFree(M->d_qnrm);
     cudaFree(M->d_qdat_f);
     cudaFree(M->d_qnrm_f);
+    cudaFree(M->d_dftab);
     free(M);
     return IA_OK;
 }

@@ -133,7 +133,8 @@ __device__ __forceinline__ void df_sincos(double theta, const DfTrigCoef &C, dfl
 //
 // theta = N pi/128 + u with N = rint(theta 128/pi) and |u| <= ~pi/256;
 // sin/cos(N pi/128) come from a 256-entry table (N mod 256) held in shared
-// memory as (sin hi, sin lo, cos hi, cos lo), filled by sincospi; sin u and
+// memory as (sin hi, sin lo, cos hi, cos lo), computed once per mesh on the
+// host in extended precision and copied in by each CTA; sin u and
 // cos u by their Taylor series to u^7 and u^8 (terms below 1e-17 dropped);
 // then the angle-sum formulas.  pi/128 is carried as p0 + p1 + p2 + p3 with
 // p0..p2 of 12 significant bits, so N p_i is exact for |N| < 4096 and the
@@ -175,17 +176,6 @@ __host__ inline DfTrigRed df_trig_reduction_constants()
     r.c2h = (float)c2;
     r.c2l = (float)(c2 - (double)r.c2h);
     return r;
-}
-
-// tab[j] = (sin, cos)(j pi / 128) as double-float pairs
-__device__ inline void df_trig_table_fill(float4 *tab, int tid, int nthreads)
-{
-    for (int j = tid; j < 256; j += nthreads) {
-        double s, c;
-        sincospi((double)j / 128.0, &s, &c);
-        const float sh = __double2float_rn(s), ch = __double2float_rn(c);
-        tab[j] = make_float4(sh, __double2float_rn(s - (double)sh), ch, __double2float_rn(c - (double)ch));
-    }
 }
 
 __device__ __forceinline__ dfl df_add_f(dfl a, float b)

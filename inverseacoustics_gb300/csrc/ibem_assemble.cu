@@ -146,7 +146,9 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
 }
 
 // Singular-rule integral of one element (raw geometry eg, rule SoA) against
-// x_o, lanes striding the points, FP64; the caller reduces over the warp.
+// x_o, FP64; the caller reduces over the warp.  With nq <= 16 the lanes split
+// as (point, half of the frequency block): each lane evaluates half the
+// frequencies, so all 32 lanes work; otherwise lanes stride the points.
 __device__ __forceinline__ void singular_element(const double *__restrict__ eg, const double *__restrict__ rule, int nq,
                                                  double xo, double yo, double zo, const FreqBlock &fb, int lane,
                                                  double2 (&a)[IBEM_FB][3], double2 (&b)[IBEM_FB][3], double &ct)
@@ -155,7 +157,10 @@ __device__ __forceinline__ void singular_element(const double *__restrict__ eg, 
     const double v1x = eg[3], v1y = eg[4], v1z = eg[5];
     const double v2x = eg[6], v2y = eg[7], v2z = eg[8];
     const double nx = eg[9], ny = eg[10], nz = eg[11], an = eg[12];
-    for (int q = lane; q < nq; q += 32) {
+    const bool halves = nq <= 16;
+    const int q0 = halves ? (lane & 15) : lane, qstep = halves ? 16 : 32;
+    const int fh = halves ? (lane >> 4) * (IBEM_FB / 2) : 0, fcount = halves ? IBEM_FB / 2 : IBEM_FB;
+    for (int q = q0; q < nq; q += qstep) {
         const double x1 = rule[q], x2 = rule[q + nq], w = rule[q + 2 * nq] * IA_INV4PI;
         const double x3 = 1.0 - x1 - x2;
         const double dx = x1 * v0x + x2 * v1x + x3 * v2x - xo;
@@ -165,11 +170,12 @@ __device__ __forceinline__ void singular_element(const double *__restrict__ eg, 
         const double invr = rsqrt(r2);
         const double r = r2 * invr;
         const double ft = (nx * dx + ny * dy + nz * dz) * (invr * invr);
-        ct = fma(-w * ft, invr, ct);
+        if (fh == 0) ct = fma(-w * ft, invr, ct);
         const double N[3] = {x1, x2, x3};
 #pragma unroll
         for (int f = 0; f < IBEM_FB; ++f) {
             if (f >= fb.nf) break;
+            if (f < fh || f >= fh + fcount) continue;
             double s, c;
             sincos(fb.k[f] * r, &s, &c);
             const double gr = c * invr, gi = s * invr;
@@ -214,8 +220,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
-    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, int split_ab, double2 *__restrict__ At,
-    double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
+    const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, const float4 *__restrict__ dftab,
+    int split_ab, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
+    double2 *__restrict__ Bhs_t)
 {
     extern __shared__ __align__(16) unsigned char ibem_smem[];
     cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // IBEM_FB x (A row, B row), m each
@@ -240,7 +247,8 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     for (int f = 0; f < IBEM_FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
     const R dkf = r_of_double<R>(fb.dk);
     for (int j = tid; j < 2 * IBEM_FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
-    if (DF) df_trig_table_fill(tab, tid, blockDim.x);
+    if (DF)
+        for (int j = tid; j < 256; j += blockDim.x) tab[j] = dftab[j];
     double xo, yo, zo;
     int self = -1;
     if (row < m) {
@@ -390,14 +398,15 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
-            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, split_ab ? 1 : 0, At, Bt, Ahs_t, Bhs_t);
+            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0, At, Bt, Ahs_t,
+            Bhs_t);
     } else {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
             mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics,
-            cp, k, c, rho, coef, red, 0, At, Bt, Ahs_t, Bhs_t);
+            cp, k, c, rho, coef, red, nullptr, 0, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
