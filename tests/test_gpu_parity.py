@@ -242,18 +242,21 @@ def test_ibem_pipeline_matches_oracle_and_is_deterministic(cuda, ctx):
         assert relerr(x[f, 0].cpu().numpy(), xo) < 1e-9
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision):
+@pytest.mark.parametrize("precision,uniform,nrhs", [(0, True, 1), (1, True, 1), (1, False, 2)])
+def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, uniform, nrhs):
     """F = 16 runs as two staggered halves of 8 on two streams; each half
     equals a plain 8-bin call bit for bit (bins stay in assembly blocks of 4,
-    later kernels work per bin)."""
+    later kernels work per bin) -- evenly spaced bins (phase recurrence in
+    the assembly) and scattered ones, one and two right-hand sides."""
     from inverseacoustics_gb300 import api
     import torch
     nodes, elems = g.icosphere(2, 0.1)
     rng = np.random.default_rng(19)
     mics = g.hemisphere_array(rng, 40, 0.3)
-    ks = 2 * np.pi * np.linspace(200.0, 1800.0, 16) / 343.0
-    p = np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0), 30.0)[None, :] for k in ks])
+    f = np.linspace(200.0, 1800.0, 16) if uniform else np.sort(rng.uniform(150.0, 1900.0, 16))
+    ks = 2 * np.pi * f / 343.0
+    p = np.stack([np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0 + r), 30.0)
+                            for r in range(nrhs)]) for k in ks])
     mesh = api.Mesh(ctx, nodes, elems)
     cfg = api.default_config(precision=precision)
     md, kd, pd = T(mics, cuda), T(ks, cuda), T(p, cuda)
