@@ -37,7 +37,13 @@
 
 namespace ia {
 
-constexpr int IBEM_FB = 4;          // frequencies per CTA
+// Frequencies per CTA.  FP64: 4, so the geometry and the singular-element
+// work of the slow FP64 pipe serve four frequencies.  Double-float: 2, which
+// halves the accumulators (146 instead of 244 registers) and the row buffers,
+// for 3 CTAs per SM instead of 2 (measured 13.1 -> 11.7 ms per 64-bin launch).
+constexpr int IBEM_FB_MAX = 4;
+template <class R> struct AsmBlock { static constexpr int FB = 4; };
+template <> struct AsmBlock<dfl> { static constexpr int FB = 2; };
 constexpr int IBEM_THREADS = IA_ASM_THREADS;   // 4 warps; mesh colours are balanced to this
 constexpr int IBEM_MAX_NQ = 64;
 
@@ -91,7 +97,7 @@ template <class R> __device__ __forceinline__ cx<R> cx_norm(cx<R> a) { return cx
 
 // per-frequency phase factors of one block
 struct FreqBlock {
-    double k[IBEM_FB];
+    double k[IBEM_FB_MAX];
     double dk;
     int nf;
     bool uniform;
@@ -100,11 +106,11 @@ struct FreqBlock {
 // Regular-rule integral of one element against x_o for the block's
 // frequencies.  qd: precomputed (x, y, z, wa0..2, wb0..2) for each point,
 // structure of arrays with stride n (elements) and 9 * n per point.
-template <class R>
+template <class R, int FB>
 __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
-                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[IBEM_FB], R dkf,
+                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[FB], R dkf,
                                                 const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C,
-                                                cx<R> (&a)[IBEM_FB][3], cx<R> (&b)[IBEM_FB][3], R &ct)
+                                                cx<R> (&a)[FB][3], cx<R> (&b)[FB][3], R &ct)
 {
     for (int q = 0; q < nq; ++q) {
         const R *p = qd + (size_t)q * 9 * n + e;
@@ -124,7 +130,7 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
 #pragma unroll
         for (int v = 0; v < 3; ++v) sa[v] = r_mul(wa[v], ft);
 #pragma unroll
-        for (int f = 0; f < IBEM_FB; ++f) {
+        for (int f = 0; f < FB; ++f) {
             if (f >= fb.nf) break;
             if (f > 0) {
                 if (fb.uniform) ph = cx_mul(ph, step);
@@ -149,17 +155,18 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
 // x_o, FP64; the caller reduces over the warp.  With nq <= 16 the lanes split
 // as (point, half of the frequency block): each lane evaluates half the
 // frequencies, so all 32 lanes work; otherwise lanes stride the points.
+template <int FB>
 __device__ __forceinline__ void singular_element(const double *__restrict__ eg, const double *__restrict__ rule, int nq,
                                                  double xo, double yo, double zo, const FreqBlock &fb, int lane,
-                                                 double2 (&a)[IBEM_FB][3], double2 (&b)[IBEM_FB][3], double &ct)
+                                                 double2 (&a)[FB][3], double2 (&b)[FB][3], double &ct)
 {
     const double v0x = eg[0], v0y = eg[1], v0z = eg[2];
     const double v1x = eg[3], v1y = eg[4], v1z = eg[5];
     const double v2x = eg[6], v2y = eg[7], v2z = eg[8];
     const double nx = eg[9], ny = eg[10], nz = eg[11], an = eg[12];
-    const bool halves = nq <= 16;
+    const bool halves = nq <= 16 && FB >= 2;
     const int q0 = halves ? (lane & 15) : lane, qstep = halves ? 16 : 32;
-    const int fh = halves ? (lane >> 4) * (IBEM_FB / 2) : 0, fcount = halves ? IBEM_FB / 2 : IBEM_FB;
+    const int fh = halves ? (lane >> 4) * (FB / 2) : 0, fcount = halves ? FB / 2 : FB;
     for (int q = q0; q < nq; q += qstep) {
         const double x1 = rule[q], x2 = rule[q + nq], w = rule[q + 2 * nq] * IA_INV4PI;
         const double x3 = 1.0 - x1 - x2;
@@ -173,7 +180,7 @@ __device__ __forceinline__ void singular_element(const double *__restrict__ eg, 
         if (fh == 0) ct = fma(-w * ft, invr, ct);
         const double N[3] = {x1, x2, x3};
 #pragma unroll
-        for (int f = 0; f < IBEM_FB; ++f) {
+        for (int f = 0; f < FB; ++f) {
             if (f >= fb.nf) break;
             if (f < fh || f >= fh + fcount) continue;
             double s, c;
@@ -224,29 +231,30 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     int split_ab, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
     double2 *__restrict__ Bhs_t)
 {
+    constexpr int FB = AsmBlock<R>::FB;
     extern __shared__ __align__(16) unsigned char ibem_smem[];
-    cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // IBEM_FB x (A row, B row), m each
+    cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // FB x (A row, B row), m each
     constexpr bool DF = std::is_same<R, dfl>::value;
-    float4 *tab = DF ? reinterpret_cast<float4 *>(rowbuf + 2 * IBEM_FB * (size_t)m) : nullptr;   // sin/cos table
+    float4 *tab = DF ? reinterpret_cast<float4 *>(rowbuf + 2 * FB * (size_t)m) : nullptr;   // sin/cos table
     __shared__ double ct_red[IBEM_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int row = blockIdx.x;
-    const int f0 = blockIdx.y * IBEM_FB;
+    const int f0 = blockIdx.y * FB;
     const int mt = m + n_ch;
     FreqBlock fb;
-    fb.nf = F - f0 < IBEM_FB ? F - f0 : IBEM_FB;
+    fb.nf = F - f0 < FB ? F - f0 : FB;
 #pragma unroll
-    for (int f = 0; f < IBEM_FB; ++f) fb.k[f] = kv[f0 + (f < fb.nf ? f : fb.nf - 1)];
+    for (int f = 0; f < FB; ++f) fb.k[f] = kv[f0 + (f < fb.nf ? f : fb.nf - 1)];
     fb.dk = fb.nf > 1 ? fb.k[1] - fb.k[0] : 0.0;
     fb.uniform = true;
 #pragma unroll
-    for (int f = 2; f < IBEM_FB; ++f)
+    for (int f = 2; f < FB; ++f)
         if (f < fb.nf && fabs(fb.k[f] - (fb.k[0] + f * fb.dk)) > 1e-12 * fabs(fb.k[f])) fb.uniform = false;
-    R kf[IBEM_FB];
+    R kf[FB];
 #pragma unroll
-    for (int f = 0; f < IBEM_FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
+    for (int f = 0; f < FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
     const R dkf = r_of_double<R>(fb.dk);
-    for (int j = tid; j < 2 * IBEM_FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
+    for (int j = tid; j < 2 * FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
     if (DF)
         for (int j = tid; j < 256; j += blockDim.x) tab[j] = dftab[j];
     double xo, yo, zo;
@@ -269,9 +277,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         for (int e = e0 + tid; e < e1; e += blockDim.x) {
             const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
             if (vv.x == self || vv.y == self || vv.z == self) continue;
-            cx<R> a[IBEM_FB][3], b[IBEM_FB][3];
+            cx<R> a[FB][3], b[FB][3];
 #pragma unroll
-            for (int f = 0; f < IBEM_FB; ++f)
+            for (int f = 0; f < FB; ++f)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
             regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, dkf,
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
-            for (int f = 0; f < IBEM_FB; ++f) {
+            for (int f = 0; f < FB; ++f) {
                 if (f >= fb.nf) break;
                 cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
 #pragma unroll
@@ -297,9 +305,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         const int a0 = adj_ptr[self], a1 = adj_ptr[self + 1];
         for (int base = a0; base < a1; base += IBEM_THREADS / 32) {
             const int ai = base + wid;
-            double2 a[IBEM_FB][3], b[IBEM_FB][3];
+            double2 a[FB][3], b[FB][3];
 #pragma unroll
-            for (int f = 0; f < IBEM_FB; ++f)
+            for (int f = 0; f < FB; ++f)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = make_double2(0.0, 0.0); b[f][v] = make_double2(0.0, 0.0); }
             int e = -1, slot = 0;
@@ -314,7 +322,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             for (int w = 0; w < IBEM_THREADS / 32; ++w) {
                 if (w == wid && e >= 0) {
 #pragma unroll
-                    for (int f = 0; f < IBEM_FB; ++f)
+                    for (int f = 0; f < FB; ++f)
 #pragma unroll
                         for (int v = 0; v < 3; ++v) {
                             a[f][v] = warp_sum2(a[f][v]);
@@ -324,7 +332,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
                         const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
                         const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
-                        for (int f = 0; f < IBEM_FB; ++f) {
+                        for (int f = 0; f < FB; ++f) {
                             if (f >= fb.nf) break;
                             cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
 #pragma unroll
@@ -388,11 +396,12 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
     const int rows = m + n_ch + l;
-    const size_t smem = sizeof(double2) * 2 * (size_t)m * IBEM_FB + (df32 ? 256 * sizeof(float4) : 0);
+    const int FB = df32 ? AsmBlock<dfl>::FB : AsmBlock<double>::FB;
+    const size_t smem = sizeof(double2) * 2 * (size_t)m * FB + (df32 ? 256 * sizeof(float4) : 0);
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
     static const DfTrigCoef coef = df_trig_coefficients();
     static const DfTrigRed red = df_trig_reduction_constants();
-    dim3 g(rows, (F + IBEM_FB - 1) / IBEM_FB);
+    dim3 g(rows, (F + FB - 1) / FB);
     if (df32) {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
