@@ -786,8 +786,9 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     // halves on two streams, the second starting when the first one's
     // assembly is done, so that the latency-bound stages of one half (LU
     // panels, Jacobi, QR, one CTA per frequency) run beside the
-    // throughput-bound stages of the other.  Frequencies stay in blocks of 4
-    // in the assembly and every later kernel works per frequency, so the
+    // throughput-bound stages of the other.  Frequencies stay in the
+    // assembly's blocks (4 bins in FP64, 1 in double-float; halves are
+    // multiples of 4) and every later kernel works per frequency, so the
     // results are bitwise those of one F-bin pass.
     const bool split = F >= 16 && F % 8 == 0;
     const int Fh = split ? F / 2 : F;

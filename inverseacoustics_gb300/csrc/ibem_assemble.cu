@@ -38,12 +38,14 @@
 namespace ia {
 
 // Frequencies per CTA.  FP64: 4, so the geometry and the singular-element
-// work of the slow FP64 pipe serve four frequencies.  Double-float: 2, which
-// halves the accumulators (146 instead of 244 registers) and the row buffers,
-// for 3 CTAs per SM instead of 2 (measured 13.1 -> 11.7 ms per 64-bin launch).
+// work of the slow FP64 pipe serve four frequencies.  Double-float: 1 -- the
+// accumulators of a block dominate the registers (244 at 4, 146 at 2, 96 at
+// 1) and the row buffers the shared memory, so one frequency per CTA runs 5
+// CTAs per SM instead of 2, which outweighs recomputing the geometry per
+// frequency (measured per 64-bin launch: 13.1 ms at 4, 11.7 at 2, 11.0 at 1).
 constexpr int IBEM_FB_MAX = 4;
 template <class R> struct AsmBlock { static constexpr int FB = 4; };
-template <> struct AsmBlock<dfl> { static constexpr int FB = 2; };
+template <> struct AsmBlock<dfl> { static constexpr int FB = 1; };
 constexpr int IBEM_THREADS = IA_ASM_THREADS;   // 4 warps; mesh colours are balanced to this
 constexpr int IBEM_MAX_NQ = 64;
 

@@ -245,7 +245,7 @@ def test_ibem_pipeline_matches_oracle_and_is_deterministic(cuda, ctx):
 @pytest.mark.parametrize("precision,uniform,nrhs", [(0, True, 1), (1, True, 1), (1, False, 2)])
 def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, uniform, nrhs):
     """F = 16 runs as two staggered halves of 8 on two streams; each half
-    equals a plain 8-bin call bit for bit (bins stay in assembly blocks of 4,
+    equals a plain 8-bin call bit for bit (bins stay in their assembly blocks,
     later kernels work per bin) -- evenly spaced bins (phase recurrence in
     the assembly) and scattered ones, one and two right-hand sides."""
     from inverseacoustics_gb300 import api
