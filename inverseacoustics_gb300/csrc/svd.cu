@@ -246,6 +246,89 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 2 * SVD_MAX_WARPS * 32 : SVD_
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
 }
 
+// The shared-memory iteration with a half-warp per pair (M, N <= 128): each
+// lane holds 8 rows of both columns, the sums reduce over 16 lanes, and a
+// 32-warp CTA works all 64 pairs of a round at once instead of two pairs per
+// warp one after the other.  Same rotation order as jacobi_smem_kernel.
+template <class T>
+__device__ __forceinline__ typename ctraits<T>::R half_sum(typename ctraits<T>::R v, unsigned mask)
+{
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    return v;
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) jacobi_half_kernel(int M, int Mdot, int N, T *Yg, long long sY,
+                                                            int max_sweeps, typename ctraits<T>::R tol, int *info)
+{
+    typedef typename ctraits<T>::R R;
+    constexpr int KPL = 8;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *Y = reinterpret_cast<T *>(smraw);
+    __shared__ int s_rot;
+    const int f = blockIdx.x;
+    Yg += f * sY;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int half = lane >> 4, hl = lane & 15;
+    const unsigned mask = half ? 0xffff0000u : 0x0000ffffu;
+    const int N2 = N + (N & 1);
+    const T zero = ctraits<T>::make(0, 0);
+    for (int e = threadIdx.x; e < M * N; e += blockDim.x) Y[e] = Yg[e];
+    __syncthreads();
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) s_rot = 0;
+        __syncthreads();
+        int rot_local = 0;
+        for (int round = 0; round < N2 - 1; ++round) {
+            for (int k = 2 * wid + half; k < N2 / 2; k += 2 * nw) {
+                int i, j;
+                rr_pair(N2, round, k, i, j);
+                if (j >= N) continue;
+                T *yi = Y + (size_t)i * M, *yj = Y + (size_t)j * M;
+                R a = 0, b = 0, c;
+                T g = zero, sp;
+                T ui[KPL], uj[KPL];
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    int r = hl + 16 * t;
+                    ui[t] = r < M ? yi[r] : zero;
+                    uj[t] = r < M ? yj[r] : zero;
+                    if (r < Mdot) {
+                        a += zabs2(ui[t]);
+                        b += zabs2(uj[t]);
+                        zcfma(g, ui[t], uj[t]);
+                    }
+                }
+                a = half_sum<T>(a, mask);
+                b = half_sum<T>(b, mask);
+                g.x = half_sum<T>(g.x, mask);
+                g.y = half_sum<T>(g.y, mask);
+                if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    int r = hl + 16 * t;
+                    if (r < M) {
+                        rotate_pair(ui[t], uj[t], c, sp);
+                        yi[r] = ui[t];
+                        yj[r] = uj[t];
+                    }
+                }
+                rot_local++;
+            }
+            __syncthreads();
+        }
+        if (hl == 0 && rot_local) atomicAdd(&s_rot, rot_local);
+        __syncthreads();
+        int total = s_rot;
+        __syncthreads();
+        if (total == 0) break;
+    }
+    for (int e = threadIdx.x; e < M * N; e += blockDim.x) Yg[e] = Y[e];
+    if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
+}
+
 template <class T>
 __global__ void identity_kernel(int N, T *V, long long sV)
 {
@@ -277,7 +360,22 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;
     const size_t smem = sizeof(T) * (size_t)M * N;
-    if (M <= 128 && N <= 128 && smem <= 200 * 1024) {
+    bool done = false;
+    if constexpr (sizeof(T) == sizeof(float2)) {
+        if (!V && M <= 128 && N <= 128 && smem <= 200 * 1024) {
+            // FP32 without accumulator: a half-warp per pair, every pair of a round at once
+            const int pairs = (N + (N & 1)) / 2;
+            int nws = (pairs + 1) / 2;
+            if (nws > 32) nws = 32;
+            if (nws < 1) nws = 1;
+            IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_half_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024));
+            jacobi_half_kernel<T><<<batch, nws * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, max_sweeps, tol, info);
+            done = true;
+        }
+    }
+    if (done) {
+    } else if (M <= 128 && N <= 128 && smem <= 200 * 1024) {
         const int wmax = sizeof(T) <= 8 ? 2 * SVD_MAX_WARPS : SVD_MAX_WARPS;
         int nws = (N + 1) / 2 < wmax ? (N + 1) / 2 : wmax;
         if (nws < 1) nws = 1;
