@@ -32,12 +32,18 @@ constexpr int QR_THREADS = 512;
 // One CTA per matrix.  Column j: reflector H_j = I - tau v v^H, v(0) = 1
 // (LAPACK zlarfg convention, beta = -sign(Re alpha) ||x||), stored below the
 // diagonal; H_j^H applied to the trailing columns of A and to every column of
-// B (B may be null).  tau may be null.
-template <class T>
+// B (B may be null).  tau may be null.  KPL > 0 (rows <= 1 + 32 KPL, dynamic
+// shared memory of rows elements): the reflector is kept in shared memory and
+// each trailing column's segment in registers, so a column costs one round of
+// independent loads instead of a dependent load per element; the arithmetic
+// and its order are those of KPL = 0.
+template <class T, int KPL>
 __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A, int lda, long long sA, T *tau,
                                                         int nrhs, T *B, int ldb, long long sB)
 {
     typedef typename ctraits<T>::R R;
+    extern __shared__ __align__(16) unsigned char qr_smem[];
+    T *xs = reinterpret_cast<T *>(qr_smem);   // the scaled reflector (KPL > 0)
     __shared__ R red[QR_THREADS / 32];
     __shared__ T s_tau;
     __shared__ T s_scale;   // 1/(alpha - beta)
@@ -74,7 +80,11 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A
         __syncthreads();
         const T tv = s_tau, sc = s_scale;
         if (tv.x == 0 && tv.y == 0) continue;
-        for (int i = 1 + tid; i < len; i += QR_THREADS) x[i] = zmul(x[i], sc);
+        for (int i = 1 + tid; i < len; i += QR_THREADS) {
+            const T xv = zmul(x[i], sc);
+            x[i] = xv;
+            if (KPL > 0) xs[i] = xv;
+        }
         __syncthreads();
         const T ctau = zconj(tv);
         const int ntrail = cols - j - 1;
@@ -82,30 +92,68 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A
         for (int c = wid; c < ntot; c += nw) {
             T *col = c < ntrail ? A + j + (size_t)(j + 1 + c) * lda : B + j + (size_t)(c - ntrail) * ldb;
             T w = lane == 0 ? col[0] : zero;
-            for (int i = 1 + lane; i < len; i += 32) zcfma(w, x[i], col[i]);
-            w = warp_sum2(w);
-            w = zmul(ctau, w);
-            if (lane == 0) col[0] = zsub(col[0], w);
-            for (int i = 1 + lane; i < len; i += 32) zfms(col[i], x[i], w);
+            if (KPL > 0) {
+                T v[KPL > 0 ? KPL : 1];
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    const int i = 1 + lane + 32 * t;
+                    v[t] = i < len ? col[i] : zero;
+                }
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    const int i = 1 + lane + 32 * t;
+                    if (i < len) zcfma(w, xs[i], v[t]);
+                }
+                w = warp_sum2(w);
+                w = zmul(ctau, w);
+                if (lane == 0) col[0] = zsub(col[0], w);
+#pragma unroll
+                for (int t = 0; t < KPL; ++t) {
+                    const int i = 1 + lane + 32 * t;
+                    if (i < len) {
+                        zfms(v[t], xs[i], w);
+                        col[i] = v[t];
+                    }
+                }
+            } else {
+                for (int i = 1 + lane; i < len; i += 32) zcfma(w, x[i], col[i]);
+                w = warp_sum2(w);
+                w = zmul(ctau, w);
+                if (lane == 0) col[0] = zsub(col[0], w);
+                for (int i = 1 + lane; i < len; i += 32) zfms(col[i], x[i], w);
+            }
         }
         __syncthreads();
     }
 }
 
+// KPL = 24 covers rows <= 769 (the bench's 642-row H^H)
+constexpr int QR_KPL = 24;
+
+template <class T>
+static int qr_launch(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int nrhs, T *B,
+                     int ldb, long long sB, int batch)
+{
+    if (rows <= 1 + 32 * QR_KPL) {
+        qr_kernel<T, QR_KPL><<<batch, QR_THREADS, sizeof(T) * (size_t)rows, ctx->stream>>>(rows, cols, A, lda, sA, tau,
+                                                                                        nrhs, B, ldb, sB);
+    } else {
+        qr_kernel<T, 0><<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, tau, nrhs, B, ldb, sB);
+    }
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
 int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
                    int ldb, long long sB, int batch)
 {
-    qr_kernel<double2><<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, nullptr, nrhs, B, ldb, sB);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
+    return qr_launch<double2>(ctx, rows, cols, A, lda, sA, nullptr, nrhs, B, ldb, sB, batch);
 }
 
 template <class T>
 int qr_batched(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int batch)
 {
-    qr_kernel<T><<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, tau, 0, nullptr, 0, 0);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
+    return qr_launch<T>(ctx, rows, cols, A, lda, sA, tau, 0, nullptr, 0, 0, batch);
 }
 template int qr_batched<float2>(ia_context *, int, int, float2 *, int, long long, float2 *, int);
 template int qr_batched<double2>(ia_context *, int, int, double2 *, int, long long, double2 *, int);
@@ -286,11 +334,8 @@ int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *
     if (transposed) st = zcopy2d_batched(ctx, n, m, A, n, sA, Y, Mr, (long long)Mr * N, true, batch);
     else st = ztranspose_batched(ctx, m, n, A, m, sA, Y, Mr, (long long)Mr * N, true, batch);
     if (st) return st;
-    if (qr) {
-        qr_kernel<double2><<<batch, QR_THREADS, 0, ctx->stream>>>(Mr, N, Y, Mr, (long long)Mr * N, tau, 0, nullptr, 0,
-                                                                  0);
-        IA_LAUNCH_CHECK(ctx);
-    }
+    if (qr && (st = qr_launch<double2>(ctx, Mr, N, Y, Mr, (long long)Mr * N, tau, 0, nullptr, 0, 0, batch)))
+        return st;
     {
         long long total = (long long)(N + nrhs) * N;
         int blocks = (int)((total + 255) / 256);
@@ -673,10 +718,7 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
         if (!st) st = copy2d_batched<double2, float2>(ctx, Mr, N, Yd, Mr, sY, Y, Mr, sY, false, batch);
     }
     if (st) return st;
-    if (qr) {
-        qr_kernel<float2><<<batch, QR_THREADS, 0, ctx->stream>>>(Mr, N, Y, Mr, sY, tau, 0, nullptr, 0, 0);
-        IA_LAUNCH_CHECK(ctx);
-    }
+    if (qr && (st = qr_launch<float2>(ctx, Mr, N, Y, Mr, sY, tau, 0, nullptr, 0, 0, batch))) return st;
     {
         long long total = (long long)N * N;
         int blocks = (int)((total + 255) / 256);
