@@ -282,6 +282,46 @@ def _bench_bem_modes(ctx, dev, stream, flush, mesh, w, reps=2):
             "info_clean": int(i1.abs().sum() + i0.abs().sum()) == 0}
 
 
+def _bench_selectors(ctx, dev, stream, flush, mesh, w, p_np, reps=3):
+    """The λ selectors on the headline workload's 64 transfer matrices
+    (120 x 642): the batched solve (SVD / eigen-refinement, selector,
+    filter, back-projection) per method, mixed path, and the selected λ
+    against the FP64 path's."""
+    import torch
+
+    from inverseacoustics_gb300 import api
+    mics = torch.as_tensor(w.arrays["mics"], device=dev)
+    k = torch.as_tensor(w.k, device=dev)
+    b = torch.as_tensor(p_np, device=dev)
+    H, _ = api.ibem_transfer_batch(ctx, mesh, mics, k, api.default_config(precision=1))
+    F, n, m = H.shape
+    res = {}
+    for name, method in (("tikhonov_gcv", 0), ("tikhonov_lcurve", 3), ("tikhonov_quasiopt", 4),
+                         ("tsvd_k36", 1), ("dsvd_lcurve", 6)):
+        out = {}
+        for prec in (1, 0):
+            cfg = api.default_config(precision=prec, method=method, tsvd_k=36)
+            api.solve_batch(ctx, H, m, n, b, cfg)
+            times = []
+            for _ in range(reps):
+                flush.zero_()
+                a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                x, lam, s, info = api.solve_batch(ctx, H, m, n, b, cfg)
+                e.record(stream)
+                e.synchronize()
+                times.append(a.elapsed_time(e))
+            out[prec] = (sum(times) / reps, x, lam, info)
+        ms, x1, l1, i1 = out[1]
+        ms64, x0, l0, i0 = out[0]
+        rel = float(((x1 - x0).abs().pow(2).sum((1, 2)).sqrt() / x0.abs().pow(2).sum((1, 2)).sqrt()).max())
+        res[name] = {"ms": ms, "value": F / (ms / 1000.0), "fp64_ms": ms64,
+                     "lambda_mixed_vs_fp64": float(((l1 - l0).abs() / l0.abs().clamp_min(1e-300)).max()),
+                     "x_mixed_vs_fp64": rel, "info_clean": int(i1.abs().sum() + i0.abs().sum()) == 0}
+    return {"workload": f"ibem_sphere_transfer_{m}x{n}_F{F}", "unit": "freq-solves/s (solve only, mixed)",
+            "note": "dsvd_* runs the FP64 solve under IA_PREC_MIXED", "methods": res}
+
+
 def _bench_admm(ctx, dev, stream, flush, w, fp64_peak, reps=2):
     """ADMM L1 inversion (MATLAB/ADMMG.m) of the sphere's monopole transfer
     matrices: 120 microphones, 642 equivalent sources, 64 frequencies, Nm = 50
@@ -506,6 +546,7 @@ def run_ours(args):
         side = (("radiation_modes", lambda: _bench_radiation(ctx, dev, stream, flush)),
                 ("esm_design_adjoint", lambda: _bench_design(ctx, dev, stream, flush)),
                 ("bem_modes", lambda: _bench_bem_modes(ctx, dev, stream, flush, mesh, w)),
+                ("lambda_selectors", lambda: _bench_selectors(ctx, dev, stream, flush, mesh, w, p_np)),
                 ("admm_l1", lambda: _bench_admm(ctx, dev, stream, flush, w, fp64_tflops_dgemm)))
         for name, fn in side:
             try:
