@@ -259,8 +259,9 @@ __device__ __forceinline__ typename ctraits<T>::R half_sum(typename ctraits<T>::
 }
 
 template <class T>
-__global__ void __launch_bounds__(1024) jacobi_half_kernel(int M, int Mdot, int N, T *Yg, long long sY,
-                                                            int max_sweeps, typename ctraits<T>::R tol, int *info)
+__global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
+    jacobi_half_kernel(int M, int Mdot, int N, T *Yg, long long sY, int max_sweeps, typename ctraits<T>::R tol,
+                       int *info)
 {
     typedef typename ctraits<T>::R R;
     constexpr int KPL = 8;
@@ -360,21 +361,19 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     const R tol = (R)(sqrt((double)Mdot) * eps);
     const long long sY = (long long)M * N, sV = (long long)N * N;
     const size_t smem = sizeof(T) * (size_t)M * N;
-    bool done = false;
-    if constexpr (sizeof(T) == sizeof(float2)) {
-        if (!V && M <= 128 && N <= 128 && smem <= 200 * 1024) {
-            // FP32 without accumulator: a half-warp per pair, every pair of a round at once
-            const int pairs = (N + (N & 1)) / 2;
-            int nws = (pairs + 1) / 2;
-            if (nws > 32) nws = 32;
-            if (nws < 1) nws = 1;
-            IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_half_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             200 * 1024));
-            jacobi_half_kernel<T><<<batch, nws * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, max_sweeps, tol, info);
-            done = true;
-        }
-    }
-    if (done) {
+    // without accumulator: a half-warp per pair (FP32: every pair of a round at
+    // once in 32 warps; FP64: 16 warps, the 128-register budget), Y in shared
+    // memory up to the per-CTA limit (an FP64 121 x 120 system fits)
+    const size_t half_smem_max = sizeof(T) <= 8 ? 200 * 1024 : 227 * 1024 - 64;   // 16 B static besides
+    if (!V && M <= 128 && N <= 128 && smem <= half_smem_max) {
+        const int pairs = (N + (N & 1)) / 2;
+        const int wcap = sizeof(T) <= 8 ? 32 : 16;
+        int nws = (pairs + 1) / 2;
+        if (nws > wcap) nws = wcap;
+        if (nws < 1) nws = 1;
+        IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_half_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)half_smem_max));
+        jacobi_half_kernel<T><<<batch, nws * 32, smem, ctx->stream>>>(M, Mdot, N, Y, sY, max_sweeps, tol, info);
     } else if (M <= 128 && N <= 128 && smem <= 200 * 1024) {
         const int wmax = sizeof(T) <= 8 ? 2 * SVD_MAX_WARPS : SVD_MAX_WARPS;
         int nws = (N + 1) / 2 < wmax ? (N + 1) / 2 : wmax;
