@@ -18,9 +18,11 @@
 // invr.cuh:904,907 take n_am as the inner dimension of the output products
 // (so only n_am = m gives H U and Z U); here every product has the sizes
 // invrS.m gives.  Real variant: left singular vectors by subspace iteration on
-// R R^T (radiation.cu).  Complex variant: one-sided Jacobi SVD of G Z (svd.cu),
-// each column's phase fixed so that its first component within 1e-6 of the
-// largest magnitude is real and positive.
+// R R^T (radiation.cu).  Complex variant: one-sided Jacobi SVD of G Z (svd.cu)
+// in FP64; in mixed precision subspace iteration on the real representation
+// of (G Z)(G Z)^H (radiation.cu again) and one complex vector per doubled
+// eigenvalue.  Each complex column's phase is fixed so that its first
+// component within 1e-6 of the largest magnitude is real and positive.
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -91,9 +93,31 @@ __global__ void modes_finish_kernel(size_t nsv, const double *__restrict__ lam, 
     }
 }
 
-// complex variant: the leading nm columns of each m x m U (and the leading nm
-// singular values), each column multiplied by the unit phase that makes its
-// first component within 1e-6 of the largest magnitude real and positive.
+// unit phase that makes a column's first component within 1e-6 of the largest
+// magnitude real and positive (warp-cooperative; every lane gets the phase)
+__device__ double2 column_phase(int m, const double2 *u, int lane)
+{
+    double best = 0.0;
+    for (int i = lane; i < m; i += 32) best = fmax(best, hypot(u[i].x, u[i].y));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+    const double thr = best * (1.0 - 1e-6);
+    int bi = m;
+    for (int i = lane; i < m; i += 32)
+        if (hypot(u[i].x, u[i].y) >= thr) { bi = i; break; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bi = min(bi, __shfl_xor_sync(0xffffffffu, bi, o));
+    double2 ph = make_double2(1.0, 0.0);
+    if (bi < m) {
+        const double2 p = u[bi];
+        const double a = hypot(p.x, p.y);
+        if (a > 0.0) ph = make_double2(p.x / a, -p.y / a);
+    }
+    return ph;
+}
+
+// complex variant (FP64): the leading nm columns of each m x m U and the
+// leading nm singular values, each column multiplied by its unit phase.
 // Block per frequency, warp per column.
 __global__ void modes_phase_kernel(int m, int nm, const double2 *__restrict__ U, const double *__restrict__ sfull,
                                    double2 *__restrict__ Uc, double *__restrict__ sr)
@@ -102,25 +126,155 @@ __global__ void modes_phase_kernel(int m, int nm, const double2 *__restrict__ U,
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = wid; j < nm; j += nw) {
         const double2 *u = U + ((size_t)f * m + j) * m;
-        double best = 0.0;
-        for (int i = lane; i < m; i += 32) best = fmax(best, hypot(u[i].x, u[i].y));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
-        const double thr = best * (1.0 - 1e-6);
-        int bi = m;
-        for (int i = lane; i < m; i += 32)
-            if (hypot(u[i].x, u[i].y) >= thr) { bi = i; break; }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) bi = min(bi, __shfl_xor_sync(0xffffffffu, bi, o));
-        double2 ph = make_double2(1.0, 0.0);
-        if (bi < m) {
-            const double2 p = u[bi];
-            const double a = hypot(p.x, p.y);
-            if (a > 0.0) ph = make_double2(p.x / a, -p.y / a);
-        }
+        const double2 ph = column_phase(m, u, lane);
         double2 *dst = Uc + ((size_t)f * nm + j) * m;
         for (int i = lane; i < m; i += 32) dst[i] = zmul(u[i], ph);
         if (lane == 0) sr[(size_t)f * nm + j] = sfull[(size_t)f * m + j];
+    }
+}
+
+// complex variant (mixed): the real representation Yr = [[Re Y, -Im Y],
+// [Im Y, Re Y]] (2m x 2m, column-major) of Y = G Z.  Yr Yr^T represents
+// Y Y^H: every eigenvalue of Y Y^H appears twice, with the eigenvectors
+// [Re u; Im u] and [-Im u; Re u] (the images of u and i u).
+__global__ void real_rep_kernel(int m, const double2 *__restrict__ Y, double *__restrict__ Yr, int batch)
+{
+    const size_t n = 2 * (size_t)m, per = n * n;
+    const size_t total = per * batch, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += stride) {
+        const size_t f = e / per, o = e % per;
+        const int r = (int)(o % n), c = (int)(o / n);
+        const int i = r < m ? r : r - m, j = c < m ? c : c - m;
+        const double2 y = Y[f * (size_t)m * m + i + (size_t)j * m];
+        Yr[e] = (r < m) == (c < m) ? y.x : (r < m ? -y.y : y.y);
+    }
+}
+
+// Complex modes from the nc leading real Ritz vectors V (2m x nc, Ritz values
+// lam descending) of the real representation.  A candidate v gives the complex
+// vector w = v(0:m) + i v(m:2m).  Ritz values within 1e-12 lam_1 of a
+// cluster's first one form the cluster: its r real vectors span (the image
+// of) r/2 complex dimensions, each eigenvalue's pair [Re u; Im u],
+// [-Im u; Re u] giving u and i u.  Per cluster, up to ceil(r/2) times: the
+// free candidate with the largest squared residual against the accepted modes
+// (ties to the lower index; none above 0.1 ends the cluster) is
+// orthogonalised (two classical Gram-Schmidt passes), normalised and accepted
+// with s = sqrt(max(lam, 0)).  Picking the largest residual keeps a cluster's
+// last complex direction reachable however the Ritz vectors split it (a
+// first-come rule with a threshold can spend it on earlier rejects).  Accepted
+// columns get the unit phase of the FP64 variant; fewer than nm accepted flags
+// IA_INFO_NOCONV (the rest zero).  Block per frequency.
+constexpr int PICK_THREADS = 256;
+
+__global__ void __launch_bounds__(PICK_THREADS) modes_pick_kernel(int m, int nm, int nc,
+                                                                  const double *__restrict__ V,
+                                                                  const double *__restrict__ lam,
+                                                                  double2 *__restrict__ Uc, double *__restrict__ sr,
+                                                                  int *__restrict__ info)
+{
+    extern __shared__ __align__(16) double2 pk_w[];              // m: candidate
+    double2 *dots = pk_w + m;                                     // nm
+    double *res = reinterpret_cast<double *>(dots + nm);          // nc
+    int *taken = reinterpret_cast<int *>(res + nc);               // nc
+    __shared__ double red[PICK_THREADS / 32];
+    __shared__ int s_pick;
+    const int f = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    const size_t n2 = 2 * (size_t)m;
+    V += (size_t)f * n2 * nc;
+    lam += (size_t)f * nc;
+    Uc += (size_t)f * nm * m;
+    sr += (size_t)f * nm;
+    for (int c = tid; c < nc; c += blockDim.x) taken[c] = 0;
+    const double ctol = 1e-12 * fmax(lam[0], 0.0);
+    __syncthreads();
+    int acc = 0, c0 = 0;
+    while (c0 < nc && acc < nm) {
+        int c1 = c0 + 1;
+        while (c1 < nc && lam[c0] - lam[c1] <= ctol) ++c1;
+        const int q = (c1 - c0 + 1) / 2;
+        for (int t = 0; t < q && acc < nm; ++t) {
+            for (int c = c0 + wid; c < c1; c += nw) {
+                if (taken[c]) {
+                    if (lane == 0) res[c] = -1.0;
+                    continue;
+                }
+                const double *v = V + (size_t)c * n2;
+                double nr = 0.0;
+                for (int i = lane; i < m; i += 32) nr = fma(v[i], v[i], fma(v[m + i], v[m + i], nr));
+                nr = warp_sum(nr);
+                double pr = 0.0;
+                for (int k = 0; k < acc; ++k) {
+                    const double2 *u = Uc + (size_t)k * m;
+                    double2 d = make_double2(0.0, 0.0);
+                    for (int i = lane; i < m; i += 32) zcfma(d, u[i], make_double2(v[i], v[m + i]));
+                    d = warp_sum2(d);
+                    pr += zabs2(d);
+                }
+                if (lane == 0) res[c] = nr - pr;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int best = -1;
+                double bv = 0.1;
+                for (int c = c0; c < c1; ++c)
+                    if (res[c] > bv) {
+                        bv = res[c];
+                        best = c;
+                    }
+                s_pick = best;
+            }
+            __syncthreads();
+            const int pick = s_pick;
+            if (pick < 0) break;
+            const double *v = V + (size_t)pick * n2;
+            for (int i = tid; i < m; i += blockDim.x) pk_w[i] = make_double2(v[i], v[m + i]);
+            __syncthreads();
+            for (int pass = 0; pass < 2; ++pass) {
+                for (int k = wid; k < acc; k += nw) {
+                    const double2 *u = Uc + (size_t)k * m;
+                    double2 d = make_double2(0.0, 0.0);
+                    for (int i = lane; i < m; i += 32) zcfma(d, u[i], pk_w[i]);     // u^H w
+                    d = warp_sum2(d);
+                    if (lane == 0) dots[k] = d;
+                }
+                __syncthreads();
+                for (int i = tid; i < m; i += blockDim.x) {
+                    double2 w = pk_w[i];
+                    for (int k = 0; k < acc; ++k) zfms(w, dots[k], Uc[(size_t)k * m + i]);
+                    pk_w[i] = w;
+                }
+                __syncthreads();
+            }
+            double nr = 0.0;
+            for (int i = tid; i < m; i += blockDim.x) nr += zabs2(pk_w[i]);
+            nr = warp_sum(nr);
+            if (lane == 0) red[wid] = nr;
+            __syncthreads();
+            double tot = 0.0;
+            for (int w = 0; w < nw; ++w) tot += red[w];
+            const double sc = 1.0 / sqrt(tot);
+            for (int i = tid; i < m; i += blockDim.x) Uc[(size_t)acc * m + i] = zscale(pk_w[i], sc);
+            if (tid == 0) {
+                sr[acc] = sqrt(fmax(lam[pick], 0.0));
+                taken[pick] = 1;
+            }
+            ++acc;
+            __syncthreads();
+        }
+        c0 = c1;
+    }
+    for (int k = acc; k < nm; ++k) {
+        for (int i = tid; i < m; i += blockDim.x) Uc[(size_t)k * m + i] = make_double2(0.0, 0.0);
+        if (tid == 0) sr[k] = 0.0;
+    }
+    if (tid == 0 && acc < nm && info) atomicOr(&info[f], IA_INFO_NOCONV);
+    __syncthreads();
+    for (int k = wid; k < acc; k += nw) {
+        double2 *u = Uc + (size_t)k * m;
+        const double2 ph = column_phase(m, u, lane);
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) u[i] = zmul(u[i], ph);
     }
 }
 
@@ -135,13 +289,44 @@ __global__ void df_join_kernel(size_t count, const float4 *__restrict__ in, doub
 
 static bool bem_mixed_solve(const ia_config *cfg, int n_ch) { return cfg->precision == IA_PREC_MIXED && n_ch == 0; }
 
+// Subspace of the mixed complex variant, on the real representation (every
+// eigenvalue doubled): 2 (nm + max(nm, mode_oversample)) real vectors, all
+// returned as Ritz vectors (a cluster of equal eigenvalues that straddles the
+// 2 nm-th one needs candidates beyond it), 2 mode_iters FP32 and
+// 4 max(1, refine_steps) FP64-level iterations.  The spectrum of G Z is dense
+// (singular values of a 642-node sphere fall only to 0.15 s_1 by the 32nd),
+// so the real variant's settings would stop near 1e-7 s_1; these reach
+// ~1e-15 s_1 and residuals ~1e-11 lambda_1 there.
+struct ComplexModeSub {
+    ia_config cfg;
+    int nr;   // real Ritz vectors
+};
+
+static ComplexModeSub complex_mode_sub(const ia_config *cfg, int m, int nm)
+{
+    ComplexModeSub c{*cfg, 0};
+    const int p = cfg->mode_oversample > nm ? cfg->mode_oversample : nm;
+    c.nr = nm + p < m ? 2 * (nm + p) : 2 * m;
+    c.cfg.mode_oversample = 0;
+    c.cfg.mode_iters = 2 * cfg->mode_iters;
+    c.cfg.refine_steps = 4 * (cfg->refine_steps > 1 ? cfg->refine_steps : 1);
+    return c;
+}
+
 size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, const ia_config *cfg, bool cplx)
 {
     const size_t M = mesh->m, MT = M + n_ch, L = l, FF = F;
     size_t b = 4 * ws_round(16 * MT * M * FF) + 4 * ws_round(16 * M * L * FF) + ws_round(4 * M * FF) +
                ws_round(8 * (size_t)mesh->gnnz) + ws_round(16 * M * nm * FF);
-    if (cplx) b += ws_round(16 * M * M * FF) + ws_round(8 * M * FF);
-    else b += ws_round(8 * M * M * FF) + ws_round(8 * nm * FF) + radiation_modes_ws_bytes(mesh->m, F, nm, cfg, true);
+    if (cplx) {
+        b += ws_round(16 * M * M * FF) + ws_round(8 * M * FF);
+        if (cfg->precision == IA_PREC_MIXED) {
+            const ComplexModeSub c = complex_mode_sub(cfg, mesh->m, nm);
+            const size_t NR = c.nr;
+            b += ws_round(32 * M * M * FF) + ws_round(16 * M * NR * FF) + ws_round(8 * NR * FF) +
+                 radiation_modes_ws_bytes(2 * mesh->m, F, c.nr, &c.cfg, true);
+        }
+    } else b += ws_round(8 * M * M * FF) + ws_round(8 * nm * FF) + radiation_modes_ws_bytes(mesh->m, F, nm, cfg, true);
     if (bem_mixed_solve(cfg, n_ch)) b += 2 * ws_round(8 * M * M * FF) + ws_round(16 * M * M * FF);
     return b + 4096;
 }
@@ -240,15 +425,34 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
     IA_LAUNCH_CHECK(ctx);
     const dim3 gz_grid((m + 127) / 128, m, F);
     if (cplx) {
-        // SVD of G Z: columns of Y orthogonalised in place, U = Y / sigma
         double2 *Y = cur.take<double2>(mm * F);
         double *sfull = cur.take<double>((size_t)m * F);
-        double2 *Ufull = Bt;
         gz_kernel<true><<<gz_grid, 128, 0, ctx->stream>>>(m, mesh->d_gptr, mesh->d_gidx, gval, Z, m, mm, Y);
         IA_LAUNCH_CHECK(ctx);
-        if ((st = jacobi_svd_batched(ctx, m, m, Y, nullptr, F, cfg->svd_max_sweeps, info))) return st;
-        if ((st = svd_finalize_batched(ctx, m, m, Y, nullptr, sfull, Ufull, nullptr, F, info))) return st;
-        modes_phase_kernel<<<F, 256, 0, ctx->stream>>>(m, nm, Ufull, sfull, Uc, sr);
+        if (cfg->precision == IA_PREC_MIXED) {
+            // subspace iteration on the real representation (radiation.cu),
+            // then one complex vector per doubled eigenvalue
+            const ComplexModeSub c = complex_mode_sub(cfg, m, nm);
+            const int n2 = 2 * m;
+            double *Yr = cur.take<double>((size_t)n2 * n2 * F);
+            double *V2 = cur.take<double>((size_t)n2 * c.nr * F);
+            double *lam2 = cur.take<double>((size_t)c.nr * F);
+            real_rep_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(m, Y, Yr, F);
+            IA_LAUNCH_CHECK(ctx);
+            if ((st = radiation_modes_batched(ctx, n2, F, Yr, c.nr, &c.cfg, lam2, V2, info, cur, true))) return st;
+            const size_t smem = sizeof(double2) * ((size_t)m + nm) + (sizeof(double) + sizeof(int)) * (size_t)c.nr;
+            if (smem > 227 * 1024) return IA_ERR_TOO_LARGE;
+            if (smem > 48 * 1024)
+                IA_CUDA_TRY(cudaFuncSetAttribute(modes_pick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem));
+            modes_pick_kernel<<<F, PICK_THREADS, smem, ctx->stream>>>(m, nm, c.nr, V2, lam2, Uc, sr, info);
+        } else {
+            // FP64 SVD of Y: columns orthogonalised in place, U = Y / sigma
+            double2 *Ufull = Bt;
+            if ((st = jacobi_svd_batched(ctx, m, m, Y, nullptr, F, cfg->svd_max_sweeps, info))) return st;
+            if ((st = svd_finalize_batched(ctx, m, m, Y, nullptr, sfull, Ufull, nullptr, F, info))) return st;
+            modes_phase_kernel<<<F, 256, 0, ctx->stream>>>(m, nm, Ufull, sfull, Uc, sr);
+        }
         IA_LAUNCH_CHECK(ctx);
     } else {
         // left singular vectors of R = Re(G Z): eigenvectors of R R^T

@@ -183,7 +183,10 @@ size_t wide_solve_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                        const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                        WsCursor &cur);
-// mixed: QR / Jacobi / GCV in FP32, x by FP64 iterative refinement against A
+// mixed solve: eigenvectors X and eigenvalues of H H^H from an FP32 QR +
+// one-sided Jacobi start, double-float Ogita-Aishima steps, Newton-Schulz and
+// an FP64 two-sided Jacobi on X^H (H H^H) X; then s, U^H b, GCV and the
+// back-projection
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                              const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,

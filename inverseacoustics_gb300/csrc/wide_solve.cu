@@ -675,17 +675,28 @@ __global__ void eig_backproject_kernel(int m, int n, int N, const double2 *H, in
     }
 }
 
-size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
+static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
 {
-    const size_t F = batch, N = m, M = n, R = nrhs;
+    const size_t F = batch, N = m, M = n;
     return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
-           7 * ws_round(16 * N * N * F) + 2 * ws_round(8 * N * F) + ws_round(4 * N * F) +
-           2 * ws_round(16 * R * N * F) + ws_round(8 * R * F) + 8192;
+           7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + 4096;
 }
 
-int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
-                             const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
-                             int *info, WsCursor &cur)
+size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
+{
+    const size_t F = batch, N = m, R = nrhs;
+    return gram_eig_mixed_ws_bytes(m, n, batch) + ws_round(8 * N * F) + ws_round(4 * N * F) +
+           2 * ws_round(16 * R * N * F) + ws_round(8 * R * F) + 4096;
+}
+
+// Steps 1-4 of the mixed solve: eigenvectors X (m x m, columns in no
+// particular order) and eigenvalues lam_e (m) of E = A A^H for A (m x n,
+// column-major), or of conj(E) for the transposed input (A^T stored, n x m):
+// FP32 QR (n > m) and one-sided Jacobi, double-float E and Ogita-Aishima steps,
+// Newton-Schulz, FP64 S = X^H E X and the two-sided Jacobi on its coupled
+// pairs.  *Xout and *lam_out point into the workspace taken from cur.
+static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed,
+                          const ia_config *cfg, double2 **Xout, double **lam_out, int *info, WsCursor &cur)
 {
     const int N = m, Mr = n;
     const bool qr = n > m;
@@ -703,11 +714,6 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     double2 *Rm = cur.take<double2>(NN * batch);
     double2 *Fc = cur.take<double2>(NN * batch);
     double *lam_e = cur.take<double>((size_t)N * batch);
-    double *s = s_out ? s_out : cur.take<double>((size_t)N * batch);
-    int *rank = cur.take<int>((size_t)N * batch);
-    double2 *beta = cur.take<double2>((size_t)nrhs * N * batch);
-    double2 *z = cur.take<double2>((size_t)nrhs * N * batch);
-    double *lam = lambda ? lambda : cur.take<double>((size_t)nrhs * batch);
     const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
     // 1. FP32 start: Y = H^H, QR, Jacobi with J accumulated
@@ -761,7 +767,10 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     // 4. pairs of near-equal eigenvalues stay coupled through the first-order
     // steps (the refinement treats them as a cluster): orthonormalise X
     // (Newton-Schulz, X <- 1.5 X - 0.5 X X^H X), form S = X^H E X in FP64 and
-    // rotate the coupled pairs apart with two-sided Jacobi; lam_e <- diag(S)
+    // rotate the coupled pairs apart with two-sided Jacobi; lam_e <- diag(S).
+    // Suited to spectra with few clusters (a transfer matrix's decaying
+    // singular values): on a dense clustered spectrum (the radiation operator
+    // of a sphere) the first-order steps stall and the Jacobi does a full sweep.
     if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
     if ((st = zcopy2d_batched(ctx, N, N, X, N, sN, Xn, N, sN, false, batch))) return st;
     if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, -0.5, X, N, sN, Rm, N, sN, 1.5, Xn, N, sN, batch))) return st;
@@ -779,6 +788,25 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
         herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
         IA_LAUNCH_CHECK(ctx);
     }
+    *Xout = X;
+    *lam_out = lam_e;
+    return IA_OK;
+}
+
+int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
+                             const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
+                             int *info, WsCursor &cur)
+{
+    const int N = m;
+    double2 *X;
+    double *lam_e;
+    int st = gram_eig_mixed(ctx, m, n, batch, A, transposed, cfg, &X, &lam_e, info, cur);
+    if (st) return st;
+    double *s = s_out ? s_out : cur.take<double>((size_t)N * batch);
+    int *rank = cur.take<int>((size_t)N * batch);
+    double2 *beta = cur.take<double2>((size_t)nrhs * N * batch);
+    double2 *z = cur.take<double2>((size_t)nrhs * N * batch);
+    double *lam = lambda ? lambda : cur.take<double>((size_t)nrhs * batch);
     // 5. s, beta, GCV, back-projection
     eig_beta_kernel<<<batch, 256, 0, ctx->stream>>>(m, N, lam_e, X, transposed ? 1 : 0, nrhs, b, s, beta, rank);
     IA_LAUNCH_CHECK(ctx);

@@ -124,3 +124,25 @@ def test_admm_l1_recovers_monopole_sources(cuda, ctx):
         assert its[f, 0] == ito
         assert relerr(c[f, 0], co) < 1e-7
         assert set(np.argsort(-np.abs(c[f, 0]))[:3]) == set(true)
+
+
+def test_admm_and_bem_modes_reject_bad_arguments(cuda, ctx):
+    """Invalid configurations come back as IA_ERR_ARG before any device work."""
+    from inverseacoustics_gb300 import api
+    from inverseacoustics_gb300._lib import IAError
+    A, B, lam0 = _problems(40, 1, 1, 8, 20)
+    bad = [dict(norm=0), dict(norm=4), dict(rho=0.0), dict(rho=-1.0), dict(max_iters=-1), dict(epsilon=-1e-6),
+           dict(norm=3, p=0.0), dict(norm=3, p=1.5), dict(norm=3, gst_iters=-1), dict(precision=2)]
+    for kw in bad:
+        with pytest.raises(IAError) as e:
+            _run(ctx, cuda, A, B, lam0, api.default_admm_config(**kw))
+        assert e.value.code == 1, kw
+    nodes, elems = g.icosphere(1, 0.1)
+    mesh = api.Mesh(ctx, nodes, elems)
+    mics, k = T(g.hemisphere_array(np.random.default_rng(1), 8, 0.3), cuda), T(np.array([3.0]), cuda)
+    for nm in (0, nodes.shape[1] + 1):
+        for cplx in (False, True):
+            with pytest.raises(IAError) as e:
+                api.bem_modes_batch(ctx, mesh, mics, k, nm, complex_modes=cplx)
+            assert e.value.code == 1
+    mesh.close()
