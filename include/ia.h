@@ -354,11 +354,12 @@ int ia_bem_modes_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double
  * F x (m x nmodes) complex, each column's phase fixed so that its first
  * component within 1e-6 of its largest magnitude is real and positive (the
  * phase of a singular vector is arbitrary; zgesvd's is not reproduced).
- * IA_PREC_FP64: one-sided Jacobi SVD of the full G Z (cfg->svd_max_sweeps).
- * IA_PREC_MIXED: double-float assembly; the leading modes by subspace
- * iteration on the real representation of (G Z)(G Z)^H with
- * nmodes + max(nmodes, mode_oversample) vectors, 2 mode_iters FP32 and
- * 4 max(1, refine_steps) double-float iterations. */
+ * While p = nmodes + max(nmodes, mode_oversample) is at most m / 2, the
+ * leading modes by subspace iteration on the real representation of
+ * (G Z)(G Z)^H with p vectors: 2 mode_iters + 4 max(1, refine_steps) FP64
+ * iterations, or with IA_PREC_MIXED (double-float assembly) 2 mode_iters FP32
+ * and 4 max(1, refine_steps) double-float ones.  Otherwise the FP64 one-sided
+ * Jacobi SVD of the whole G Z (cfg->svd_max_sweeps). */
 int ia_bem_modes_complex_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
                                const double *d_cp, int F, const double *d_k, int nmodes, const ia_config *cfg,
                                ia_complex *d_Ur, double *d_sr, ia_complex *d_Hr, ia_complex *d_Pr, int *d_info);

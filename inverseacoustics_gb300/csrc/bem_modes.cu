@@ -18,11 +18,12 @@
 // invr.cuh:904,907 take n_am as the inner dimension of the output products
 // (so only n_am = m gives H U and Z U); here every product has the sizes
 // invrS.m gives.  Real variant: left singular vectors by subspace iteration on
-// R R^T (radiation.cu).  Complex variant: one-sided Jacobi SVD of G Z (svd.cu)
-// in FP64; in mixed precision subspace iteration on the real representation
-// of (G Z)(G Z)^H (radiation.cu again) and one complex vector per doubled
-// eigenvalue.  Each complex column's phase is fixed so that its first
-// component within 1e-6 of the largest magnitude is real and positive.
+// R R^T (radiation.cu).  Complex variant: subspace iteration on the real
+// representation of (G Z)(G Z)^H (radiation.cu again) and one complex vector
+// per doubled eigenvalue while the subspace is at most half the space, else
+// the one-sided Jacobi SVD of G Z (svd.cu).  Each complex column's phase is
+// fixed so that its first component within 1e-6 of the largest magnitude is
+// real and positive.
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -289,14 +290,14 @@ __global__ void df_join_kernel(size_t count, const float4 *__restrict__ in, doub
 
 static bool bem_mixed_solve(const ia_config *cfg, int n_ch) { return cfg->precision == IA_PREC_MIXED && n_ch == 0; }
 
-// Subspace of the mixed complex variant, on the real representation (every
+// Subspace of the complex variant, on the real representation (every
 // eigenvalue doubled): 2 (nm + max(nm, mode_oversample)) real vectors, all
 // returned as Ritz vectors (a cluster of equal eigenvalues that straddles the
-// 2 nm-th one needs candidates beyond it), 2 mode_iters FP32 and
-// 4 max(1, refine_steps) FP64-level iterations.  The spectrum of G Z is dense
-// (singular values of a 642-node sphere fall only to 0.15 s_1 by the 32nd),
-// so the real variant's settings would stop near 1e-7 s_1; these reach
-// ~1e-15 s_1 and residuals ~1e-11 lambda_1 there.
+// 2 nm-th one needs candidates beyond it).  Mixed: 2 mode_iters FP32 and
+// 4 max(1, refine_steps) double-float iterations; FP64: as many FP64 ones.
+// The spectrum of G Z is dense (singular values of a 642-node sphere fall
+// only to 0.15 s_1 by the 32nd), so the real variant's settings would stop
+// near 1e-7 s_1; these reach ~1e-15 s_1 and residuals ~1e-11 lambda_1 there.
 struct ComplexModeSub {
     ia_config cfg;
     int nr;   // real Ritz vectors
@@ -306,11 +307,25 @@ static ComplexModeSub complex_mode_sub(const ia_config *cfg, int m, int nm)
 {
     ComplexModeSub c{*cfg, 0};
     const int p = cfg->mode_oversample > nm ? cfg->mode_oversample : nm;
+    const int refine = 4 * (cfg->refine_steps > 1 ? cfg->refine_steps : 1);
     c.nr = nm + p < m ? 2 * (nm + p) : 2 * m;
     c.cfg.mode_oversample = 0;
-    c.cfg.mode_iters = 2 * cfg->mode_iters;
-    c.cfg.refine_steps = 4 * (cfg->refine_steps > 1 ? cfg->refine_steps : 1);
+    if (cfg->precision == IA_PREC_MIXED) {
+        c.cfg.mode_iters = 2 * cfg->mode_iters;
+        c.cfg.refine_steps = refine;
+    } else {
+        c.cfg.mode_iters = 2 * cfg->mode_iters + refine;
+    }
     return c;
+}
+
+// The subspace pays while it is at most half the space (2 (nm + p) <= m);
+// beyond that (invr with n_am near m) the complex variant takes the FP64
+// one-sided Jacobi SVD of the whole G Z.
+static bool complex_mode_subspace(const ia_config *cfg, int m, int nm)
+{
+    const int p = cfg->mode_oversample > nm ? cfg->mode_oversample : nm;
+    return 2 * (long long)(nm + p) <= m;
 }
 
 size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, const ia_config *cfg, bool cplx)
@@ -320,7 +335,7 @@ size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, c
                ws_round(8 * (size_t)mesh->gnnz) + ws_round(16 * M * nm * FF);
     if (cplx) {
         b += ws_round(16 * M * M * FF) + ws_round(8 * M * FF);
-        if (cfg->precision == IA_PREC_MIXED) {
+        if (complex_mode_subspace(cfg, mesh->m, nm)) {
             const ComplexModeSub c = complex_mode_sub(cfg, mesh->m, nm);
             const size_t NR = c.nr;
             b += ws_round(32 * M * M * FF) + ws_round(16 * M * NR * FF) + ws_round(8 * NR * FF) +
@@ -429,7 +444,7 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
         double *sfull = cur.take<double>((size_t)m * F);
         gz_kernel<true><<<gz_grid, 128, 0, ctx->stream>>>(m, mesh->d_gptr, mesh->d_gidx, gval, Z, m, mm, Y);
         IA_LAUNCH_CHECK(ctx);
-        if (cfg->precision == IA_PREC_MIXED) {
+        if (complex_mode_subspace(cfg, m, nm)) {
             // subspace iteration on the real representation (radiation.cu),
             // then one complex vector per doubled eigenvalue
             const ComplexModeSub c = complex_mode_sub(cfg, m, nm);

@@ -216,3 +216,17 @@ def test_bem_modes_complex_mixed_dense_spectrum(cuda, ctx):
             P = X[:, a:b] @ X[:, a:b].conj().T
             Po = Uo[:, a:b] @ Uo[:, a:b].conj().T
             assert np.linalg.norm(P - Po) < 1e-7, (f, a, b)
+
+
+def test_bem_modes_complex_mixed_many_modes(cuda, ctx, ellipsoid):
+    """Mixed complex variant with nm + max(nm, oversample) above m / 2: the
+    FP64 Jacobi SVD of the double-float G Z, so s agrees with the FP64 run to
+    the assembly's accuracy and the columns are orthonormal."""
+    nm = 90
+    s1, U1, _, _, info1 = _run(ctx, cuda, ellipsoid, nm, 1, True)
+    s0, U0, _, _, info0 = _run(ctx, cuda, ellipsoid, nm, 0, True)
+    assert int(np.abs(info1).sum()) == 0 and int(np.abs(info0).sum()) == 0
+    for f in range(len(ellipsoid[3])):
+        assert np.max(np.abs(s1[f] - s0[f])) <= 1e-10 * s0[f][0]
+        X = U1[f].T
+        assert np.max(np.abs(X.conj().T @ X - np.eye(nm))) < 1e-12
