@@ -248,8 +248,9 @@ def _bench_design(ctx, dev, stream, flush, reps=3):
 
 def _bench_bem_modes(ctx, dev, stream, flush, mesh, w, reps=2):
     """BEM radiation modes of the headline sphere (642 nodes, 120 field
-    points), 16 frequencies, 32 modes of Re(G Z): assembly, LU, G Z, subspace
-    iteration, modal transfer.  Mixed and FP64 timed."""
+    points), 16 frequencies, 32 modes of Re(G Z) and (complex_modes) of G Z
+    itself: assembly, LU, G Z, subspace iteration, modal transfer.  Mixed and
+    FP64 timed."""
     import torch
 
     from inverseacoustics_gb300 import api
@@ -274,12 +275,33 @@ def _bench_bem_modes(ctx, dev, stream, flush, mesh, w, reps=2):
     s1, _, H1, _, i1 = outs[1]
     s0, _, H0, _, i0 = outs[0]
     err_s2 = float(((s1 ** 2 - s0 ** 2).abs().amax(1) / s0[:, 0] ** 2).max())
+    # complex variant (the C++ invr() modes of G Z itself)
+    cres, couts = {}, {}
+    for prec in (1, 0):
+        cfg = api.default_config(precision=prec)
+        api.bem_modes_batch(ctx, mesh, mics, k, nm, cfg, complex_modes=True)
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            couts[prec] = api.bem_modes_batch(ctx, mesh, mics, k, nm, cfg, complex_modes=True)
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        cres[prec] = sum(times) / reps
+    cs1, cs0 = couts[1][0], couts[0][0]
+    err_cs = float(((cs1 - cs0).abs().amax(1) / cs0[:, 0]).max())
     return {"workload": f"bem_modes_sphere_{mesh.m}n_120fp_F{F}_modes{nm}", "frequencies": F,
             "value": F / (res[1] / 1000.0), "unit": "freq/s (assembly + Z + G Z + modes + H_r, P_r)",
             "fp64_value": F / (res[0] / 1000.0), "mixed_speedup": res[0] / res[1],
             "ms": {"mixed": res[1], "fp64": res[0]},
             "accuracy": {"s2_mixed_vs_fp64_rel_s1sq": err_s2},
-            "info_clean": int(i1.abs().sum() + i0.abs().sum()) == 0}
+            "info_clean": int(i1.abs().sum() + i0.abs().sum()) == 0,
+            "complex_modes": {"value": F / (cres[1] / 1000.0), "fp64_value": F / (cres[0] / 1000.0),
+                              "ms": {"mixed": cres[1], "fp64": cres[0]}, "mixed_speedup": cres[0] / cres[1],
+                              "accuracy": {"s_mixed_vs_fp64_rel_s1": err_cs},
+                              "info_clean": int(couts[1][4].abs().sum() + couts[0][4].abs().sum()) == 0}}
 
 
 def _bench_selectors(ctx, dev, stream, flush, mesh, w, p_np, reps=3):

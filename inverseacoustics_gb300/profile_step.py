@@ -4,12 +4,14 @@ workloads and code paths as bench.py's timed steps.
 
     python -m inverseacoustics_gb300.profile_step [--workload ibem|radiation|design|bemmodes|admm]
         [--precision mixed|fp64] [--reps 2] [--freqs 64] [--subdiv 3] [--admm-iters 50]
+        [--complex-modes]
 
 ibem: the IBEM sphere pipeline (642 nodes / 1280 triangles / 120 mics).
 radiation: the baffled plate (1280 elements, 192 mics): sinc R, 32 radiation
 modes, ESM TSVD reconstruction (k = 36), sound power.
 design: ESM array design (128 mics, 642 sources, 16 fields), forward + adjoint.
-bemmodes: BEM radiation modes of the IBEM sphere, 32 modes of Re(G Z).
+bemmodes: BEM radiation modes of the IBEM sphere, 32 modes of Re(G Z), or
+with --complex-modes of G Z itself (the C++ invr()).
 admm: L1 ADMM on the sphere's monopole transfer matrices (120 mics, 642
 sources), epsilon = 0: all 14 continuation stages of --admm-iters iterations.
 """
@@ -88,7 +90,7 @@ def _bemmodes(a, dev, api, g):
     cfg = api.default_config(precision=1 if a.precision == "mixed" else 0)
     out = None
     for _ in range(a.reps):
-        out = api.bem_modes_batch(ctx, mesh, md, kd, 32, cfg)
+        out = api.bem_modes_batch(ctx, mesh, md, kd, 32, cfg, complex_modes=a.complex_modes)
     torch.cuda.synchronize()
     return float(out[0].sum()), int(out[4].abs().sum())
 
@@ -128,6 +130,7 @@ def main():
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--freqs", type=int, default=None)
     ap.add_argument("--subdiv", type=int, default=3)
+    ap.add_argument("--complex-modes", action="store_true", help="bemmodes: modes of G Z instead of Re(G Z)")
     a = ap.parse_args()
     if a.freqs is None:
         a.freqs = {"ibem": 64, "radiation": 256, "design": 128, "bemmodes": 16, "admm": 64}[a.workload]
