@@ -6,6 +6,7 @@
 // CUDA/ibem.cuh:755; cublasZgemm CUDA/ibem.cuh:398; cublasZgeam
 // CUDA/esm.cuh:79).  Every launch covers the whole frequency batch (grid.z or
 // grid.x = batch).
+#include <type_traits>
 #include "ia_common.cuh"
 #include "ia_internal.h"
 #include "tune.h"
@@ -469,10 +470,150 @@ int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int l
     return IA_OK;
 }
 
+// Fused LU solve (FP32 complex): the row interchanges, the unit-lower L solve
+// and the upper U solve for GETRS_RB right-hand-side columns of one matrix per
+// CTA, in one launch, the n x GETRS_RB block of B in shared memory.  Block
+// steps of LU_NB rows: the diagonal block is staged in shared memory and
+// solved warp per column (lane per row, each solved entry broadcast by
+// shuffle); the rows below (forward) or above (backward) are then updated
+// thread per row, the block's LU_NB columns of L or U read coalesced from
+// global memory (L2).  Replaces 2 n / LU_NB dependent small launches (a
+// diagonal-block solve and a GEMM update per step) by one.
+constexpr int GETRS_RB = 8;
+constexpr int GETRS_THREADS = 32 * GETRS_RB;   // a warp per column in the diagonal solves
+
+__device__ __forceinline__ float2 shfl_c(float2 v, int src)
+{
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+__global__ void __launch_bounds__(GETRS_THREADS) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
+                                                                     int lda, long long sA,
+                                                                     const int *__restrict__ ipiv, float2 *B, int ldb,
+                                                                     long long sB)
+{
+    extern __shared__ __align__(16) unsigned char gf_smem[];
+    float2 *X = reinterpret_cast<float2 *>(gf_smem);                                  // n x GETRS_RB
+    float2(*D)[LU_NB + 1] = reinterpret_cast<float2(*)[LU_NB + 1]>(X + (size_t)n * GETRS_RB);
+    int *piv = reinterpret_cast<int *>(D + LU_NB);                                    // n
+    const int f = blockIdx.y, c0 = blockIdx.x * GETRS_RB;
+    const int nc = nrhs - c0 < GETRS_RB ? nrhs - c0 : GETRS_RB;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    LU += f * sA;
+    ipiv += (size_t)f * n;
+    B += f * sB + (size_t)c0 * ldb;
+    const float2 zero = make_float2(0.f, 0.f);
+    for (int e = tid; e < n * GETRS_RB; e += blockDim.x) {
+        const int i = e % n, c = e / n;
+        X[e] = c < nc ? B[i + (size_t)c * ldb] : zero;
+    }
+    for (int j = tid; j < n; j += blockDim.x) piv[j] = ipiv[j];
+    __syncthreads();
+    if (tid < GETRS_RB) {
+        float2 *x = X + (size_t)tid * n;
+        for (int j = 0; j < n; ++j) {
+            const int p = piv[j];
+            if (p != j) {
+                const float2 t = x[j];
+                x[j] = x[p];
+                x[p] = t;
+            }
+        }
+    }
+    __syncthreads();
+    // forward: L Y = P B
+    for (int k0 = 0; k0 < n; k0 += LU_NB) {
+        const int nb = n - k0 < LU_NB ? n - k0 : LU_NB, kend = k0 + nb;
+        for (int e = tid; e < nb * nb; e += blockDim.x) {
+            const int r = e % nb, cc = e / nb;
+            D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
+        }
+        __syncthreads();
+        {
+            float2 *x = X + (size_t)wid * n + k0;
+            float2 v = lane < nb ? x[lane] : zero;
+            for (int r = 0; r < nb; ++r) {
+                const float2 xr = shfl_c(v, r);
+                if (lane > r && lane < nb) zfms(v, D[lane][r], xr);
+            }
+            if (lane < nb) x[lane] = v;
+        }
+        __syncthreads();
+        for (int i = kend + tid; i < n; i += blockDim.x) {
+            float2 acc[GETRS_RB];
+#pragma unroll
+            for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
+            for (int t = 0; t < nb; ++t) {
+                const float2 l = LU[i + (size_t)(k0 + t) * lda];
+#pragma unroll
+                for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], l, X[k0 + t + (size_t)c * n]);
+            }
+#pragma unroll
+            for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];
+        }
+        __syncthreads();
+    }
+    // backward: U X = Y
+    for (int k0 = ((n - 1) / LU_NB) * LU_NB; k0 >= 0; k0 -= LU_NB) {
+        const int nb = n - k0 < LU_NB ? n - k0 : LU_NB;
+        for (int e = tid; e < nb * nb; e += blockDim.x) {
+            const int r = e % nb, cc = e / nb;
+            D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
+        }
+        __syncthreads();
+        {
+            float2 *x = X + (size_t)wid * n + k0;
+            float2 v = lane < nb ? x[lane] : zero;
+            for (int r = nb - 1; r >= 0; --r) {
+                if (lane == r) v = zdiv(v, D[r][r]);
+                const float2 xr = shfl_c(v, r);
+                if (lane < r) zfms(v, D[lane][r], xr);
+            }
+            if (lane < nb) x[lane] = v;
+        }
+        __syncthreads();
+        for (int i = tid; i < k0; i += blockDim.x) {
+            float2 acc[GETRS_RB];
+#pragma unroll
+            for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
+            for (int t = 0; t < nb; ++t) {
+                const float2 u = LU[i + (size_t)(k0 + t) * lda];
+#pragma unroll
+                for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], u, X[k0 + t + (size_t)c * n]);
+            }
+#pragma unroll
+            for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * nc; e += blockDim.x) {
+        const int i = e % n, c = e / n;
+        B[i + (size_t)c * ldb] = X[e];
+    }
+}
+
+static size_t getrs_fused_smem(int n)
+{
+    return sizeof(float2) * ((size_t)n * GETRS_RB + (size_t)LU_NB * (LU_NB + 1)) + sizeof(int) * (size_t)n;
+}
+
 template <class T>
 int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long long sA, const int *ipiv, T *B,
                   int ldb, long long sB, int batch)
 {
+    if (n <= 0 || nrhs <= 0 || batch <= 0) return IA_OK;
+    if constexpr (std::is_same<T, float2>::value) {
+        const size_t smem = getrs_fused_smem(n);
+        if (smem <= 200 * 1024) {
+            if (smem > 48 * 1024)
+                IA_CUDA_TRY(cudaFuncSetAttribute(getrs_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 200 * 1024));
+            dim3 gf((nrhs + GETRS_RB - 1) / GETRS_RB, batch);
+            getrs_fused_kernel<<<gf, GETRS_THREADS, smem, ctx->stream>>>(n, nrhs, LU, lda, sA, ipiv, B, ldb, sB);
+            IA_LAUNCH_CHECK(ctx);
+            return IA_OK;
+        }
+    }
     const T one = ctraits<T>::make(1, 0), mone = ctraits<T>::make(-1, 0);
     dim3 g((nrhs + 127) / 128, batch);
     apply_pivots_kernel<T><<<g, 128, 0, ctx->stream>>>(n, nrhs, ipiv, B, ldb, sB);

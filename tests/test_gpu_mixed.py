@@ -54,6 +54,29 @@ def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
         assert relerr(Hmx[f].cpu().numpy(), H64[f].cpu().numpy()) < 1e-11
 
 
+def test_mixed_transfer_fp32_solve_and_refinement_steps(cuda, ctx):
+    """The FP32 LU solve alone (refine_steps = 0) against FP64: H within the
+    FP32 level (1e-4, with the sphere's condition numbers); each double-float
+    refinement step then gains several digits (1e-8 after one, 1e-11 after
+    two).  Catches a wrong but refinement-masked FP32 solve."""
+    from inverseacoustics_gb300 import api
+    import torch
+    w = g.ibem_sphere(n_freq=64)
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    ks = w.k[[2, 30, 54]]
+    mesh = api.Mesh(ctx, nodes, elems)
+    H64, _ = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
+    errs = []
+    for steps in (0, 1, 2):
+        H, info = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda),
+                                          api.default_config(precision=1, refine_steps=steps))
+        torch.cuda.synchronize()
+        assert int(info.abs().sum()) == 0
+        errs.append(max(relerr(H[f].cpu().numpy(), H64[f].cpu().numpy()) for f in range(len(ks))))
+    assert errs[0] < 1e-4 and errs[1] < 1e-8 and errs[2] < 1e-11, errs
+    assert errs[1] < 1e-2 * errs[0]
+
+
 def test_mixed_ibem_pipeline_full_size(cuda, ctx):
     """Full bench configuration at 8 of its 64 frequencies (two next to the
     interior resonance): mixed x and lambda against the FP64 oracle."""
