@@ -36,24 +36,81 @@ constexpr int QR_THREADS = 512;
 // shared memory of rows elements): the reflector is kept in shared memory and
 // each trailing column's segment in registers, so a column costs one round of
 // independent loads instead of a dependent load per element; the arithmetic
-// and its order are those of KPL = 0.
-template <class T, int KPL>
+// and its order are those of KPL = 0.  PIV: column pivoting (perm).
+template <class T, int KPL, bool PIV>
 __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A, int lda, long long sA, T *tau,
-                                                        int nrhs, T *B, int ldb, long long sB)
+                                                        int nrhs, T *B, int ldb, long long sB, int *perm)
 {
     typedef typename ctraits<T>::R R;
     extern __shared__ __align__(16) unsigned char qr_smem[];
     T *xs = reinterpret_cast<T *>(qr_smem);   // the scaled reflector (KPL > 0)
+    R *cn = reinterpret_cast<R *>(qr_smem + (KPL > 0 ? sizeof(T) * (size_t)rows : 0));   // pivoting: column norms^2
+    int *idx = reinterpret_cast<int *>(cn + cols);                                        // pivoting: column order
     __shared__ R red[QR_THREADS / 32];
     __shared__ T s_tau;
     __shared__ T s_scale;   // 1/(alpha - beta)
+    __shared__ int s_piv;
     const int f = blockIdx.x;
     A += f * sA;
     if (B) B += f * sB;
     if (tau) tau += (size_t)f * cols;
+    if (PIV) perm += (size_t)f * cols;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = QR_THREADS / 32;
     const T zero = ctraits<T>::make(0, 0);
+    if (PIV) {
+        for (int c = wid; c < cols; c += nw) {
+            R a = 0;
+            for (int i = lane; i < rows; i += 32) a += zabs2(A[i + (size_t)c * lda]);
+            a = warp_sum(a);
+            if (lane == 0) {
+                cn[c] = a;
+                idx[c] = c;
+            }
+        }
+        __syncthreads();
+    }
     for (int j = 0; j < cols && j < rows; ++j) {
+        if (PIV) {
+            // column pivoting: the remaining column of largest norm (first on
+            // ties) moves to position j, whole column (Businger-Golub)
+            if (wid == 0) {
+                R best = -1;
+                int bi = j;
+                for (int c = j + lane; c < cols; c += 32)
+                    if (cn[c] > best) {
+                        best = cn[c];
+                        bi = c;
+                    }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ov > best || (ov == best && oi < bi)) {
+                        best = ov;
+                        bi = oi;
+                    }
+                }
+                if (lane == 0) s_piv = bi;
+            }
+            __syncthreads();
+            const int p = s_piv;
+            if (p != j) {
+                for (int i = tid; i < rows; i += QR_THREADS) {
+                    const T t = A[i + (size_t)j * lda];
+                    A[i + (size_t)j * lda] = A[i + (size_t)p * lda];
+                    A[i + (size_t)p * lda] = t;
+                }
+                if (tid == 0) {
+                    const R tn = cn[j];
+                    cn[j] = cn[p];
+                    cn[p] = tn;
+                    const int ti = idx[j];
+                    idx[j] = idx[p];
+                    idx[p] = ti;
+                }
+            }
+            __syncthreads();
+        }
         T *x = A + j + (size_t)j * lda;
         const int len = rows - j;
         R sg = 0;
@@ -79,7 +136,17 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A
         }
         __syncthreads();
         const T tv = s_tau, sc = s_scale;
-        if (tv.x == 0 && tv.y == 0) continue;
+        if (tv.x == 0 && tv.y == 0) {
+            // no reflector: the trailing columns' norms lose their row j
+            if (PIV) {
+                for (int c = j + 1 + tid; c < cols; c += QR_THREADS) {
+                    const R v = cn[c] - zabs2(A[j + (size_t)c * lda]);
+                    cn[c] = v > 0 ? v : 0;
+                }
+                __syncthreads();
+            }
+            continue;
+        }
         for (int i = 1 + tid; i < len; i += QR_THREADS) {
             const T xv = zmul(x[i], sc);
             x[i] = xv;
@@ -107,41 +174,83 @@ __global__ void __launch_bounds__(QR_THREADS) qr_kernel(int rows, int cols, T *A
                 w = warp_sum2(w);
                 w = zmul(ctau, w);
                 if (lane == 0) col[0] = zsub(col[0], w);
+                R nr = 0;
 #pragma unroll
                 for (int t = 0; t < KPL; ++t) {
                     const int i = 1 + lane + 32 * t;
                     if (i < len) {
                         zfms(v[t], xs[i], w);
                         col[i] = v[t];
+                        nr += zabs2(v[t]);
                     }
+                }
+                // pivoting: the norm of the rows below j, exact from the
+                // updated segment
+                if (PIV && c < ntrail) {
+                    nr = warp_sum(nr);
+                    if (lane == 0) cn[j + 1 + c] = nr;
                 }
             } else {
                 for (int i = 1 + lane; i < len; i += 32) zcfma(w, x[i], col[i]);
                 w = warp_sum2(w);
                 w = zmul(ctau, w);
                 if (lane == 0) col[0] = zsub(col[0], w);
-                for (int i = 1 + lane; i < len; i += 32) zfms(col[i], x[i], w);
+                R nr = 0;
+                for (int i = 1 + lane; i < len; i += 32) {
+                    zfms(col[i], x[i], w);
+                    nr += zabs2(col[i]);
+                }
+                if (PIV && c < ntrail) {
+                    nr = warp_sum(nr);
+                    if (lane == 0) cn[j + 1 + c] = nr;
+                }
             }
         }
         __syncthreads();
     }
+    if (PIV)
+        for (int c = tid; c < cols; c += QR_THREADS) perm[c] = idx[c];
 }
 
 // KPL = 24 covers rows <= 769 (the bench's 642-row H^H)
 constexpr int QR_KPL = 24;
 
-template <class T>
-static int qr_launch(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int nrhs, T *B,
-                     int ldb, long long sB, int batch)
+// perm (batch x cols, may be null): column pivoting, perm[k] = the input
+// column that ends in position k
+template <class T, bool PIV>
+static int qr_launch_t(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int nrhs, T *B,
+                       int ldb, long long sB, int batch, int *perm)
 {
+    typedef typename ctraits<T>::R R;
+    const size_t piv = PIV ? (sizeof(R) + sizeof(int)) * (size_t)cols : 0;
     if (rows <= 1 + 32 * QR_KPL) {
-        qr_kernel<T, QR_KPL><<<batch, QR_THREADS, sizeof(T) * (size_t)rows, ctx->stream>>>(rows, cols, A, lda, sA, tau,
-                                                                                        nrhs, B, ldb, sB);
+        const size_t smem = sizeof(T) * (size_t)rows + piv;
+        if (smem > 48 * 1024) {
+            if (smem > 227 * 1024) return IA_ERR_TOO_LARGE;
+            IA_CUDA_TRY(cudaFuncSetAttribute(qr_kernel<T, QR_KPL, PIV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem));
+        }
+        qr_kernel<T, QR_KPL, PIV><<<batch, QR_THREADS, smem, ctx->stream>>>(rows, cols, A, lda, sA, tau, nrhs, B,
+                                                                           ldb, sB, perm);
     } else {
-        qr_kernel<T, 0><<<batch, QR_THREADS, 0, ctx->stream>>>(rows, cols, A, lda, sA, tau, nrhs, B, ldb, sB);
+        if (piv > 48 * 1024) {
+            if (piv > 227 * 1024) return IA_ERR_TOO_LARGE;
+            IA_CUDA_TRY(cudaFuncSetAttribute(qr_kernel<T, 0, PIV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)piv));
+        }
+        qr_kernel<T, 0, PIV><<<batch, QR_THREADS, piv, ctx->stream>>>(rows, cols, A, lda, sA, tau, nrhs, B, ldb, sB,
+                                                                     perm);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
+}
+
+template <class T>
+static int qr_launch(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int nrhs, T *B,
+                     int ldb, long long sB, int batch, int *perm = nullptr)
+{
+    if (perm) return qr_launch_t<T, true>(ctx, rows, cols, A, lda, sA, tau, nrhs, B, ldb, sB, batch, perm);
+    return qr_launch_t<T, false>(ctx, rows, cols, A, lda, sA, tau, nrhs, B, ldb, sB, batch, nullptr);
 }
 
 int zgeqrs_batched(ia_context *ctx, int rows, int cols, double2 *A, int lda, long long sA, int nrhs, double2 *B,
@@ -204,11 +313,12 @@ __global__ void build_rh_kernel(int N, int Mrows, const float2 *Y, int full, flo
 }
 
 // unit columns of Y (N x N per matrix); a zero column becomes e_j
-__global__ void normalize_cols_kernel(int N, const float2 *Y, float2 *X)
+__global__ void normalize_cols_kernel(int N, const float2 *Y, float2 *X, const int *perm)
 {
     const int f = blockIdx.x;
     Y += (size_t)f * N * N;
     X += (size_t)f * N * N;
+    if (perm) perm += (size_t)f * N;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = wid; j < N; j += nw) {
         const float2 *y = Y + (size_t)j * N;
@@ -217,7 +327,8 @@ __global__ void normalize_cols_kernel(int N, const float2 *Y, float2 *X)
         a = warp_sum(a);
         const float inv = a > 0.f ? rsqrtf(a) : 0.f;
         for (int r = lane; r < N; r += 32)
-            X[r + (size_t)j * N] = a > 0.f ? make_float2(y[r].x * inv, y[r].y * inv) : make_float2(r == j ? 1.f : 0.f, 0.f);
+            X[(perm ? perm[r] : r) + (size_t)j * N] =
+                a > 0.f ? make_float2(y[r].x * inv, y[r].y * inv) : make_float2(r == j ? 1.f : 0.f, 0.f);
     }
 }
 
@@ -679,7 +790,7 @@ static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
 {
     const size_t F = batch, N = m, M = n;
     return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
-           7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + 4096;
+           7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + ws_round(4 * N * F) + 4096;
 }
 
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
@@ -714,9 +825,14 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     double2 *Rm = cur.take<double2>(NN * batch);
     double2 *Fc = cur.take<double2>(NN * batch);
     double *lam_e = cur.take<double>((size_t)N * batch);
+    int *perm = qr ? cur.take<int>((size_t)N * batch) : nullptr;
     const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
-    // 1. FP32 start: Y = H^H, QR, Jacobi with J accumulated
+    // 1. FP32 start: Y = H^H, QR with column pivoting (Y P = Q R), one-sided
+    // Jacobi on R^H.  Pivoting orders R's diagonal by decreasing size, which
+    // cuts the Jacobi's sweeps from 12-13 to 7-8 on the bench's transfer
+    // matrices (Drmac-Veselic preconditioning); H H^H = P R^H R P^T, so the
+    // Jacobi's vectors come back through P.
     if (transposed) {
         st = copy2d_batched<double2, float2>(ctx, n, m, A, n, sA, Y, Mr, sY, true, batch);
     } else {
@@ -724,7 +840,7 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
         if (!st) st = copy2d_batched<double2, float2>(ctx, Mr, N, Yd, Mr, sY, Y, Mr, sY, false, batch);
     }
     if (st) return st;
-    if (qr && (st = qr_launch<float2>(ctx, Mr, N, Y, Mr, sY, tau, 0, nullptr, 0, 0, batch))) return st;
+    if (qr && (st = qr_launch<float2>(ctx, Mr, N, Y, Mr, sY, tau, 0, nullptr, 0, 0, batch, perm))) return st;
     {
         long long total = (long long)N * N;
         int blocks = (int)((total + 255) / 256);
@@ -736,7 +852,7 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     // = H H^H, so no rotation accumulator is needed
     st = jacobi_rows_batched<float2>(ctx, N, N, N, R32, nullptr, batch, cfg->svd_max_sweeps, info);
     if (st) return st;
-    normalize_cols_kernel<<<batch, 256, 0, ctx->stream>>>(N, R32, J32);
+    normalize_cols_kernel<<<batch, 256, 0, ctx->stream>>>(N, R32, J32, perm);
     IA_LAUNCH_CHECK(ctx);
     // 2. E = H H^H (or its conjugate for H^T input) by the double-float GEMM:
     // H reaches this path from the double-float transfer (~1e-13 relative), so
