@@ -164,16 +164,27 @@ static bool all_finite(const double *p, size_t n)
 
 int ensure_side_stream(ia_context *ctx)
 {
-    if (ctx->side) return IA_OK;
-    cudaStream_t s;
-    IA_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    cudaError_t e = cudaEventCreateWithFlags(&ctx->ev_split[0], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_split[1], cudaEventDisableTiming);
+    if (ctx->side[0]) return IA_OK;
+    cudaStream_t s[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t er[4] = {}, ed[4] = {};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&er[i], cudaEventDisableTiming);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ed[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        cudaStreamDestroy(s);
+        for (int i = 0; i < 4; ++i) {
+            if (er[i]) cudaEventDestroy(er[i]);
+            if (ed[i]) cudaEventDestroy(ed[i]);
+        }
+        for (int i = 0; i < 3; ++i)
+            if (s[i]) cudaStreamDestroy(s[i]);
         return cuda_status(e);
     }
-    ctx->side = s;
+    for (int i = 0; i < 3; ++i) ctx->side[i] = s[i];
+    for (int i = 0; i < 4; ++i) {
+        ctx->ev_rows[i] = er[i];
+        ctx->ev_done[i] = ed[i];
+    }
     return IA_OK;
 }
 
@@ -260,15 +271,18 @@ int ia_create(ia_context **out, int device, void *stream)
 int ia_destroy(ia_context *ctx)
 {
     if (!ctx) return IA_OK;
-    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    for (int i = 0; i < 3; ++i)
+        if (ctx->side[i]) cudaStreamSynchronize(ctx->side[i]);
     if (ctx->ws) {
         cudaFreeAsync(ctx->ws, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
     }
-    if (ctx->side) {
-        cudaEventDestroy(ctx->ev_split[0]);
-        cudaEventDestroy(ctx->ev_split[1]);
-        cudaStreamDestroy(ctx->side);
+    if (ctx->side[0]) {
+        for (int i = 0; i < 4; ++i) {
+            cudaEventDestroy(ctx->ev_rows[i]);
+            cudaEventDestroy(ctx->ev_done[i]);
+        }
+        for (int i = 0; i < 3; ++i) cudaStreamDestroy(ctx->side[i]);
     }
     free(ctx);
     return IA_OK;
@@ -782,43 +796,52 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     if (!ctx || !mesh || !cfg || l < 1 || F < 1 || nrhs < 1 || !d_mics || !d_k || !d_p || !d_x || !d_info)
         return IA_ERR_ARG;
     const int m = mesh->m;
-    // Staggered halves: with F a multiple of 8 the bins are solved as two
-    // halves on two streams, the second starting when the first one's
-    // assembly is done, so that the latency-bound stages of one half (LU
-    // panels, Jacobi, QR, one CTA per frequency) run beside the
-    // throughput-bound stages of the other.  Frequencies stay in the
-    // assembly's blocks (4 bins in FP64, 1 in double-float; halves are
-    // multiples of 4) and every later kernel works per frequency, so the
-    // results are bitwise those of one F-bin pass.
-    const bool split = F >= 16 && F % 8 == 0;
-    const int Fh = split ? F / 2 : F;
-    const size_t need = ibem_solve_ws_bytes(m, l, Fh, nrhs, cfg);
-    int st = ws_reserve(ctx, split ? 2 * need : need);
+    // Staggered parts: the bins are solved as P parts (4 when F is a multiple
+    // of 16 and at least 32, 2 when a multiple of 8 and at least 16), each on
+    // its own stream, part q starting when part q-1's assembly is done.  So
+    // the latency-bound stages of one part (LU panels, Jacobi, QR: one CTA
+    // per frequency) run beside the throughput-bound stages of the others,
+    // and only the last part's chain is left exposed at the end.  Each part
+    // has its own workspace region.  Frequencies stay in the assembly's
+    // blocks (4 bins in FP64, 1 in double-float; parts are multiples of 4)
+    // and every later kernel works per frequency, so the results are bitwise
+    // those of one F-bin pass.
+    const int parts = (F >= 32 && F % 16 == 0) ? IA_SPLIT_PARTS : (F >= 16 && F % 8 == 0) ? 2 : 1;
+    const int Fp = F / parts;
+    const size_t need = ibem_solve_ws_bytes(m, l, Fp, nrhs, cfg);
+    int st = ws_reserve(ctx, need * parts);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
-    if (!split) {
+    if (parts == 1) {
         WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
         return ibem_solve_part(ctx, mesh, l, d_mics, F, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x,
                                d_lambda, d_s, d_info, cur, nullptr);
     }
     if ((st = ensure_side_stream(ctx))) return st;
     const int p = l < m ? l : m;
-    WsCursor ca{(char *)ctx->ws, 0, need}, cb{(char *)ctx->ws + need, 0, need};
-    st = ibem_solve_part(ctx, mesh, l, d_mics, Fh, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda,
-                         d_s, d_info, ca, ctx->ev_split[0]);
-    if (st) return st;
-    if (ca.off > need) return IA_ERR_ALLOC;    // workspace accounting broken: the halves would overlap
     cudaStream_t main = ctx->stream;
-    IA_CUDA_TRY(cudaStreamWaitEvent(ctx->side, ctx->ev_split[0], 0));
-    ctx->stream = ctx->side;
-    st = ibem_solve_part(ctx, mesh, l, d_mics, Fh, d_k + Fh, nrhs, (const double2 *)d_p + (size_t)Fh * nrhs * l, cfg,
-                         (double2 *)d_x + (size_t)Fh * nrhs * m, d_lambda ? d_lambda + (size_t)Fh * nrhs : nullptr,
-                         d_s ? d_s + (size_t)Fh * p : nullptr, d_info + Fh, cb, nullptr);
-    cudaError_t e = cudaEventRecord(ctx->ev_split[1], ctx->side);
-    ctx->stream = main;
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, ctx->ev_split[1], 0);
+    cudaError_t e = cudaSuccess;
+    int q = 0;
+    for (; q < parts && !st; ++q) {
+        const int f0 = q * Fp;
+        cudaStream_t sq = q == 0 ? main : ctx->side[q - 1];
+        if (q > 0 && (e = cudaStreamWaitEvent(sq, ctx->ev_rows[q - 1], 0)) != cudaSuccess) break;
+        ctx->stream = sq;
+        WsCursor cur{(char *)ctx->ws + need * q, 0, need};
+        st = ibem_solve_part(ctx, mesh, l, d_mics, Fp, d_k + f0, nrhs, (const double2 *)d_p + (size_t)f0 * nrhs * l,
+                             cfg, (double2 *)d_x + (size_t)f0 * nrhs * m,
+                             d_lambda ? d_lambda + (size_t)f0 * nrhs : nullptr, d_s ? d_s + (size_t)f0 * p : nullptr,
+                             d_info + f0, cur, q + 1 < parts ? ctx->ev_rows[q] : nullptr);
+        ctx->stream = main;
+        if (!st && cur.off > need) st = IA_ERR_ALLOC;   // workspace accounting broken: the parts would overlap
+    }
+    // join every started side stream back into the caller's stream
+    for (int j = 1; j < q; ++j) {
+        cudaError_t ej = cudaEventRecord(ctx->ev_done[j], ctx->side[j - 1]);
+        if (ej == cudaSuccess) ej = cudaStreamWaitEvent(main, ctx->ev_done[j], 0);
+        if (e == cudaSuccess) e = ej;
+    }
     if (st) return st;
-    if (cb.off > need) return IA_ERR_ALLOC;
     return e == cudaSuccess ? IA_OK : cuda_status(e);
 }
 

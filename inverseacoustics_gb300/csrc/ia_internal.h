@@ -13,10 +13,11 @@ struct ia_context {
     long long launches;    // kernels launched through this context
     int sm_count;
     int capturing;         // between ia_capture_begin and ia_capture_end
-    // second stream and events of the staggered two-half IBEM pipeline,
-    // created at its first use or by ia_capture_begin (ensure_side_stream)
-    cudaStream_t side;
-    cudaEvent_t ev_split[2];
+    // extra streams and events of the staggered IBEM pipeline (one stream per
+    // part beyond the first), created at their first use or by
+    // ia_capture_begin (ensure_side_stream)
+    cudaStream_t side[3];
+    cudaEvent_t ev_rows[4], ev_done[4];
 };
 
 namespace ia {
@@ -25,6 +26,8 @@ int ensure_side_stream(ia_context *ctx);
 
 // threads per CTA of the IBEM assembly kernel; mesh colours are balanced to it
 #define IA_ASM_THREADS 128
+// staggered parts of a large IBEM batch (one stream each; at most 4)
+#define IA_SPLIT_PARTS 4
 
 struct ia_mesh {
     ia_context *ctx;

@@ -242,18 +242,20 @@ def test_ibem_pipeline_matches_oracle_and_is_deterministic(cuda, ctx):
         assert relerr(x[f, 0].cpu().numpy(), xo) < 1e-9
 
 
-@pytest.mark.parametrize("precision,uniform,nrhs", [(0, True, 1), (1, True, 1), (1, False, 2)])
-def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, uniform, nrhs):
-    """F = 16 runs as two staggered halves of 8 on two streams; each half
-    equals a plain 8-bin call bit for bit (bins stay in their assembly blocks,
-    later kernels work per bin) -- evenly spaced bins (phase recurrence in
-    the assembly) and scattered ones, one and two right-hand sides."""
+@pytest.mark.parametrize("precision,uniform,nrhs,F", [(0, True, 1, 16), (1, True, 1, 16), (1, False, 2, 16),
+                                                       (1, True, 1, 32), (0, False, 1, 32)])
+def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, uniform, nrhs, F):
+    """F = 16 runs as two staggered parts of 8 on two streams, F = 32 as four
+    parts of 8 alternating between them; each part equals a plain 8-bin call
+    bit for bit (bins stay in their assembly blocks, later kernels work per
+    bin) -- evenly spaced bins (phase recurrence in the assembly) and
+    scattered ones, one and two right-hand sides."""
     from inverseacoustics_gb300 import api
     import torch
     nodes, elems = g.icosphere(2, 0.1)
     rng = np.random.default_rng(19)
     mics = g.hemisphere_array(rng, 40, 0.3)
-    f = np.linspace(200.0, 1800.0, 16) if uniform else np.sort(rng.uniform(150.0, 1900.0, 16))
+    f = np.linspace(200.0, 1800.0, F) if uniform else np.sort(rng.uniform(150.0, 1900.0, F))
     ks = 2 * np.pi * f / 343.0
     p = np.stack([np.stack([g.add_noise(rng, g.pulsating_sphere_pressure(mics, k, 0.1, 1.0 + r), 30.0)
                             for r in range(nrhs)]) for k in ks])
@@ -261,11 +263,12 @@ def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, un
     cfg = api.default_config(precision=precision)
     md, kd, pd = T(mics, cuda), T(ks, cuda), T(p, cuda)
     x, lam, s, info = api.ibem_solve_batch(ctx, mesh, md, kd, pd, cfg)
+    starts = list(range(0, F, 8))
     parts = [api.ibem_solve_batch(ctx, mesh, md, kd[h:h + 8].contiguous(), pd[h:h + 8].contiguous(), cfg)
-             for h in (0, 8)]
+             for h in starts]
     torch.cuda.synchronize()
     assert int(info.abs().sum()) == 0
-    for h, (xh, lh, sh, ih) in zip((0, 8), parts):
+    for h, (xh, lh, sh, ih) in zip(starts, parts):
         assert torch.equal(x[h:h + 8], xh) and torch.equal(lam[h:h + 8], lh) and torch.equal(s[h:h + 8], sh)
         assert torch.equal(info[h:h + 8], ih)
 
