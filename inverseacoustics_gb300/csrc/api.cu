@@ -165,23 +165,24 @@ static bool all_finite(const double *p, size_t n)
 int ensure_side_stream(ia_context *ctx)
 {
     if (ctx->side[0]) return IA_OK;
-    cudaStream_t s[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t er[4] = {}, ed[4] = {};
+    constexpr int NS = IA_SPLIT_PARTS - 1, NE = IA_SPLIT_PARTS;
+    cudaStream_t s[NS] = {};
+    cudaEvent_t er[NE] = {}, ed[NE] = {};
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking);
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&er[i], cudaEventDisableTiming);
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ed[i], cudaEventDisableTiming);
+    for (int i = 0; i < NS && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking);
+    for (int i = 0; i < NE && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&er[i], cudaEventDisableTiming);
+    for (int i = 0; i < NE && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ed[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < NE; ++i) {
             if (er[i]) cudaEventDestroy(er[i]);
             if (ed[i]) cudaEventDestroy(ed[i]);
         }
-        for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < NS; ++i)
             if (s[i]) cudaStreamDestroy(s[i]);
         return cuda_status(e);
     }
-    for (int i = 0; i < 3; ++i) ctx->side[i] = s[i];
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < NS; ++i) ctx->side[i] = s[i];
+    for (int i = 0; i < NE; ++i) {
         ctx->ev_rows[i] = er[i];
         ctx->ev_done[i] = ed[i];
     }
@@ -271,18 +272,18 @@ int ia_create(ia_context **out, int device, void *stream)
 int ia_destroy(ia_context *ctx)
 {
     if (!ctx) return IA_OK;
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < IA_SPLIT_PARTS - 1; ++i)
         if (ctx->side[i]) cudaStreamSynchronize(ctx->side[i]);
     if (ctx->ws) {
         cudaFreeAsync(ctx->ws, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
     }
     if (ctx->side[0]) {
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < IA_SPLIT_PARTS; ++i) {
             cudaEventDestroy(ctx->ev_rows[i]);
             cudaEventDestroy(ctx->ev_done[i]);
         }
-        for (int i = 0; i < 3; ++i) cudaStreamDestroy(ctx->side[i]);
+        for (int i = 0; i < IA_SPLIT_PARTS - 1; ++i) cudaStreamDestroy(ctx->side[i]);
     }
     free(ctx);
     return IA_OK;
@@ -806,7 +807,7 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     // blocks (4 bins in FP64, 1 in double-float; parts are multiples of 4)
     // and every later kernel works per frequency, so the results are bitwise
     // those of one F-bin pass.
-    const int parts = (F >= 32 && F % 16 == 0) ? IA_SPLIT_PARTS : (F >= 16 && F % 8 == 0) ? 2 : 1;
+    const int parts = (F >= 32 && F % 16 == 0) ? 4 : (F >= 16 && F % 8 == 0) ? 2 : 1;
     const int Fp = F / parts;
     const size_t need = ibem_solve_ws_bytes(m, l, Fp, nrhs, cfg);
     int st = ws_reserve(ctx, need * parts);

