@@ -550,16 +550,32 @@ def run_ours(args):
         del a64
     except Exception:
         pass
-    # DRAM bytes (read + write) of one 64-frequency launch of the mixed-path
-    # assembly kernel, from the ncu launch list in
-    # profiles/ibem_pipeline_mixed_launches_F64.txt (1891.5 MB over 2 launches)
-    asm_traffic = 945.8e6
+    # DRAM bytes (read + write) of the mixed-path assembly kernel per 64
+    # frequencies, from the ncu launch list in
+    # profiles/ibem_pipeline_mixed_launches_F64.txt (1535.7 MB over 2 passes)
+    asm_traffic = 767.9e6
+    # FP32-pipe view of the same kernel: warp instructions of the captured
+    # 8-frequency launch (762 rows x 8 = 6096 CTAs; a 16-bin call runs as two
+    # staggered parts) from the ncu capture in
+    # profiles/ibem_rows_kernel_dfl_F16.txt (smsp__inst_executed.sum 1.34e9;
+    # the work per (row, frequency) CTA is fixed, so a 64-frequency launch
+    # issues 8x that), against the SMs' issue rate of one warp instruction per
+    # SM sub-partition per clock at the sampled SM clock
+    asm_warp_instr = 8 * 1.33994e9
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+    issue_peak = props.multi_processor_count * 4 * sm_mhz * 1e6
+    issue_achieved = asm_warp_instr / (t_asm / 1000.0)
     roofline = {"kernel": "ibem_rows_kernel<dfl> (mixed-path assembly)", "bound": "hbm",
                 "achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": asm_traffic,
                 "peak_kind": peak_kind,
-                "note": "issue/latency bound on the FP32 pipe (ncu: FMA 26%, FP64 34%, issue 32%), "
-                        "not HBM bound; traffic equals the algorithmic output",
+                "note": "instruction-issue bound on the FP32 pipe, not HBM bound (ncu: issue 76%, FMA pipe 68%, "
+                        "FP64 pipe 25%, 393 FP32 lane instructions per quadrature-point evaluation); DRAM "
+                        "traffic is below the algorithmic output (rows partly stay in L2)",
+                "issue": {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
+                          "frac": issue_achieved / issue_peak, "instructions_per_launch": asm_warp_instr,
+                          "sm_mhz": sm_mhz},
                 "compute": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
                             "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
                             "peak_dgemm_measured": fp64_tflops_dgemm}}
