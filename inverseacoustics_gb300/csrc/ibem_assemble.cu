@@ -112,7 +112,7 @@ template <class R, int FB>
 __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
                                                 R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[FB], R dkf,
                                                 const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C,
-                                                cx<R> (&a)[FB][3], cx<R> (&b)[FB][3], R &ct)
+                                                const R *cw, cx<R> (&a)[FB][3], cx<R> (&b)[FB][3], R &ct)
 {
     for (int q = 0; q < nq; ++q) {
         const R *p = qd + (size_t)q * 9 * n + e;
@@ -124,7 +124,7 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
         const R r = r_mul(r2, invr);
         const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
         const R ft = r_mul(nd, r_mul(invr, invr));
-        r_mac(ct, r_mul(r_add(r_add(wa[0], wa[1]), wa[2]), ft), r_sub(r_zero(R()), invr));
+        r_mac(ct, r_mul(cw[q], ft), r_sub(r_zero(R()), invr));   // C term: w_q / 4pi (-ft / r)
         cx<R> ph, step;
         r_sincos(r_mul(kf[0], r), tab, P, C, ph.im, ph.re);
         if (fb.uniform && fb.nf > 1) r_sincos(r_mul(dkf, r), tab, P, C, step.im, step.re);
@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
+    const double *__restrict__ reg,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
     const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, const float4 *__restrict__ dftab,
     int split_ab, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
@@ -239,6 +240,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     constexpr bool DF = std::is_same<R, dfl>::value;
     float4 *tab = DF ? reinterpret_cast<float4 *>(rowbuf + 2 * FB * (size_t)m) : nullptr;   // sin/cos table
     __shared__ double ct_red[IBEM_THREADS / 32];
+    __shared__ R cw[IBEM_MAX_NQ];   // regular-rule weights w_q / 4pi (the C term)
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int row = blockIdx.x;
     const int f0 = blockIdx.y * FB;
@@ -259,6 +261,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     for (int j = tid; j < 2 * FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
     if (DF)
         for (int j = tid; j < 256; j += blockDim.x) tab[j] = dftab[j];
+    for (int q = tid; q < nq; q += blockDim.x) cw[q] = r_of_double<R>(reg[q + 2 * nq] * IA_INV4PI);
     double xo, yo, zo;
     int self = -1;
     if (row < m) {
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
             regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, dkf,
-                               tab, P, C, a, b, ctr);
+                               tab, P, C, cw, a, b, ctr);
             ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
@@ -409,15 +412,15 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
-            mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0, At, Bt, Ahs_t,
-            Bhs_t);
+            mesh->d_reg, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0, At,
+            Bt, Ahs_t, Bhs_t);
     } else {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
-            mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_sing, mesh->nqs, mics,
-            cp, k, c, rho, coef, red, nullptr, 0, At, Bt, Ahs_t, Bhs_t);
+            mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_reg, mesh->d_sing,
+            mesh->nqs, mics, cp, k, c, rho, coef, red, nullptr, 0, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
