@@ -8,6 +8,7 @@
 #include <mutex>
 #include <vector>
 #include "ia_common.cuh"
+#include "df32.cuh"
 #include "ia_internal.h"
 
 static thread_local int g_last_cuda_error = 0;
@@ -500,13 +501,13 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
     up((void **)&M->d_qdat_f, qdat_f.data(), sizeof(float) * qdat_f.size());
     up((void **)&M->d_qnrm_f, qnrm_f.data(), sizeof(float) * qnrm_f.size());
     {
-        // (sin, cos)(j pi / 128) as double-float pairs, evaluated in long
+        // (sin, cos)(j pi / 512) as double-float pairs, evaluated in long
         // double (x86 extended or Arm quad) so the argument carries more
         // bits than the FP64 result
         const long double pi_l = 3.14159265358979323846264338327950288L;
-        std::vector<float> tab(4 * 256);
-        for (int j = 0; j < 256; ++j) {
-            const long double t = (long double)j * pi_l / 128.0L;
+        std::vector<float> tab(4 * DF_TRIG_TABLE);
+        for (int j = 0; j < DF_TRIG_TABLE; ++j) {
+            const long double t = (long double)j * pi_l / (DF_TRIG_TABLE / 2);
             const double s = (double)sinl(t), c = (double)cosl(t);
             const float sh = (float)s, ch = (float)c;
             tab[4 * j] = sh;

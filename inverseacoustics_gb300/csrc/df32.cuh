@@ -131,19 +131,23 @@ __device__ __forceinline__ void df_sincos(double theta, const DfTrigCoef &C, dfl
 
 // ---- table-driven sin/cos of a double-float argument (no FP64 operations)
 //
-// theta = N pi/128 + u with N = rint(theta 128/pi) and |u| <= ~pi/256;
-// sin/cos(N pi/128) come from a 256-entry table (N mod 256) held in shared
+// theta = N pi/512 + u with N = rint(theta 512/pi) and |u| <= ~pi/1024;
+// sin/cos(N pi/512) come from a 1024-entry table (N mod 1024) held in shared
 // memory as (sin hi, sin lo, cos hi, cos lo), computed once per mesh on the
-// host in extended precision and copied in by each CTA; sin u and
-// cos u by their Taylor series to u^7 and u^8 (terms below 1e-17 dropped);
-// then the angle-sum formulas.  pi/128 is carried as p0 + p1 + p2 + p3 with
-// p0..p2 of 12 significant bits, so N p_i is exact for |N| < 4096 and the
+// host in extended precision and copied in by each CTA.  With |u| <= 3.1e-3
+// the series need little double-float work: sin u = u + u^3 (-1/6 + u^2/120)
+// with the correction (< 5e-9) in FP32 plus its first-order term in u's low
+// word, and cos u = 1 - u^2/2 + u^4/24 with u^2 in double-float and u^4/24
+// (< 4e-12) in FP32; dropped terms are below 2e-18 and the FP32 parts add
+// ~1e-15 absolute, the level of a double-float result near 1.  Then the
+// angle-sum formulas.  pi/512 is carried as p0 + ... + p4 with p0..p3 of 10
+// significant bits, so N p_i is exact for |N| < 2^14 (theta < 100) and the
 // reduction is exact up to the last part (Cody & Waite 1980).  Larger
 // arguments take the FP64-reduced series above.
+constexpr int DF_TRIG_TABLE = 1024;
+
 struct DfTrigRed {
-    float p[4];            // pi/128 split
-    float s3h, s3l;        // -1/6
-    float c2h, c2l;        // 1/24
+    float p[5];            // pi/512 split
 };
 
 __host__ inline float df_round_bits(double x, int bits)
@@ -157,24 +161,15 @@ __host__ inline float df_round_bits(double x, int bits)
 
 __host__ inline DfTrigRed df_trig_reduction_constants()
 {
-    // pi/2 as a double-double (hi exact to 53 bits, lo the next 53), / 64
-    const double hi = 1.5707963267948966 / 64.0, lo = 6.123233995736766e-17 / 64.0;
+    // pi/2 as a double-double (hi exact to 53 bits, lo the next 53), / 256
+    const double hi = 1.5707963267948966 / 256.0, lo = 6.123233995736766e-17 / 256.0;
     DfTrigRed r;
-    const float p0 = df_round_bits(hi, 12);
-    const double r1 = hi - (double)p0;
-    const float p1 = df_round_bits(r1, 12);
-    const double r2 = r1 - (double)p1;
-    const float p2 = df_round_bits(r2, 12);
-    const double r3 = (r2 - (double)p2) + lo;
-    r.p[0] = p0;
-    r.p[1] = p1;
-    r.p[2] = p2;
-    r.p[3] = (float)r3;
-    const double s3 = -1.0 / 6.0, c2 = 1.0 / 24.0;
-    r.s3h = (float)s3;
-    r.s3l = (float)(s3 - (double)r.s3h);
-    r.c2h = (float)c2;
-    r.c2l = (float)(c2 - (double)r.c2h);
+    double rest = hi;
+    for (int i = 0; i < 4; ++i) {
+        r.p[i] = df_round_bits(rest, 10);
+        rest -= (double)r.p[i];
+    }
+    r.p[4] = (float)(rest + lo);
     return r;
 }
 
@@ -188,24 +183,26 @@ __device__ __forceinline__ dfl df_add_f(dfl a, float b)
 __device__ __forceinline__ void df_sincos_tab(dfl theta, const float4 *__restrict__ tab, const DfTrigRed &P,
                                               const DfTrigCoef &C, dfl &s, dfl &c)
 {
-    const float N = rintf(theta.hi * 40.74366543152521f);     // 128 / pi
-    if (!(fabsf(N) < 4096.0f)) {                               // outside the exact reduction range
+    const float N = rintf(theta.hi * 162.97466172610082f);    // 512 / pi
+    if (!(fabsf(N) < 16384.0f)) {                              // outside the exact reduction range
         df_sincos(df_to_double(theta), C, s, c);
         return;
     }
-    // u = theta - N (p0 + p1 + p2 + p3); theta.hi - N p0 is exact
+    // u = theta - N (p0 + ... + p4); theta.hi - N p0 is exact
     dfl u = two_sum(fmaf(-N, P.p[0], theta.hi), theta.lo);
     u = df_add_f(u, -N * P.p[1]);
     u = df_add_f(u, -N * P.p[2]);
     u = df_add_f(u, -N * P.p[3]);
+    u = df_add_f(u, -N * P.p[4]);
+    const float uh = u.hi, u2h = uh * uh;
+    // sin u = u + u^3 (-1/6 + u^2/120); d(-u^3/6)/du = -u^2/2 carries u.lo
+    const float ds = fmaf(uh * u2h, fmaf(u2h, 1.0f / 120.0f, -1.0f / 6.0f), -0.5f * u2h * u.lo);
+    const dfl su = df_add_f(u, ds);
+    // cos u = 1 - u^2/2 + u^4/24
     const dfl u2 = df_mul(u, u);
-    // sin u = u + u u2 (-1/6 + u2/120 - u2^2/5040)
-    const float ts = u2.hi * fmaf(u2.hi, -1.0f / 5040.0f, 1.0f / 120.0f);
-    const dfl su = df_add(u, df_mul(u, df_mul(u2, df_add_f(dfl{P.s3h, P.s3l}, ts))));
-    // cos u = 1 + u2 (-1/2 + u2 (1/24 - u2/720 + u2^2/40320))
-    const float tc = u2.hi * fmaf(u2.hi, 1.0f / 40320.0f, -1.0f / 720.0f);
-    const dfl cu = df_add_f(df_mul(u2, df_add_f(df_mul(u2, df_add_f(dfl{P.c2h, P.c2l}, tc)), -0.5f)), 1.0f);
-    const float4 t = tab[((int)N) & 255];
+    const dfl w = df_add_f(dfl{-0.5f * u2.hi, -0.5f * u2.lo}, u2h * u2h * (1.0f / 24.0f));
+    const dfl cu = df_add_f(w, 1.0f);
+    const float4 t = tab[((int)N) & (DF_TRIG_TABLE - 1)];
     const dfl sj{t.x, t.y}, cj{t.z, t.w};
     s = df_add(df_mul(sj, cu), df_mul(cj, su));
     c = df_sub(df_mul(cj, cu), df_mul(sj, su));

@@ -48,7 +48,7 @@ struct ia_mesh {
     double *d_qnrm;        // element normals [3][element]
     float *d_qdat_f;       // d_qdat as double-float (hi, lo) pairs
     float *d_qnrm_f;       // d_qnrm as double-float (hi, lo) pairs
-    float4 *d_dftab;       // 256 x (sin hi, sin lo, cos hi, cos lo)(j pi / 128) for the double-float assembly
+    float4 *d_dftab;       // 1024 x (sin hi, sin lo, cos hi, cos lo)(j pi / 512) for the double-float assembly
     int *d_gptr, *d_gidx;  // node-node pattern, CSR (m + 1, gnnz): nodes sharing an element
     int gnnz;
 };

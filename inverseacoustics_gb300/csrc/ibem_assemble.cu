@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     const R dkf = r_of_double<R>(fb.dk);
     for (int j = tid; j < 2 * FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
     if (DF)
-        for (int j = tid; j < 256; j += blockDim.x) tab[j] = dftab[j];
+        for (int j = tid; j < DF_TRIG_TABLE; j += blockDim.x) tab[j] = dftab[j];
     for (int q = tid; q < nq; q += blockDim.x) cw[q] = r_of_double<R>(reg[q + 2 * nq] * IA_INV4PI);
     double xo, yo, zo;
     int self = -1;
@@ -402,7 +402,7 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     const int m = mesh->m;
     const int rows = m + n_ch + l;
     const int FB = df32 ? AsmBlock<dfl>::FB : AsmBlock<double>::FB;
-    const size_t smem = sizeof(double2) * 2 * (size_t)m * FB + (df32 ? 256 * sizeof(float4) : 0);
+    const size_t smem = sizeof(double2) * 2 * (size_t)m * FB + (df32 ? DF_TRIG_TABLE * sizeof(float4) : 0);
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
     static const DfTrigCoef coef = df_trig_coefficients();
     static const DfTrigRed red = df_trig_reduction_constants();
