@@ -557,11 +557,11 @@ def run_ours(args):
     # FP32-pipe view of the same kernel: warp instructions of the captured
     # 8-frequency launch (762 rows x 8 = 6096 CTAs; a 16-bin call runs as two
     # staggered parts) from the ncu capture in
-    # profiles/ibem_rows_kernel_dfl_F16.txt (smsp__inst_executed.sum 1.34e9;
+    # profiles/ibem_rows_kernel_dfl_F16.txt (smsp__inst_executed.sum 1.2536e9;
     # the work per (row, frequency) CTA is fixed, so a 64-frequency launch
     # issues 8x that), against the SMs' issue rate of one warp instruction per
     # SM sub-partition per clock at the sampled SM clock
-    asm_warp_instr = 8 * 1.33994e9
+    asm_warp_instr = 8 * 1.25363e9
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = props.multi_processor_count * 4 * sm_mhz * 1e6
@@ -570,8 +570,8 @@ def run_ours(args):
                 "achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": asm_traffic,
                 "peak_kind": peak_kind,
-                "note": "instruction-issue bound on the FP32 pipe, not HBM bound (ncu: issue 76%, FMA pipe 68%, "
-                        "FP64 pipe 25%, 393 FP32 lane instructions per quadrature-point evaluation); DRAM "
+                "note": "instruction-issue bound on the FP32 pipe, not HBM bound (ncu: issue 75%, FMA pipe 66%, "
+                        "FP64 pipe 26%, 734 FP32 lane instructions per quadrature-point evaluation); DRAM "
                         "traffic is below the algorithmic output (rows partly stay in L2)",
                 "issue": {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
                           "frac": issue_achieved / issue_peak, "instructions_per_launch": asm_warp_instr,
