@@ -38,6 +38,26 @@ def test_mixed_assembly_matches_fp64(cuda, ctx):
         assert np.max(np.abs(b - a)) < 1e-12 * np.max(np.abs(a))
 
 
+def test_mixed_assembly_large_arguments(cuda, ctx):
+    """kr up to ~150: the table-driven double-float sin/cos reduces by pi/512
+    exactly for kr < 100 and hands larger arguments to the FP64-reduced series;
+    both regimes (and the switch between them inside one row) agree with the
+    FP64 kernel to 1e-12."""
+    from inverseacoustics_gb300 import api
+    import torch
+    nodes, elems = g.icosphere(2, 1.0)
+    mics = g.hemisphere_array(np.random.default_rng(5), 16, 3.0)
+    ks = np.array([20.0, 37.5, 41.0])            # kr_max ~ 4 k (mics at 3 m, surface at 1 m)
+    mesh = api.Mesh(ctx, nodes, elems)
+    r64 = api.ibem_assemble_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
+    rmx = api.ibem_assemble_batch(ctx, mesh, T(mics, cuda), T(ks, cuda), api.default_config(precision=1))
+    torch.cuda.synchronize()
+    for a, b in zip(r64, rmx):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        for f in range(len(ks)):
+            assert relerr(b[f], a[f]) < 1e-12, f
+
+
 def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
     from inverseacoustics_gb300 import api
     import torch
