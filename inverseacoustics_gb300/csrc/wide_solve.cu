@@ -864,9 +864,13 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     // 3. eigen-refinement from X = J (conj(J) for H^T input)
     if ((st = copy2d_batched<float2, double2>(ctx, N, N, J32, N, sN, X, N, sN, transposed, batch))) return st;
     // the FP32 Jacobi leaves X accurate to ~1e-5 (its stopping threshold sits
-    // above FP32 rounding noise); two quadratic steps reach the double-float
+    // above FP32 rounding noise); the quadratic steps reach the double-float
     // level of their products, and step 4's FP64 S = X^H E X with the
-    // two-sided Jacobi finishes at FP64 level
+    // two-sided Jacobi finishes at FP64 level.  Two steps: emulated on the
+    // bench's transfer matrices they leave 27-143 pairs coupled above that
+    // Jacobi's threshold and three steps 0-6, but the third step's four
+    // double-float products cost more than the Jacobi sweeps they save
+    // (measured 14.3 -> 14.9 ms per 64-bin solve).
     const int steps = cfg->refine_steps > 2 ? cfg->refine_steps : 2;
     for (int it = 0; it < steps; ++it) {
         if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
