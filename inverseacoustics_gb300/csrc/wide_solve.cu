@@ -636,7 +636,9 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
                 ++mine;
             }
             if (mine) atomicAdd(&s_rot, mine);
-            __syncthreads();
+            // a round without rotations (most rounds once the refinement has
+            // run) skips both apply phases and their barriers
+            if (!__syncthreads_or(mine)) continue;
             // columns of S and X: [u v] <- [u v] G
             for (int k = wid; k < P; k += nw) {
                 const int i = pi[k];
