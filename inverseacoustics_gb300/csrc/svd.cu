@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
     extern __shared__ __align__(16) unsigned char smraw[];
     T *Y = reinterpret_cast<T *>(smraw);
     __shared__ int s_rot;
+    __shared__ unsigned s_maxrel;   // largest |y_i^H y_j| / (|y_i||y_j|) rotated in the sweep (float bits)
     const int f = blockIdx.x;
     Yg += f * sY;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -279,9 +280,13 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
     __syncthreads();
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
-        if (threadIdx.x == 0) s_rot = 0;
+        if (threadIdx.x == 0) {
+            s_rot = 0;
+            s_maxrel = 0u;
+        }
         __syncthreads();
         int rot_local = 0;
+        float relmax = 0.f;
         for (int round = 0; round < N2 - 1; ++round) {
             for (int k = 2 * wid + half; k < N2 / 2; k += 2 * nw) {
                 int i, j;
@@ -307,6 +312,7 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
                 g.x = half_sum<T>(g.x, mask);
                 g.y = half_sum<T>(g.y, mask);
                 if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
+                if (sizeof(R) == 4) relmax = fmaxf(relmax, (float)(sqrt(g.x * g.x + g.y * g.y) / (sqrt(a) * sqrt(b))));
 #pragma unroll
                 for (int t = 0; t < KPL; ++t) {
                     int r = hl + 16 * t;
@@ -320,11 +326,20 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
             }
             __syncthreads();
         }
-        if (hl == 0 && rot_local) atomicAdd(&s_rot, rot_local);
+        if (hl == 0 && rot_local) {
+            atomicAdd(&s_rot, rot_local);
+            if (sizeof(R) == 4) atomicMax(&s_maxrel, __float_as_uint(relmax));
+        }
         __syncthreads();
-        int total = s_rot;
+        const int total = s_rot;
+        const float maxrel = __uint_as_float(s_maxrel);
         __syncthreads();
         if (total == 0) break;
+        // FP32 (a start for the FP64-level refinement that follows): when the
+        // largest rotated coupling of the sweep was below sqrt(tol) / 2, the
+        // next sweep's couplings are below tol (quadratic convergence) and
+        // would only confirm it -- skip that sweep.  FP64 runs to the test.
+        if (sizeof(R) == 4 && maxrel < 0.5f * sqrtf((float)tol)) break;
     }
     for (int e = threadIdx.x; e < M * N; e += blockDim.x) Yg[e] = Y[e];
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
