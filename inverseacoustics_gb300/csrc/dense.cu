@@ -246,7 +246,6 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
     T *P = reinterpret_cast<T *>(lu_smem);          // P[c * pr + (i - k0)]
     __shared__ R sval[PANEL_THREADS / 32];
     __shared__ int sidx[PANEL_THREADS / 32];
-    __shared__ int s_piv;
     const int f = blockIdx.x;
     A += f * sA;
     ipiv += (size_t)f * n;
@@ -257,16 +256,13 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
         P[e] = A[k0 + i + (size_t)(k0 + c) * lda];
     }
     __syncthreads();
-    // A(i, c) of the panel is P[(c - k0) * pr + i - k0]
-    for (int j = k0; j < kend; ++j) {
-        const T *col = P + (size_t)(j - k0) * pr;           // col[i - k0] = A(i, j)
-        R best = -1;
-        int bi = n;
-        for (int i = j + tid; i < n; i += PANEL_THREADS) {
-            T a = col[i - k0];
-            R v = fabs(a.x) + fabs(a.y);
-            if (v > best) { best = v; bi = i; }
-        }
+    // A(i, c) of the panel is P[(c - k0) * pr + i - k0].  The pivot search of
+    // column j + 1 rides in column j's rank-1 update (the threads that update
+    // column j + 1 keep the running maximum of the new values), so a column
+    // costs three barriers: interchange, scale, update.  Every thread decides
+    // the pivot from the per-warp maxima itself.  Same values, same order of
+    // comparison, so the pivots are those of a separate search.
+    auto warp_best = [&](R best, int bi) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             R ov = __shfl_xor_sync(0xffffffffu, best, o);
@@ -274,22 +270,29 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
             if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
         }
         if (lane == 0) { sval[wid] = best; sidx[wid] = bi; }
-        __syncthreads();
-        if (tid == 0) {
-            R bv = sval[0];
-            int bidx = sidx[0];
-            for (int w = 1; w < PANEL_THREADS / 32; ++w)
-                if (sval[w] > bv || (sval[w] == bv && sidx[w] < bidx)) { bv = sval[w]; bidx = sidx[w]; }
-            if (!(bv > 0)) {
-                if (!(bv == 0)) info[f] |= IA_INFO_NONFINITE;
-                else info[f] |= IA_INFO_SINGULAR;
-                bidx = j;
-            }
-            s_piv = bidx;
-            ipiv[j] = bidx;
+    };
+    {
+        const T *col = P;                                   // column k0
+        R best = -1;
+        int bi = n;
+        for (int i = k0 + tid; i < n; i += PANEL_THREADS) {
+            T a = col[i - k0];
+            R v = fabs(a.x) + fabs(a.y);
+            if (v > best) { best = v; bi = i; }
         }
+        warp_best(best, bi);
         __syncthreads();
-        const int piv = s_piv;
+    }
+    for (int j = k0; j < kend; ++j) {
+        R bv = sval[0];
+        int piv = sidx[0];
+        for (int w = 1; w < PANEL_THREADS / 32; ++w)
+            if (sval[w] > bv || (sval[w] == bv && sidx[w] < piv)) { bv = sval[w]; piv = sidx[w]; }
+        if (!(bv > 0)) piv = j;
+        if (tid == 0) {
+            if (!(bv > 0)) info[f] |= (bv == 0) ? IA_INFO_SINGULAR : IA_INFO_NONFINITE;
+            ipiv[j] = piv;
+        }
         if (piv != j) {
             for (int c = tid; c < nb; c += PANEL_THREADS) {
                 T *pc = P + (size_t)c * pr;
@@ -307,6 +310,8 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
         }
         __syncthreads();
         const int rows = n - j - 1, ncols = kend - j - 1;
+        R best = -1;
+        int bi = n;
         for (int idx = tid; idx < rows * ncols; idx += PANEL_THREADS) {
             int r = j + 1 + idx % rows;
             int c = j + 1 + idx / rows;
@@ -314,7 +319,12 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
             T v = pc[r - k0];
             zfms(v, cj[r - k0], pc[j - k0]);
             pc[r - k0] = v;
+            if (c == j + 1) {
+                R av = fabs(v.x) + fabs(v.y);
+                if (av > best) { best = av; bi = r; }
+            }
         }
+        if (ncols > 0) warp_best(best, bi);
         __syncthreads();
     }
     for (int e = tid; e < pr * nb; e += PANEL_THREADS) {
