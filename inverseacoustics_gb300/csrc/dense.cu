@@ -489,7 +489,7 @@ int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int l
 // thread per row, the block's LU_NB columns of L or U read coalesced from
 // global memory (L2).  Replaces 2 n / LU_NB dependent small launches (a
 // diagonal-block solve and a GEMM update per step) by one.
-constexpr int GETRS_RB = 8;
+constexpr int GETRS_RB = 8;   // 4 and 16 measured slower (transfer stage 30.1 / 30.5 vs 29.5 ms per 64 bins)
 constexpr int GETRS_THREADS = 32 * GETRS_RB;   // a warp per column in the diagonal solves
 
 __device__ __forceinline__ float2 shfl_c(float2 v, int src)
