@@ -27,18 +27,25 @@ __device__ __forceinline__ void rr_pair(int N2, int round, int k, int &i, int &j
         i = round;
         j = N2 - 1;
     } else {
-        i = (round + k) % (N2 - 1);
-        j = (round - k + N2 - 1) % (N2 - 1);
+        // (round + k) mod (N2 - 1) and (round - k + N2 - 1) mod (N2 - 1):
+        // both operands lie in [0, 2 (N2 - 1)), so one conditional
+        // subtraction replaces the integer division
+        i = round + k;
+        if (i >= N2 - 1) i -= N2 - 1;
+        j = round - k + N2 - 1;
+        if (j >= N2 - 1) j -= N2 - 1;
     }
     if (i > j) { int t = i; i = j; j = t; }
 }
 
 // Rotation that zeroes y_i^H y_j for column norms a, b and product g.
 template <class T, class R>
-__device__ __forceinline__ bool jacobi_rotation(R a, R b, T g, R tol, R &c, T &sp)
+__device__ __forceinline__ bool jacobi_rotation(R a, R b, T g, R tol, R &c, T &sp, R *rel = nullptr)
 {
     R gm = sqrt(g.x * g.x + g.y * g.y);
-    if (!(gm > tol * sqrt(a) * sqrt(b)) || gm == 0) return false;
+    const R sa = sqrt(a), sb = sqrt(b);
+    if (!(gm > tol * sa * sb) || gm == 0) return false;
+    if (rel) *rel = gm / (sa * sb);   // the relative coupling |y_i^H y_j| / (|y_i||y_j|)
     R zeta = (b - a) / (2 * gm);
     R t;
     if (fabs(zeta) > (R)1e30) t = (R)0.5 / zeta;
@@ -311,8 +318,9 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
                 b = half_sum<T>(b, mask);
                 g.x = half_sum<T>(g.x, mask);
                 g.y = half_sum<T>(g.y, mask);
-                if (!jacobi_rotation(a, b, g, tol, c, sp)) continue;
-                if (sizeof(R) == 4) relmax = fmaxf(relmax, (float)(sqrt(g.x * g.x + g.y * g.y) / (sqrt(a) * sqrt(b))));
+                R rel = 0;
+                if (!jacobi_rotation(a, b, g, tol, c, sp, sizeof(R) == 4 ? &rel : nullptr)) continue;
+                relmax = fmaxf(relmax, (float)rel);
 #pragma unroll
                 for (int t = 0; t < KPL; ++t) {
                     int r = hl + 16 * t;

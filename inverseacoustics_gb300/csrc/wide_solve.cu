@@ -576,8 +576,13 @@ __device__ __forceinline__ void hj_pair(int N2, int round, int k, int &i, int &j
         i = round;
         j = N2 - 1;
     } else {
-        i = (round + k) % (N2 - 1);
-        j = (round - k + N2 - 1) % (N2 - 1);
+        // (round + k) mod (N2 - 1) and (round - k + N2 - 1) mod (N2 - 1):
+        // both operands lie in [0, 2 (N2 - 1)), so one conditional
+        // subtraction replaces the integer division
+        i = round + k;
+        if (i >= N2 - 1) i -= N2 - 1;
+        j = round - k + N2 - 1;
+        if (j >= N2 - 1) j -= N2 - 1;
     }
     if (i > j) { int t = i; i = j; j = t; }
 }
