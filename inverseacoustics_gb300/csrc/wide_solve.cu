@@ -568,6 +568,12 @@ __global__ void __launch_bounds__(OA_THREADS) oa_update_kernel(int N, const doub
 //   G = [[c, s e], [-s conj(e), c]],  e = S_ij/|S_ij|,  t = tan(theta) from
 //   zeta = (S_jj - S_ii) / (2 |S_ij|)   (Rutishauser's stable form)
 // zeroes S_ij; S <- G^H S G on the pair, X <- X G.  LAM <- diag(S).
+// Each sweep first checks every pair at once and runs only the rounds that
+// hold a coupled pair; a round's rotations are applied with every (pair,
+// matrix, row) and (pair, column) update spread over the whole CTA, one round
+// of memory latency per phase.  (Applied warp per pair, with the global-memory
+// updates in sequence while the other warps waited at the barrier, the kernel
+// stalled on barriers: 68 cycles per issue.)
 constexpr int HJ_THREADS = 512;
 
 __device__ __forceinline__ void hj_pair(int N2, int round, int k, int &i, int &j)
@@ -596,8 +602,10 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
     double2 *se = reinterpret_cast<double2 *>(hj_sm + P + (P & 1));   // P, 16-byte aligned
     int *pi = reinterpret_cast<int *>(se + P);            // P
     int *pj = pi + P;                                     // P
+    int *rflag = pj + P;                                  // N2 - 1: rounds with a coupled pair
     __shared__ double red[HJ_THREADS / 32];
     __shared__ int s_rot;
+    __shared__ int s_nact;   // rotating pairs of the current round (cs, se, pi, pj slots)
     const int f = blockIdx.x;
     S += (size_t)f * N * N;
     X += (size_t)f * N * N;
@@ -617,14 +625,31 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
     const double tol = 2.0 * (double)N * 2.220446049250313e-16 * red[0];
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
-        if (tid == 0) s_rot = 0;
+        // every pair of the sweep checked at once (independent loads): only
+        // rounds holding a pair above tol run; couplings that rotations of
+        // this sweep raise in skipped rounds are met by the next sweep's check,
+        // and a converged S costs one pass instead of N2 - 1 serial rounds
+        for (int r = tid; r < N2 - 1; r += blockDim.x) rflag[r] = 0;
+        if (tid == 0) {
+            s_rot = 0;
+            s_nact = 0;
+        }
+        __syncthreads();
+        for (int e = tid; e < (N2 - 1) * P; e += blockDim.x) {
+            const int round = e / P, k = e - round * P;
+            int i, j;
+            hj_pair(N2, round, k, i, j);
+            if (j >= N) continue;
+            const double2 s = S[i + (size_t)j * N];
+            if (sqrt(s.x * s.x + s.y * s.y) > tol) rflag[round] = 1;
+        }
         __syncthreads();
         for (int round = 0; round < N2 - 1; ++round) {
+            if (!rflag[round]) continue;
             int mine = 0;
             for (int k = tid; k < P; k += blockDim.x) {
                 int i, j;
                 hj_pair(N2, round, k, i, j);
-                pi[k] = -1;
                 if (j >= N) continue;
                 const double2 s = S[i + (size_t)j * N];
                 const double g = sqrt(s.x * s.x + s.y * s.y);
@@ -634,53 +659,50 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
                 const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                 const double c = 1.0 / sqrt(1.0 + t * t);
                 const double sn = t * c;
-                cs[k] = c;
-                se[k] = make_double2(sn * s.x / g, sn * s.y / g);   // s e
-                pi[k] = i;
-                pj[k] = j;
+                const int slot = atomicAdd(&s_nact, 1);
+                cs[slot] = c;
+                se[slot] = make_double2(sn * s.x / g, sn * s.y / g);   // s e
+                pi[slot] = i;
+                pj[slot] = j;
                 ++mine;
             }
             if (mine) atomicAdd(&s_rot, mine);
-            // a round without rotations (most rounds once the refinement has
-            // run) skips both apply phases and their barriers
+            // a round without rotations skips both apply phases and their barriers
             if (!__syncthreads_or(mine)) continue;
+            const int nact = s_nact;
+            // the round's pairs are disjoint: every (pair, matrix, row) of the
+            // column phase and every (pair, column) of the row phase is an
+            // independent update, spread over the whole CTA
             // columns of S and X: [u v] <- [u v] G
-            for (int k = wid; k < P; k += nw) {
-                const int i = pi[k];
-                if (i < 0) continue;
-                const int j = pj[k];
-                const double c = cs[k];
-                const double2 w = se[k];
-                for (int m = 0; m < 2; ++m) {
-                    double2 *M = m == 0 ? S : X;
-                    double2 *ci = M + (size_t)i * N, *cj = M + (size_t)j * N;
-                    for (int r = lane; r < N; r += 32) {
-                        const double2 u = ci[r], v = cj[r];
-                        double2 nu = zscale(u, c), nv = zscale(v, c);
-                        zfms(nu, zconj(w), v);                 // c u - conj(s e) v
-                        zfma(nv, w, u);                        // c v + s e u
-                        ci[r] = nu;
-                        cj[r] = nv;
-                    }
-                }
+            for (int e = tid; e < nact * 2 * N; e += blockDim.x) {
+                const int q = e / (2 * N), rem = e - q * 2 * N, mat = rem / N, r = rem - mat * N;
+                const int i = pi[q], j = pj[q];
+                const double c = cs[q];
+                const double2 w = se[q];
+                double2 *M = mat == 0 ? S : X;
+                double2 *ci = M + (size_t)i * N, *cj = M + (size_t)j * N;
+                const double2 u = ci[r], v = cj[r];
+                double2 nu = zscale(u, c), nv = zscale(v, c);
+                zfms(nu, zconj(w), v);                 // c u - conj(s e) v
+                zfma(nv, w, u);                        // c v + s e u
+                ci[r] = nu;
+                cj[r] = nv;
             }
             __syncthreads();
+            if (tid == 0) s_nact = 0;                  // every thread has read it
             // rows of S: [u; v] <- G^H [u; v]
-            for (int k = wid; k < P; k += nw) {
-                const int i = pi[k];
-                if (i < 0) continue;
-                const int j = pj[k];
-                const double c = cs[k];
-                const double2 w = se[k];
-                for (int col = lane; col < N; col += 32) {
-                    double2 *a = S + i + (size_t)col * N, *b = S + j + (size_t)col * N;
-                    const double2 u = *a, v = *b;
-                    double2 nu = zscale(u, c), nv = zscale(v, c);
-                    zfms(nu, w, v);                            // c u - s e v
-                    zfma(nv, zconj(w), u);                     // c v + conj(s e) u
-                    *a = nu;
-                    *b = nv;
-                }
+            for (int e = tid; e < nact * N; e += blockDim.x) {
+                const int q = e / N, col = e - q * N;
+                const int i = pi[q], j = pj[q];
+                const double c = cs[q];
+                const double2 w = se[q];
+                double2 *a = S + i + (size_t)col * N, *b = S + j + (size_t)col * N;
+                const double2 u = *a, v = *b;
+                double2 nu = zscale(u, c), nv = zscale(v, c);
+                zfms(nu, w, v);                            // c u - s e v
+                zfma(nv, zconj(w), u);                     // c v + conj(s e) u
+                *a = nu;
+                *b = nv;
             }
             __syncthreads();
         }
@@ -910,7 +932,8 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;
     {
         const int P = (N + (N & 1)) / 2;
-        const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P;
+        const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
+                            sizeof(int) * (size_t)(2 * P);
         const int sweeps = cfg->svd_max_sweeps < 16 ? cfg->svd_max_sweeps : 16;
         herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
         IA_LAUNCH_CHECK(ctx);
