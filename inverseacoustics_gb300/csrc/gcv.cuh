@@ -61,16 +61,39 @@ __device__ __forceinline__ double gcv_slope(const GcvData &d, double t, int lane
     return dnum * den - 2.0 * num * dden;
 }
 
+// The root of the slope in t = log lambda on the grid bracket, by the Illinois
+// variant of regula falsi (Dowell & Jarratt 1971): secant steps that keep the
+// bracket, the retained end's value halved when the same end moves twice, so
+// both ends converge superlinearly.  Stops when the bracket is below 1e-12 in
+// t (lambda to ~1e-12 relative) or the slope is exactly 0; a midpoint step
+// replaces a secant point that falls outside the open bracket.  Each slope
+// evaluation is ~200 FP64 warp instructions on GB300's slow FP64 pipe, so this
+// takes ~10 evaluations where bisection to the same width took 40.
 __device__ __forceinline__ double gcv_bisect(const GcvData &d, double lo, double hi, int lane)
 {
     if (lo == hi) return lo;
     double a = log(lo), b = log(hi);
-    if (gcv_slope(d, a, lane) >= 0.0) return lo;
-    if (gcv_slope(d, b, lane) <= 0.0) return hi;
-    for (int it = 0; it < GCV_BISECT_ITERS; ++it) {
-        double mid = 0.5 * (a + b);
-        if (gcv_slope(d, mid, lane) < 0.0) a = mid;
-        else b = mid;
+    double fa = gcv_slope(d, a, lane), fb;
+    if (fa >= 0.0) return lo;
+    fb = gcv_slope(d, b, lane);
+    if (fb <= 0.0) return hi;
+    int side = 0;
+    for (int it = 0; it < GCV_BISECT_ITERS && b - a > 1e-12; ++it) {
+        double c = b - fb * (b - a) / (fb - fa);
+        if (!(c > a && c < b)) c = 0.5 * (a + b);
+        const double fc = gcv_slope(d, c, lane);
+        if (fc == 0.0) return exp(c);
+        if (fc < 0.0) {
+            a = c;
+            fa = fc;
+            if (side < 0) fb *= 0.5;
+            side = -1;
+        } else {
+            b = c;
+            fb = fc;
+            if (side > 0) fa *= 0.5;
+            side = 1;
+        }
     }
     return exp(0.5 * (a + b));
 }
