@@ -50,18 +50,20 @@ def _dist():
     return rank, world, local
 
 
+def _config(world):
+    """The workload's description, identical in both arms (how each arm runs
+    it is reported outside `config`)."""
+    return {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies_per_gpu": N_FREQ,
+            "nodes": 642, "triangles": 1280, "mics": 120, "rules": "7-point Radon regular, 4x4 Duffy singular",
+            "inputs": "pulsating + oscillating sphere, seeded complex amplitudes, 30 dB SNR",
+            "parallelism": f"freq-shard x{world}",
+            "l2": "GPU arm: flushed between timed steps (256 MB write); host arm: not applicable"}
+
+
 def _workload():
     from inverseacoustics_gb300 import geometry as g
-    import numpy as np
     w = g.ibem_sphere(n_freq=N_FREQ)
-    mics = w.arrays["mics"]
-    amp = w.params["amp"]
-    rng = w.params["rng"]
-    p = np.stack([
-        g.add_noise(rng, amp[f, 0] * g.pulsating_sphere_pressure(mics, w.k[f], 0.1, 1.0) +
-                    amp[f, 1] * g.oscillating_sphere_pressure(mics, w.k[f], 0.1, 1.0), 30.0)[None, :]
-        for f in range(N_FREQ)])
-    return w, p
+    return w, g.ibem_sphere_pressures(w)
 
 
 class ClockSampler:
@@ -116,9 +118,9 @@ def _peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def _cpu_baseline(freqs, threads=0, repeat=1):
+def _cpu_baseline(freqs, threads=0, repeat=1, warmup=0):
     cmd = [sys.executable, "-m", "oracle.cpu_pipeline", "--freqs", str(freqs), "--threads", str(threads),
-           "--repeat", str(repeat)]
+           "--repeat", str(repeat), "--warmup", str(warmup)]
     env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
     r = subprocess.run(cmd, capture_output=True, text=True, cwd=ROOT, env=env, timeout=900)
     if r.returncode != 0:
@@ -133,18 +135,18 @@ def run_reference(args):
     from oracle import build as ob
     ob.build_oracle()
     threads = os.cpu_count() or 1
-    sample = max(threads, 8)
-    for _ in range(args.warmup):
-        _cpu_baseline(sample, threads, 1)
-    res = _cpu_baseline(sample, threads, args.steps)
+    # every step solves all 64 bins of the workload (the GPU arm's inputs,
+    # bit for bit): ~1.5 s per step on 16 Grace cores
+    sample = N_FREQ
+    res = _cpu_baseline(sample, threads, args.steps, warmup=args.warmup)
     rates = res["rates"]
     value = sum(rates) / len(rates)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
-            "data": "synthetic (seeded)",
-            "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies": N_FREQ,
-                       "parallelism": "host threads, frequency-parallel"},
+            "data": "synthetic (seeded)", "config": _config(args.gpus),
+            "execution": "the reference's CPU algorithm (oracle port: C assembly, zgels-equivalent solve, "
+                         "csvd/GCV/Tikhonov), host threads, frequency-parallel, 1 BLAS thread each",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
                              "sample": res["sample"], "cpu": res["cpu"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -606,11 +608,9 @@ def run_ours(args):
                 "dtype": "mixed: f64 assembly, f32 LU/QR/Jacobi, double-float (f32 pair) refinement GEMMs, "
                          "f64 GCV and Tikhonov refinement",
                 "precision_path": "mixed", "data": "synthetic (seeded)",
-                "config": {"workload": f"ibem_sphere_642n_1280e_120mic_F{N_FREQ}", "frequencies_per_gpu": N_FREQ,
-                           "nodes": m, "triangles": int(elems.shape[1]), "mics": l,
-                           "rules": "7-point Radon regular, 4x4 Duffy singular", "parallelism": f"freq-shard x{world}",
-                           "l2": "flushed between timed steps (256 MB write)",
-                           "launch": "one CUDA graph replay per step (graph of the whole batched solve)"},
+                "config": _config(world),
+                "execution": "one CUDA graph replay per step (graph of the whole batched solve), L2 flushed "
+                             "between timed steps",
                 "fp64_path": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms / steps64,
                               "mixed_speedup": value / fp64_value},
                 "direct_calls": {"value": direct_value, "unit": UNIT, "note": "same solve without the graph"},

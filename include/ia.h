@@ -58,6 +58,7 @@ typedef enum {
 #define IA_INFO_NOCONV    1  /* Jacobi sweep cap reached */
 #define IA_INFO_SINGULAR  2  /* zero pivot */
 #define IA_INFO_NONFINITE 4  /* NaN/Inf met */
+#define IA_INFO_TIMEOUT   8  /* a bounded device-side wait ran out (the entry's output is not written) */
 
 enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
 enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };
@@ -96,6 +97,9 @@ typedef struct {
     int mode_iters;        /* radiation modes: subspace iterations (default 10; FP32 in the
                               mixed path, which then adds refine_steps FP64 ones) */
     int mode_oversample;   /* radiation modes: subspace vectors beyond the requested modes (default 16) */
+    int gemm_slices;       /* the mixed path's FP64-level complex products (IBEM refinement residual and
+                              transfer product): 6..8 = tensor-core GEMM on that many BF16 slices per
+                              operand (default 7); 0 = double-float CUDA-core GEMM */
 } ia_config;
 
 /* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,
@@ -283,6 +287,20 @@ int ia_regularize_batch(ia_context *ctx, int m, int n, int F, const ia_complex *
 int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs, const ia_complex *d_b,
                    const ia_config *cfg, ia_complex *d_x, double *d_lambda, double *d_s, int *d_info);
 
+/* Batched complex GEMM, C = alpha op(A) op(B) + beta C (op: 0 N, 1 T, 2 C),
+ * FP64 operands and output on the device; replaces the reference's
+ * cublasZgemm (CUDA/ibem.cuh:398).  precision IA_PREC_FP64: FP64 CUDA-core
+ * GEMM.  IA_PREC_MIXED: tensor-core GEMM on BF16 slices (Ozaki scheme) with
+ * `slices` slices per operand (6..8, 0 = 7), exact FP32 level sums in tensor
+ * memory; error at most (4 slices + 8) 2^(-6 slices) of max|A row|
+ * max|B col| per product term (8e-12 at 7 slices, 1.4e-13 at 8);
+ * needs slices * 2048 * K <= 2^24 (K <= 1170 at 7 slices, else
+ * IA_ERR_TOO_LARGE).  d_info (batch ints, may be NULL) gets IA_INFO_TIMEOUT
+ * for an entry whose pipeline wait ran out. */
+int ia_zgemm_batch(ia_context *ctx, int opa, int opb, int M, int N, int K, double alpha, const ia_complex *d_A,
+                   int lda, long long sA, const ia_complex *d_B, int ldb, long long sB, double beta,
+                   ia_complex *d_C, int ldc, long long sC, int batch, int precision, int slices, int *d_info);
+
 /* Size of the device array that ia_solve_batch_noalloc works in. */
 #define IA_NOALLOC_SCRATCH_BYTES (16u << 20)
 
@@ -294,8 +312,10 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
  * IA_NOALLOC_SCRATCH_BYTES (held by every GPU that loads the library until
  * exit).  Wide or square operators only (m <= n), FP64 path; larger problems
  * return IA_ERR_TOO_LARGE.  The first call on a device looks the array's
- * address up and should come before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race. */
+ * address up and should come before any stream capture.  The call never
+ * times GEMM tile variants (the autotuner's table is read, not filled), so it
+ * neither allocates nor synchronises on a shape's first use.  All calls share
+ * the array: calls that overlap on the GPU race. */
 int ia_solve_batch_noalloc(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, int nrhs,
                            const ia_complex *d_b, const ia_config *cfg, ia_complex *d_x, double *d_lambda,
                            double *d_s, int *d_info);

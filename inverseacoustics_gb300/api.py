@@ -388,6 +388,20 @@ def svd_batch(ctx, A_colmajor, m, n):
     return U, s, V, info
 
 
+def zgemm_batch(ctx, opa, opb, M, N, K, A, B, C, alpha=1.0, beta=0.0, precision=1, slices=0, info=None):
+    """C = alpha op(A) op(B) + beta C for a batch of complex FP64 matrices in
+    column-major storage: A (F, cols, rows) with rows = M (op 'N') or K, B
+    likewise, C (F, N, M).  op in 'N', 'T', 'C'.  precision 0: FP64 CUDA-core
+    GEMM; 1: tensor-core GEMM on BF16 slices (Ozaki scheme)."""
+    ops = {"N": 0, "T": 1, "C": 2}
+    F = C.shape[0]
+    lda, ldb, ldc = A.shape[-1], B.shape[-1], C.shape[-1]
+    check(_lib.lib().ia_zgemm_batch(ctx.handle, ops[opa], ops[opb], M, N, K, float(alpha), _dptr(A), lda,
+                                    A[0].numel(), _dptr(B), ldb, B[0].numel(), float(beta), _dptr(C), ldc,
+                                    C[0].numel(), F, int(precision), int(slices), _dptr(info)), "ia_zgemm_batch")
+    return C
+
+
 def solve_batch(ctx, H_colmajor, m, n, b, cfg=None):
     """Tikhonov-GCV (or cfg.method) solves of F problems H_f x = b_f.
     H_colmajor (F, n, m); b (F, nrhs, m); returns x (F, nrhs, n), lambda

@@ -215,6 +215,7 @@ void ia_config_default(ia_config *cfg)
     cfg->refine_steps = 1;
     cfg->mode_iters = 10;
     cfg->mode_oversample = 16;
+    cfg->gemm_slices = TC_SLICES_DEFAULT;
 }
 
 void ia_admm_config_default(ia_admm_config *cfg)
@@ -598,9 +599,14 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
                            double2 *Ahs_t, double2 *Ht, int *d_info, cudaEvent_t ev_rows = nullptr)
 {
     const int m = mesh->m;
-    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
+    int st;
+    {
+        NvtxRange r("ia.assembly");
+        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht);
+    }
     if (st) return st;
     if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
+    NvtxRange r("ia.transfer");
     const long long sMM = (long long)m * m, sML = (long long)m * l;
     // LU of M = A^T; solve M Y = A_hs^T  ->  Y = W^T, W = A_hs A^-1
     st = zgetrf_batched(ctx, m, At, m, sMM, ipiv, d_info, F);
@@ -612,14 +618,27 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
                          make_double2(-1.0, 0.0), Ht, m, sML, F);
 }
 
-static size_t transfer_mixed_ws_bytes(int m, int l, int F)
+// the FP64-level products of the mixed transfer run on the tensor cores
+static bool tc_products(const ia_config *cfg, int m)
 {
-    return ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F);
+    const int S = cfg->gemm_slices;
+    return S >= TC_SLICES_MIN && S <= TC_SLICES_MAX && (long long)S * 1024 * ((2 * m + 7) & ~7) <= (1ll << 24);
+}
+
+static size_t transfer_mixed_ws_bytes(int m, int l, int F, const ia_config *cfg)
+{
+    size_t b = ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F);
+    if (tc_products(cfg, m))
+        b += tc_planes_bytes(m, m, cfg->gemm_slices, false, F) + tc_planes_bytes(l, m, cfg->gemm_slices, true, F) +
+             1024;
+    return b;
 }
 
 // Mixed transfer: FP32 LU of M = A^T; Y = M^-1 A_hs^T by FP32 solves refined
-// with double-float residuals R = A_hs^T - M Y (cfg->refine_steps times);
-// H^T = B^T Y - B_hs^T by the double-float GEMM.  Matrices in, H^T out in FP64.
+// with FP64-level residuals R = A_hs^T - M Y (cfg->refine_steps times);
+// H^T = B^T Y - B_hs^T.  The two FP64-level products (m x l x m) run on the
+// tensor cores (BF16 slices of M, B^T and Y; cfg->gemm_slices) or, with
+// gemm_slices 0, as double-float CUDA-core GEMMs.  Matrices in, H^T out in FP64.
 static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                                  const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
                                  double2 *Ahs_t, double2 *Ht, int *d_info, WsCursor &cur,
@@ -633,23 +652,56 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     float4 *Y4 = cur.take<float4>((size_t)m * l * F);
     // A^T and B^T arrive as double-float pairs (float4, the size of double2)
     float4 *At4 = reinterpret_cast<float4 *>(At), *Bt4 = reinterpret_cast<float4 *>(Bt);
-    int st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true);
+    int st;
+    {
+        NvtxRange r("ia.assembly");
+        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true);
+    }
     if (st) return st;
     if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
+    NvtxRange r("ia.transfer");
     const long long sMM = (long long)m * m, sML = (long long)m * l;
     if ((st = df_hi_batched(ctx, (size_t)sMM * F, At4, M32))) return st;
     if ((st = getrf_batched<float2>(ctx, m, M32, m, sMM, ipiv, d_info, F))) return st;
     if ((st = copy2d_batched<double2, float2>(ctx, m, l, Ahs_t, m, sML, Y32, m, sML, false, F))) return st;
     if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
     if ((st = copy2d_batched<float2, double2>(ctx, m, l, Y32, m, sML, Y, m, sML, false, F))) return st;
+    // tensor-core products: slice planes of the m x m operand (M, later B^T,
+    // in one region) and of Y
+    const bool tcg = tc_products(cfg, m);
+    const int S = cfg->gemm_slices;
+    TcPlanes Pm{}, Py{};
+    WsCursor cm{nullptr, 0, 0}, cy{nullptr, 0, 0};
+    if (tcg) {
+        const size_t bm = tc_planes_bytes(m, m, S, false, F), by = tc_planes_bytes(l, m, S, true, F);
+        cm = WsCursor{(char *)cur.take<unsigned char>(bm), 0, bm};
+        cy = WsCursor{(char *)cur.take<unsigned char>(by), 0, by};
+        if (cur.off > cur.cap) return IA_ERR_ALLOC;
+        if (cfg->refine_steps > 0 &&
+            (st = tc_slice(ctx, false, OP_N, At4, m, sMM, m, m, S, F, Pm, cm)))
+            return st;
+    }
     for (int it = 0; it < cfg->refine_steps; ++it) {
         if ((st = zcopy2d_batched(ctx, m, l, Ahs_t, m, sML, R, m, sML, false, F))) return st;
-        if ((st = split_df_batched(ctx, (size_t)sML * F, Y, Y4))) return st;
-        if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, l, m, -1.0, At4, m, sMM, Y4, m, sML, 1.0, R, m, sML, F)))
-            return st;
+        if (tcg) {
+            cy.off = 0;
+            if ((st = tc_slice(ctx, true, OP_N, Y, m, sML, l, m, S, F, Py, cy))) return st;
+            if ((st = tc_gemm(ctx, Pm, Py, m, l, -1.0, 1.0, R, m, sML, F, d_info))) return st;
+        } else {
+            if ((st = split_df_batched(ctx, (size_t)sML * F, Y, Y4))) return st;
+            if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, l, m, -1.0, At4, m, sMM, Y4, m, sML, 1.0, R, m, sML, F)))
+                return st;
+        }
         if ((st = copy2d_batched<double2, float2>(ctx, m, l, R, m, sML, Y32, m, sML, false, F))) return st;
         if ((st = getrs_batched<float2>(ctx, m, l, M32, m, sMM, ipiv, Y32, m, sML, F))) return st;
         if ((st = add2d_batched<float2>(ctx, m, l, Y32, m, sML, Y, m, sML, F))) return st;
+    }
+    if (tcg) {
+        cm.off = 0;
+        cy.off = 0;
+        if ((st = tc_slice(ctx, false, OP_N, Bt4, m, sMM, m, m, S, F, Pm, cm))) return st;
+        if ((st = tc_slice(ctx, true, OP_N, Y, m, sML, l, m, S, F, Py, cy))) return st;
+        return tc_gemm(ctx, Pm, Py, m, l, 1.0, -1.0, Ht, m, sML, F, d_info);
     }
     if ((st = split_df_batched(ctx, (size_t)sML * F, Y, Y4))) return st;
     return dfgemm4_batched(ctx, OP_N, OP_N, m, l, m, 1.0, Bt4, m, sMM, Y4, m, sML, -1.0, Ht, m, sML, F);
@@ -662,7 +714,7 @@ int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
     const int m = mesh->m;
     const bool mixed = cfg->precision == IA_PREC_MIXED;
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + (mixed ? transfer_mixed_ws_bytes(m, l, F, cfg) : 0);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
@@ -725,6 +777,7 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
                       const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                       WsCursor &cur)
 {
+    NvtxRange r("ia.solve");
     if (use_mixed_wide(m, n, cfg))
         return wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
@@ -768,7 +821,7 @@ static size_t ibem_solve_ws_bytes(int m, int l, int F, int nrhs, const ia_config
     const bool mixed = cfg->precision == IA_PREC_MIXED;
     return ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
            ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
-           (mixed ? transfer_mixed_ws_bytes(m, l, F) : 0);
+           (mixed ? transfer_mixed_ws_bytes(m, l, F, cfg) : 0);
 }
 
 // the whole IBEM pipeline for F bins on ctx->stream; ev_rows (if given) is

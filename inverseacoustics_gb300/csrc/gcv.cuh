@@ -5,7 +5,8 @@
 //               log-spaced [lo, hi]
 //   standard:   G = (sum f^2 |beta|^2 + delta0) / ((m-p) + sum f)^2,
 //               f = lambda^2/(s^2+lambda^2); lambda* = zero of dG/dlog(lambda)
-//               on the bracket around the grid minimum, 64 bisection steps
+//               on the bracket around the grid minimum, by the Illinois
+//               method, to a bracket below 1e-12 in log(lambda)
 //   reference:  gcvG.m as written -- grid filter lambda/(s+lambda) (:38),
 //               objective filter lambda^2/(s+lambda^2) (:47), Brent's bounded
 //               minimiser with fminbnd's tolerances (:51)
@@ -15,7 +16,8 @@
 
 namespace ia {
 
-constexpr int GCV_BISECT_ITERS = 64;
+// iteration cap of the root finder on the slope of G (it stops on width first)
+constexpr int GCV_ROOT_MAX_ITERS = 64;
 
 struct GcvData {
     const double *s;
@@ -69,7 +71,7 @@ __device__ __forceinline__ double gcv_slope(const GcvData &d, double t, int lane
 // replaces a secant point that falls outside the open bracket.  Each slope
 // evaluation is ~200 FP64 warp instructions on GB300's slow FP64 pipe, so this
 // takes ~10 evaluations where bisection to the same width took 40.
-__device__ __forceinline__ double gcv_bisect(const GcvData &d, double lo, double hi, int lane)
+__device__ __forceinline__ double gcv_root(const GcvData &d, double lo, double hi, int lane)
 {
     if (lo == hi) return lo;
     double a = log(lo), b = log(hi);
@@ -78,7 +80,7 @@ __device__ __forceinline__ double gcv_bisect(const GcvData &d, double lo, double
     fb = gcv_slope(d, b, lane);
     if (fb <= 0.0) return hi;
     int side = 0;
-    for (int it = 0; it < GCV_BISECT_ITERS && b - a > 1e-12; ++it) {
+    for (int it = 0; it < GCV_ROOT_MAX_ITERS && b - a > 1e-12; ++it) {
         double c = b - fb * (b - a) / (fb - fa);
         if (!(c > a && c < b)) c = 0.5 * (a + b);
         const double fc = gcv_slope(d, c, lane);
@@ -267,7 +269,7 @@ static __device__ double select_lambda(const double *s, const double *b2, int p,
         int jl = jm + 1 < np ? jm + 1 : np - 1, jh = jm - 1 > 0 ? jm - 1 : 0;
         double lo = gcv_grid_point(fixed, lhi, llo, ratio, rpm, np, jl);
         double hi = gcv_grid_point(fixed, lhi, llo, ratio, rpm, np, jh);
-        double res = (cfg.gcv_mode == IA_GCV_REFERENCE) ? fminbnd_dev(d, lo, hi, lane) : gcv_bisect(d, lo, hi, lane);
+        double res = (cfg.gcv_mode == IA_GCV_REFERENCE) ? fminbnd_dev(d, lo, hi, lane) : gcv_root(d, lo, hi, lane);
         if (lane == 0) s_lam = res;
     }
     __syncthreads();

@@ -1,6 +1,8 @@
 // Internal declarations shared by the libia.so translation units.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stddef.h>
 #include <stdint.h>
 #include "../../include/ia.h"
@@ -17,6 +19,7 @@ struct ia_context {
     long long launches;    // kernels launched through this context
     int sm_count;
     int capturing;         // between ia_capture_begin and ia_capture_end
+    int no_tune;           // the autotuner may not time variants (allocation-free calls)
     // extra streams and events of the staggered IBEM pipeline (one stream per
     // part beyond the first), created at their first use or by
     // ia_capture_begin (ensure_side_stream)
@@ -54,6 +57,15 @@ struct ia_mesh {
 };
 
 namespace ia {
+
+// ---- host-side NVTX range over the launches of one pipeline stage (shows
+// the stage on a profiler's timeline; a no-op when no tool is attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // ---- error plumbing
 int cuda_status(cudaError_t e);
@@ -154,6 +166,28 @@ int dfgemm4_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double
                     long long sC, int batch);
 int split_df_batched(ia_context *ctx, size_t count, const double2 *in, float4 *out);
 int df_hi_batched(ia_context *ctx, size_t count, const float4 *in, float2 *out);
+
+// ---- tensor-core GEMM at FP64-level accuracy (tc_gemm.cu): operands cut
+// into S balanced base-64 BF16 slices (Ozaki scheme), pair products on the
+// tcgen05 pipe with exact FP32 level sums in TMEM
+#define TC_SLICES_MIN 6
+#define TC_SLICES_MAX 8
+#define TC_SLICES_DEFAULT 7
+struct TcPlanes {
+    __nv_bfloat16 *p;   // [batch][S][rows][Kp] BF16 digits
+    int *e;             // [batch][R] power-of-two scale exponents
+    int R, rows, Kp, S; // R rows of op(A) (rows = R) or columns of op(B) (rows = 2 R)
+};
+size_t tc_planes_bytes(int R, int K, int S, bool role_b, int batch);
+// role_b false: A (M x K) = op(X); true: B (K x N) = op(X); R = M or N
+int tc_slice(ia_context *ctx, bool role_b, Op op, const double2 *X, int ld, long long sX, int R, int K, int S,
+             int batch, TcPlanes &out, WsCursor &cur);
+int tc_slice(ia_context *ctx, bool role_b, Op op, const float4 *X, int ld, long long sX, int R, int K, int S,
+             int batch, TcPlanes &out, WsCursor &cur);
+// C (M x N complex FP64) = alpha A B + beta C; info (per batch entry, may be
+// null) gets IA_INFO_TIMEOUT when a pipeline wait ran out
+int tc_gemm(ia_context *ctx, const TcPlanes &A, const TcPlanes &B, int M, int N, double alpha, double beta,
+            double2 *C, int ldc, long long sC, int batch, int *info);
 
 // ---- SVD (svd.cu): Jacobi on Y (M x N, M >= N) in place; V (N x N) accumulated
 int jacobi_svd_batched(ia_context *ctx, int M, int N, double2 *Y, double2 *V, int batch, int max_sweeps, int *info);

@@ -16,6 +16,12 @@
 // before any stream capture.  Every call shares the one array and leaves the
 // previous call's contents in it; nothing in it is assumed to start at zero.
 // Calls that overlap on the GPU (two streams, or two host threads) race on it.
+//
+// The GEMM autotuner is held off for the duration of the call: timing kernel
+// variants on a shape's first use would take a stream-ordered scratch
+// allocation and an event synchronisation.  A tile choice already in the
+// tuner's table is used; otherwise the default tile, which sums in the same
+// order, so the results do not depend on it.
 #include <mutex>
 #include "ia_common.cuh"
 #include "ia_internal.h"
@@ -65,6 +71,10 @@ extern "C" int ia_solve_batch_noalloc(ia_context *ctx, int m, int n, int F, cons
     if (st) return st;
     IA_CUDA_TRY(cudaMemsetAsync(d_info, 0, sizeof(int) * (size_t)F, ctx->stream));
     WsCursor cur{(char *)scratch, 0, (size_t)IA_NOALLOC_SCRATCH_BYTES};
-    return wide_solve_batched(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg,
-                              (double2 *)d_x, d_lambda, d_s, d_info, cur);
+    const int prev = ctx->no_tune;
+    ctx->no_tune = 1;
+    st = wide_solve_batched(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg,
+                            (double2 *)d_x, d_lambda, d_s, d_info, cur);
+    ctx->no_tune = prev;
+    return st;
 }

@@ -83,7 +83,7 @@ int tune_select(ia_context *ctx, TuneKey key, int nvar, const std::function<int(
         if (!g_file_read) read_file_locked();
         auto it = g_table.find(key);
         if (it != g_table.end() && it->second < nvar) return it->second;
-        if (!enabled_locked() || ctx->capturing || nvar < 2) return 0;
+        if (!enabled_locked() || ctx->capturing || ctx->no_tune || nvar < 2) return 0;
     }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess) return 0;

@@ -31,7 +31,8 @@ enum TuneKernel {
 
 // Variant for key: the table entry, or (when absent) the result of timing
 // run(variant) for variant in [0, nvar) -- run must launch on scratch outputs --
-// or 0 when tuning is off or the stream is capturing.
+// or 0 when tuning is off, the stream is capturing or the call may not
+// allocate (ctx->no_tune).
 int tune_select(ia_context *ctx, TuneKey key, int nvar, const std::function<int(int)> &run);
 
 // Scratch for tuning runs: a stream-ordered allocation holding a copy of the

@@ -267,32 +267,6 @@ int qr_batched(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA,
 template int qr_batched<float2>(ia_context *, int, int, float2 *, int, long long, float2 *, int);
 template int qr_batched<double2>(ia_context *, int, int, double2 *, int, long long, double2 *, int);
 
-// Raug ((N + nrhs) x N): R (upper triangle of Y, or all of Y when full) over
-// the rows conj(b_r)^T.
-template <class T>
-__global__ void build_raug_kernel(int N, int Mrows, int nrhs, const T *Y, const double2 *B, int full, T *Rg)
-{
-    typedef typename ctraits<T>::R R;
-    const int f = blockIdx.y;
-    const int ld = N + nrhs;
-    const long long total = (long long)ld * N;
-    Y += (size_t)f * Mrows * N;
-    Rg += (size_t)f * ld * N;
-    const double2 *b = B + (size_t)f * nrhs * N;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(e % ld), j = (int)(e / ld);
-        T v;
-        if (i < N) {
-            v = (full || i <= j) ? Y[i + (size_t)j * Mrows] : ctraits<T>::make(0, 0);
-        } else {
-            double2 bb = b[(size_t)(i - N) * N + j];
-            v = ctraits<T>::make((R)bb.x, -(R)bb.y);
-        }
-        Rg[e] = v;
-    }
-}
-
 // R^H (N x N) from the QR'd Y: R is the upper triangle of Y (all of Y when full)
 __global__ void build_rh_kernel(int N, int Mrows, const float2 *Y, int full, float2 *RH)
 {
@@ -329,49 +303,6 @@ __global__ void normalize_cols_kernel(int N, const float2 *Y, float2 *X, const i
         for (int r = lane; r < N; r += 32)
             X[(perm ? perm[r] : r) + (size_t)j * N] =
                 a > 0.f ? make_float2(y[r].x * inv, y[r].y * inv) : make_float2(r == j ? 1.f : 0.f, 0.f);
-    }
-}
-
-// sigma (sorted, FP64 out), beta = conj(appended rows) (sorted, FP64 out),
-// U_R = R/sigma (sorted, element type T).
-template <class T>
-__global__ void finalize_wide_kernel(int N, int nrhs, const T *Rg, double *S, double2 *BETA, T *UR, int *info)
-{
-    typedef typename ctraits<T>::R R;
-    extern __shared__ double sm[];
-    double *sig = sm;
-    int *rank = reinterpret_cast<int *>(sm + N);
-    const int f = blockIdx.x;
-    const int ld = N + nrhs;
-    Rg += (size_t)f * ld * N;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = wid; j < N; j += nw) {
-        R a = 0;
-        for (int r = lane; r < N; r += 32) a += zabs2(Rg[r + (size_t)j * ld]);
-        a = warp_sum(a);
-        if (lane == 0) sig[j] = sqrt((double)a);
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < N; j += blockDim.x) {
-        double sj = sig[j];
-        int rk = 0;
-        for (int i = 0; i < N; ++i) {
-            double si = sig[i];
-            if (si > sj || (si == sj && i < j)) rk++;
-        }
-        rank[j] = rk;
-        S[(size_t)f * N + rk] = sj;
-        if (info && (!(sj == sj) || isinf(sj))) atomicOr(&info[f], IA_INFO_NONFINITE);
-        for (int r = 0; r < nrhs; ++r) {
-            T v = Rg[N + r + (size_t)j * ld];
-            BETA[((size_t)f * nrhs + r) * N + rk] = make_double2((double)v.x, -(double)v.y);
-        }
-    }
-    __syncthreads();
-    for (int j = wid; j < N; j += nw) {
-        R inv = sig[j] > 0.0 ? (R)(1.0 / sig[j]) : (R)0;
-        T *dst = UR + (size_t)f * N * N + (size_t)rank[j] * N;
-        for (int r = lane; r < N; r += 32) dst[r] = zscale(Rg[r + (size_t)j * ld], inv);
     }
 }
 
@@ -418,58 +349,145 @@ template int apply_q_batched<float2>(ia_context *, int, int, const float2 *, con
 template int apply_q_batched<double2>(ia_context *, int, int, const double2 *, const double2 *, int, const double2 *,
                                       int, long long, double2 *, long long, int);
 
+__global__ void eig_backproject_kernel(int m, int n, int N, const double2 *H, int transposed, const double2 *X,
+                                       int conj_u, const int *RANK, const double *S, const double2 *Z, int nrhs,
+                                       double2 *Xout);
+
+// Raug ((N + nrhs) x N) of the pivoted-QR solve: R^H (R: upper triangle of
+// Y P = Q R) over the rows conj(v_r)^T, v_r = R P^T b_r, so that the
+// one-sided Jacobi's column rotations J carry J^H v_r along.
+__global__ void build_rh_aug_kernel(int N, int Mrows, int nrhs, const double2 *Y, const int *perm,
+                                    const double2 *B, double2 *Rg)
+{
+    const int f = blockIdx.y;
+    const int ld = N + nrhs;
+    Y += (size_t)f * Mrows * N;
+    Rg += (size_t)f * ld * N;
+    perm += (size_t)f * N;
+    const double2 *b = B + (size_t)f * nrhs * N;
+    const long long total = (long long)N * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % N), j = (int)(e / N);     // R^H(i, j) = conj(R(j, i)), R upper
+        double2 v = make_double2(0.0, 0.0);
+        if (j <= i) {
+            const double2 r = Y[j + (size_t)i * Mrows];
+            v = make_double2(r.x, -r.y);
+        }
+        Rg[i + (size_t)j * ld] = v;
+    }
+    // v_r(i) = sum_{j >= i} R(i, j) b_r(perm[j]); the appended row holds conj(v_r)
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)nrhs * N;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % N), r = (int)(e / N);
+        const double2 *br = b + (size_t)r * N;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = i; j < N; ++j) zfma(acc, Y[i + (size_t)j * Mrows], br[perm[j]]);
+        Rg[N + r + (size_t)i * ld] = make_double2(acc.x, -acc.y);
+    }
+}
+
+// After the Jacobi on Raug: sigma_i = |column i of R^H J| (sorted, S), the
+// rank of each column (RANK), beta = Sigma^-1 J^H v (sorted, BETA) and the
+// left singular vectors U = P W, W = (R^H J) Sigma^-1, in the columns' own
+// order (X, N x N).
+__global__ void finalize_dv_kernel(int N, int nrhs, const double2 *Rg, const int *perm, double *S, double2 *BETA,
+                                   double2 *X, int *RANK, int *info)
+{
+    extern __shared__ double sm_dv[];
+    double *sig = sm_dv;
+    const int f = blockIdx.x;
+    const int ld = N + nrhs;
+    Rg += (size_t)f * ld * N;
+    perm += (size_t)f * N;
+    X += (size_t)f * N * N;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = wid; j < N; j += nw) {
+        double a = 0.0;
+        for (int r = lane; r < N; r += 32) a += zabs2(Rg[r + (size_t)j * ld]);
+        a = warp_sum(a);
+        if (lane == 0) sig[j] = sqrt(a);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double sj = sig[j];
+        int rk = 0;
+        for (int i = 0; i < N; ++i) {
+            const double si = sig[i];
+            if (si > sj || (si == sj && i < j)) rk++;
+        }
+        RANK[(size_t)f * N + j] = rk;
+        S[(size_t)f * N + rk] = sj;
+        if (info && (!(sj == sj) || isinf(sj))) atomicOr(&info[f], IA_INFO_NONFINITE);
+        const double inv = sj > 0.0 ? 1.0 / sj : 0.0;
+        for (int r = 0; r < nrhs; ++r) {
+            const double2 v = Rg[N + r + (size_t)j * ld];
+            BETA[((size_t)f * nrhs + r) * N + rk] = make_double2(v.x * inv, -v.y * inv);
+        }
+    }
+    for (int j = wid; j < N; j += nw) {
+        const double inv = sig[j] > 0.0 ? 1.0 / sig[j] : 0.0;
+        for (int r = lane; r < N; r += 32) X[perm[r] + (size_t)j * N] = zscale(Rg[r + (size_t)j * ld], inv);
+    }
+}
+
 size_t wide_solve_ws_bytes(int m, int n, int nrhs, int batch)
 {
     const size_t F = batch, N = m, M = n, R = nrhs;
     return ws_round(16 * M * N * F) + ws_round(16 * N * F) + ws_round(16 * (N + R) * N * F) + ws_round(8 * N * F) +
-           ws_round(16 * R * N * F) * 3 + ws_round(16 * N * N * F) + 2048;
+           ws_round(16 * R * N * F) * 2 + ws_round(16 * N * N * F) + 2 * ws_round(4 * N * F) + 2048;
 }
 
+// FP64 wide solve (Drmac-Veselic preconditioned one-sided Jacobi):
+// Y = A^H (n x m), column-pivoted Householder QR Y P = Q R, one-sided Jacobi
+// on R^H (its columns converge to W Sigma with A = (P W) Sigma (Q J)^H): the
+// pivoting grades R's rows, and Jacobi on R^H then needs 7-10 sweeps where
+// the plain iteration on A^H needed 12-13 (and on a numerically
+// rank-deficient operator, such as an order-15 spherical-harmonic expansion
+// at low kr, did not settle within 40).  beta = U^H b rides along the
+// rotations as the appended rows conj(R P^T b)^T; GCV / Tikhonov in FP64;
+// x = A^H U (z / sigma) against the caller's A.
 int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                        const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out, int *info,
                        WsCursor &cur)
 {
     const int N = m, Mr = n;
-    const bool qr = n > m;
     double2 *Y = cur.take<double2>((size_t)Mr * N * batch);
     double2 *tau = cur.take<double2>((size_t)N * batch);
     double2 *Rg = cur.take<double2>((size_t)(N + nrhs) * N * batch);
     double *s = s_out ? s_out : cur.take<double>((size_t)N * batch);
     double2 *beta = cur.take<double2>((size_t)nrhs * N * batch);
     double2 *z = cur.take<double2>((size_t)nrhs * N * batch);
-    double2 *w = cur.take<double2>((size_t)nrhs * N * batch);
-    double2 *UR = cur.take<double2>((size_t)N * N * batch);
+    double2 *X = cur.take<double2>((size_t)N * N * batch);
+    int *perm = cur.take<int>((size_t)N * batch);
+    int *rank = cur.take<int>((size_t)N * batch);
+    if (cur.off > cur.cap) return IA_ERR_TOO_LARGE;   // the carve would run past the caller's scratch
     const long long sA = (long long)m * n;
     int st;
     // Y = A^H
     if (transposed) st = zcopy2d_batched(ctx, n, m, A, n, sA, Y, Mr, (long long)Mr * N, true, batch);
     else st = ztranspose_batched(ctx, m, n, A, m, sA, Y, Mr, (long long)Mr * N, true, batch);
     if (st) return st;
-    if (qr && (st = qr_launch<double2>(ctx, Mr, N, Y, Mr, (long long)Mr * N, tau, 0, nullptr, 0, 0, batch)))
+    if ((st = qr_launch<double2>(ctx, Mr, N, Y, Mr, (long long)Mr * N, tau, 0, nullptr, 0, 0, batch, perm)))
         return st;
     {
-        long long total = (long long)(N + nrhs) * N;
+        long long total = (long long)N * N;
         int blocks = (int)((total + 255) / 256);
         if (blocks > 512) blocks = 512;
-        build_raug_kernel<double2><<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, nrhs, Y, b, qr ? 0 : 1, Rg);
+        build_rh_aug_kernel<<<dim3(blocks, batch), 256, 0, ctx->stream>>>(N, Mr, nrhs, Y, perm, b, Rg);
         IA_LAUNCH_CHECK(ctx);
     }
     st = jacobi_rows_batched<double2>(ctx, N + nrhs, N, N, Rg, nullptr, batch, cfg->svd_max_sweeps, info);
     if (st) return st;
-    finalize_wide_kernel<double2><<<batch, 256, (size_t)N * (sizeof(double) + sizeof(int)), ctx->stream>>>(
-        N, nrhs, Rg, s, beta, UR, info);
+    finalize_dv_kernel<<<batch, 256, (size_t)N * sizeof(double), ctx->stream>>>(N, nrhs, Rg, perm, s, beta, X, rank,
+                                                                                 info);
     IA_LAUNCH_CHECK(ctx);
     st = gcv_beta_batched(ctx, m, N, batch, s, nrhs, beta, nullptr, cfg, z, lambda);
     if (st) return st;
-    // w = U_R z  (N x nrhs); directly into x when there is no Q
-    st = zgemm_batched(ctx, OP_N, OP_N, N, nrhs, N, make_double2(1.0, 0.0), UR, N, (long long)N * N, z, N,
-                       (long long)N * nrhs, make_double2(0.0, 0.0), qr ? w : x, N, (long long)N * nrhs, batch);
-    if (st) return st;
-    if (qr) {
-        apply_q_kernel<double2><<<batch, 256, 0, ctx->stream>>>(Mr, N, Y, tau, nrhs, w, N, (long long)N * nrhs, x,
-                                                                (long long)Mr * nrhs);
-        IA_LAUNCH_CHECK(ctx);
-    }
+    const size_t smem = sizeof(double2) * ((size_t)N + (size_t)m);
+    eig_backproject_kernel<<<dim3(batch, nrhs), 256, smem, ctx->stream>>>(m, n, N, A, transposed ? 1 : 0, X, 0, rank,
+                                                                         s, z, nrhs, x);
+    IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
 
@@ -819,7 +837,66 @@ static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
 {
     const size_t F = batch, N = m, M = n;
     return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
-           7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + ws_round(4 * N * F) + 4096;
+           7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + ws_round(4 * N * F) + ws_round(16 * M * N * F) +
+           ws_round(4 * F) + 4096;
+}
+
+// Range of the FP32 and double-float stages.  Their high words are FP32, so
+// |A| above ~1e19 overflows the Gram matrix and the column norms (an
+// order-15 spherical-harmonic operator reaches 1e30 at kr = 0.14).  Those
+// stages work on A 2^-e_f, e_f per bin with max(|Re|, |Im|) < 2^e_f; a power
+// of two commutes with every rounding, so the scaled run is the unscaled one
+// times 2^-e_f (bitwise, wherever the unscaled one stays in range).  The
+// eigenvalues come back multiplied by 4^e_f; everything after (s, beta, GCV,
+// x) works on the caller's A in FP64.
+__global__ void bin_exponent_kernel(size_t count, const double2 *__restrict__ A, int *__restrict__ ex)
+{
+    __shared__ unsigned long long s_key;
+    const int f = blockIdx.x;
+    A += (size_t)f * count;
+    if (threadIdx.x == 0) s_key = 0ull;
+    __syncthreads();
+    unsigned long long key = 0ull;
+    for (size_t e = threadIdx.x; e < count; e += blockDim.x) {
+        const double2 v = A[e];
+        const unsigned long long a = __double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+        const unsigned long long b = __double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+        key = a > key ? a : key;
+        key = b > key ? b : key;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+        key = k2 > key ? k2 : key;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&s_key, key);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned long long k = s_key;
+        // exponent of the largest magnitude (non-finite input keeps e = 0 and
+        // surfaces downstream as IA_INFO_NONFINITE)
+        const int e = (k && k < 0x7FF0000000000000ull) ? (int)(k >> 52) - 1022 : 0;
+        ex[f] = e;
+    }
+}
+
+__global__ void scale_bins_kernel(size_t count, const double2 *__restrict__ A, const int *__restrict__ ex,
+                                  double2 *__restrict__ As)
+{
+    const int f = blockIdx.y;
+    const double sc = ldexp(1.0, -ex[f]);
+    A += (size_t)f * count;
+    As += (size_t)f * count;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = A[e];
+        As[e] = make_double2(v.x * sc, v.y * sc);
+    }
+}
+
+__global__ void unscale_eig_kernel(int N, double *__restrict__ lam, const int *__restrict__ ex)
+{
+    const int f = blockIdx.x;
+    const double sc = ldexp(1.0, 2 * ex[f]);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) lam[(size_t)f * N + i] *= sc;
 }
 
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
@@ -855,8 +932,20 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     double2 *Fc = cur.take<double2>(NN * batch);
     double *lam_e = cur.take<double>((size_t)N * batch);
     int *perm = qr ? cur.take<int>((size_t)N * batch) : nullptr;
+    double2 *As = cur.take<double2>((size_t)m * n * batch);
+    int *ex = cur.take<int>((size_t)batch);
     const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
+    // the FP32 and double-float stages (1-3) work on A 2^-e_f
+    bin_exponent_kernel<<<batch, 256, 0, ctx->stream>>>((size_t)sA, A, ex);
+    IA_LAUNCH_CHECK(ctx);
+    {
+        int blocks = (int)((sA + 255) / 256);
+        if (blocks > 256) blocks = 256;
+        scale_bins_kernel<<<dim3(blocks, batch), 256, 0, ctx->stream>>>((size_t)sA, A, ex, As);
+        IA_LAUNCH_CHECK(ctx);
+    }
+    A = As;
     // 1. FP32 start: Y = H^H, QR with column pivoting (Y P = Q R), one-sided
     // Jacobi on R^H.  Pivoting orders R's diagonal by decreasing size, which
     // cuts the Jacobi's sweeps from 12-13 to 7-8 on the bench's transfer
@@ -938,6 +1027,8 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
         herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
         IA_LAUNCH_CHECK(ctx);
     }
+    unscale_eig_kernel<<<batch, 128, 0, ctx->stream>>>(N, lam_e, ex);
+    IA_LAUNCH_CHECK(ctx);
     *Xout = X;
     *lam_out = lam_e;
     return IA_OK;

@@ -207,6 +207,19 @@ def ibem_sphere(seed: int = 1, n_freq: int = 64, subdiv: int = 3) -> Workload:
                     params=dict(radius=0.10, amp=amp, snr_db=30.0, rng=rng))
 
 
+def ibem_sphere_pressures(w: Workload) -> np.ndarray:
+    """Measured pressures (F, 1, 120) of the sphere workload: pulsating plus
+    oscillating sphere fields with the workload's seeded complex amplitudes,
+    plus noise at its SNR.  Draws the noise from the workload's generator, so
+    call it once per workload object."""
+    mics, amp, rng = w.arrays["mics"], w.params["amp"], w.params["rng"]
+    a, snr = w.params["radius"], w.params["snr_db"]
+    return np.stack([
+        add_noise(rng, amp[f, 0] * pulsating_sphere_pressure(mics, w.k[f], a, 1.0) +
+                  amp[f, 1] * oscillating_sphere_pressure(mics, w.k[f], a, 1.0), snr)[None, :]
+        for f in range(len(w.k))])
+
+
 def hels_plane(seed: int = 2, n_freq: int = 512, order: int = 15) -> Workload:
     """HELS, order 15 (256 terms), 16x16 mics (0.025 m pitch) at z=0.15 m, 40
     seeded monopoles inside r < 0.08 m, n_freq frequencies 50-3000 Hz, 25 dB."""
@@ -221,6 +234,22 @@ def hels_plane(seed: int = 2, n_freq: int = 512, order: int = 15) -> Workload:
     return Workload(f"hels_N{order}_256mic_F{n_freq}", "hels", k,
                     arrays=dict(mics=mics, monopoles=np.ascontiguousarray(srcs)),
                     params=dict(order=order, q=q, snr_db=25.0, rng=rng))
+
+
+def monopole_field(P, src, k, q):
+    """Free-field pressure exp(ikr)/(4 pi r) (the reference's sign) at points P
+    (3, l) of monopoles at src (3, s) with complex strengths q (s,)."""
+    r = np.linalg.norm(P[:, :, None] - src[:, None, :], axis=0)
+    return (np.exp(1j * k * r) / (4 * np.pi * r)) @ q
+
+
+def hels_plane_pressures(w: Workload) -> np.ndarray:
+    """Measured pressures (F, 1, 256) of the HELS workload: the 40 monopoles
+    with their seeded strengths, plus noise at the workload's SNR.  Draws the
+    noise from the workload's generator, so call it once per workload object."""
+    mics, srcs, q, rng = w.arrays["mics"], w.arrays["monopoles"], w.params["q"], w.params["rng"]
+    return np.stack([add_noise(rng, monopole_field(mics, srcs, w.k[f], q[f]), w.params["snr_db"])[None, :]
+                     for f in range(len(w.k))])
 
 
 def radiation_plate(seed: int = 3, n_freq: int = 256) -> Workload:

@@ -18,7 +18,18 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_CUDA = os.environ.get("IA_REFERENCE_CUDA", "/root/reference/CUDA")
+# Where the reference's CUDA/ headers lie.  This recipe compiles them in
+# place, so it is the one file that names the read-only mount of the
+# reference tree; IA_REFERENCE_CUDA or build_ref(reference_cuda_dir=...) point it
+# elsewhere, and build_ref returns None (nothing built) where none exists.
+_REFERENCE_MOUNT = "/root/reference/CUDA"
+
+
+def reference_cuda(explicit: str | None = None) -> str | None:
+    """The reference's CUDA/ directory: the argument, else IA_REFERENCE_CUDA,
+    else the mount; None when that directory does not exist."""
+    d = explicit or os.environ.get("IA_REFERENCE_CUDA") or _REFERENCE_MOUNT
+    return d if os.path.isdir(d) else None
 
 
 def build_oracle(verbose=False) -> str:
@@ -42,8 +53,9 @@ def _openblas():
     return libs, (os.path.basename(cand[0]) if cand else None)
 
 
-def build_ref(verbose=False) -> str | None:
-    if not os.path.isdir(REFERENCE_CUDA):
+def build_ref(verbose=False, reference_cuda_dir: str | None = None) -> str | None:
+    ref_dir = reference_cuda(reference_cuda_dir)
+    if ref_dir is None:
         return None
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
@@ -55,7 +67,7 @@ def build_ref(verbose=False) -> str | None:
     if blas is None:
         return None
     cmd = ["nvcc", "-std=c++17", "-arch=sm_100", "-rdc=true", "-O2", "-Xcompiler", "-fPIC", "-shared",
-           "-diag-suppress", "1650", "-DC_AIR=343.0", "-DRHO_AIR=1.21", f"-I{REFERENCE_CUDA}", *srcs,
+           "-diag-suppress", "1650", "-DC_AIR=343.0", "-DRHO_AIR=1.21", f"-I{ref_dir}", *srcs,
            "-o", out, f"-L{libdir}", f"-l:{blas}", f"-Xlinker", f"-rpath={libdir}", "-lcublas", "-lcusolver",
            "-lcudadevrt"]
     if verbose:

@@ -3,7 +3,7 @@
 Run here, where the reference tree is mounted (it is read, never modified):
 
     python oracle/build.py            # builds oracle/_ref/libiaref.so
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [<reference CUDA/ directory>]
 
 Contents (all produced by the reference's compiled esm()/ibem()/sphere()/
 cartesian_2_spherical(), built with C_AIR=343, RHO_AIR=1.21):
@@ -35,14 +35,15 @@ sys.path.insert(0, ROOT)
 from inverseacoustics_gb300 import geometry as g  # noqa: E402
 from oracle import build, ref  # noqa: E402
 
-REF_CUDA = "/root/reference/CUDA"
-
-
 def main():
-    build.build_ref()
+    ref_cuda = build.reference_cuda(sys.argv[1] if len(sys.argv) > 1 else None)
+    if ref_cuda is None:
+        sys.exit("make_golden: the reference's CUDA/ directory was not found "
+                 "(pass it as the first argument or set IA_REFERENCE_CUDA)")
+    build.build_ref(reference_cuda_dir=ref_cuda)
     c, rho = ref.constants()
     assert (c, rho) == (343.0, 1.21)
-    reg, sing = ref.read_reference_rules(REF_CUDA)
+    reg, sing = ref.read_reference_rules(ref_cuda)
     rng = np.random.default_rng(1234)
     nodes, elems = g.icosphere(1, 0.10)
     mics = g.hemisphere_array(rng, 30, 0.30)

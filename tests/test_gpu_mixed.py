@@ -58,7 +58,15 @@ def test_mixed_assembly_large_arguments(cuda, ctx):
             assert relerr(b[f], a[f]) < 1e-12, f
 
 
-def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
+# FP64-level products of the refinement and the transfer GEMM: the
+# double-float CUDA-core GEMM (0) and the tensor-core GEMM on 7 (the default)
+# or 8 BF16 slices.  At 7 slices the product's own bound (8e-12 of the row and
+# column maxima per term) sets the floor near 5e-11 on these operators.
+SLICE_TOL = [(0, 1e-11), (7, 1e-10), (8, 1e-11)]
+
+
+@pytest.mark.parametrize("slices,tol", SLICE_TOL)
+def test_mixed_transfer_is_fp64_accurate(cuda, ctx, slices, tol):
     from inverseacoustics_gb300 import api
     import torch
     w = g.ibem_sphere(n_freq=64)
@@ -67,18 +75,21 @@ def test_mixed_transfer_is_fp64_accurate(cuda, ctx):
     mesh = api.Mesh(ctx, nodes, elems)
     H64, i64 = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda))
     Hmx, imx = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda),
-                                       api.default_config(precision=1, refine_steps=2))
+                                       api.default_config(precision=1, refine_steps=2, gemm_slices=slices))
     torch.cuda.synchronize()
     assert int(imx.abs().sum()) == 0
-    for f in range(len(ks)):
-        assert relerr(Hmx[f].cpu().numpy(), H64[f].cpu().numpy()) < 1e-11
+    errs = [relerr(Hmx[f].cpu().numpy(), H64[f].cpu().numpy()) for f in range(len(ks))]
+    print(f"\nmixed transfer, {slices} slices: H vs FP64 max {max(errs):.3e}")
+    assert max(errs) < tol
 
 
-def test_mixed_transfer_fp32_solve_and_refinement_steps(cuda, ctx):
+@pytest.mark.parametrize("slices,tol", SLICE_TOL)
+def test_mixed_transfer_fp32_solve_and_refinement_steps(cuda, ctx, slices, tol):
     """The FP32 LU solve alone (refine_steps = 0) against FP64: H within the
-    FP32 level (1e-4, with the sphere's condition numbers); each double-float
-    refinement step then gains several digits (1e-8 after one, 1e-11 after
-    two).  Catches a wrong but refinement-masked FP32 solve."""
+    FP32 level (1e-4, with the sphere's condition numbers); each refinement
+    step with FP64-level residuals then gains several digits (1e-8 after one,
+    the product's floor after two).  Catches a wrong but refinement-masked
+    FP32 solve."""
     from inverseacoustics_gb300 import api
     import torch
     w = g.ibem_sphere(n_freq=64)
@@ -89,11 +100,12 @@ def test_mixed_transfer_fp32_solve_and_refinement_steps(cuda, ctx):
     errs = []
     for steps in (0, 1, 2):
         H, info = api.ibem_transfer_batch(ctx, mesh, T(mics, cuda), T(ks, cuda),
-                                          api.default_config(precision=1, refine_steps=steps))
+                                          api.default_config(precision=1, refine_steps=steps,
+                                                             gemm_slices=slices))
         torch.cuda.synchronize()
         assert int(info.abs().sum()) == 0
         errs.append(max(relerr(H[f].cpu().numpy(), H64[f].cpu().numpy()) for f in range(len(ks))))
-    assert errs[0] < 1e-4 and errs[1] < 1e-8 and errs[2] < 1e-11, errs
+    assert errs[0] < 1e-4 and errs[1] < 1e-8 and errs[2] < tol, errs
     assert errs[1] < 1e-2 * errs[0]
 
 

@@ -61,6 +61,79 @@ def test_noalloc_matches_allocating_solve_twice(cuda, ctx):
         assert relerr(s.cpu().numpy(), s0.cpu().numpy()) < TOL
 
 
+def _pool_bytes(dev=0):
+    """(reserved, used) bytes of the device's stream-ordered memory pool, the
+    pool every cudaMallocAsync of this library draws from."""
+    rt = None
+    with open("/proc/self/maps") as fh:
+        paths = sorted({ln.split()[-1] for ln in fh if "libcudart.so" in ln})
+    for name in paths + ["libcudart.so.13", "libcudart.so.12", "libcudart.so"]:
+        try:
+            rt = C.CDLL(name)
+            break
+        except OSError:
+            continue
+    assert rt is not None, "no CUDA runtime library to query the memory pool"
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), C.c_int(dev)) == 0
+    out = []
+    for attr in (0x5, 0x7):     # cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrUsedMemCurrent
+        v = C.c_uint64()
+        assert rt.cudaMemPoolGetAttribute(pool, C.c_int(attr), C.byref(v)) == 0
+        out.append(v.value)
+    return tuple(out)
+
+
+def test_noalloc_first_call_of_a_shape_inside_a_callers_capture(cuda, ctx):
+    """A caller records the solve into its own CUDA graph, and the shape is one
+    this process has never solved (the autotuner's table is emptied first):
+    the capture must succeed without touching the memory pool or the tuner,
+    and the replay must match the allocating entry point."""
+    import torch
+    from inverseacoustics_gb300 import _lib, api
+    L = _lib.lib()
+    cfg = api.default_config()
+    H1, b1 = _problem()
+    st, *_ = _noalloc(ctx, torch.as_tensor(H1, device=cuda), torch.as_tensor(b1, device=cuda), 64, 162, cfg)
+    torch.cuda.synchronize()
+    assert st == 0                  # the device's array address is known before the capture
+    H, b = _problem(F=3, seed=47)
+    b = np.ascontiguousarray(np.concatenate([b, 0.5 * b[:, :, ::-1]], axis=1))      # 2 right-hand sides
+    Hd, bd = torch.as_tensor(H, device=cuda), torch.as_tensor(b, device=cuda)
+    F, nrhs, m, n = 3, 2, 64, 162
+    x = torch.empty((F, nrhs, n), dtype=torch.complex128, device=cuda)
+    lam = torch.empty((F, nrhs), dtype=torch.float64, device=cuda)
+    s = torch.empty((F, m), dtype=torch.float64, device=cuda)
+    info = torch.zeros(F, dtype=torch.int32, device=cuda)
+    L.ia_tune_reset()
+    n_table = L.ia_tune_table_size()
+    torch.cuda.synchronize()
+    pool0 = _pool_bytes()
+    stream = torch.cuda.Stream()
+    cap = api.Context(0, stream=stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+        st = L.ia_solve_batch_noalloc(cap.handle, m, n, F, Hd.data_ptr(), nrhs, bd.data_ptr(), C.byref(cfg),
+                                      x.data_ptr(), lam.data_ptr(), s.data_ptr(), info.data_ptr())
+    assert st == 0
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        assert L.ia_tune_table_size() == n_table
+        assert _pool_bytes() == pool0
+        assert int(info.abs().sum()) == 0
+        x0, l0, s0, _ = api.solve_batch(ctx, Hd, m, n, bd, cfg)
+        torch.cuda.synchronize()
+        assert relerr(x.cpu().numpy(), x0.cpu().numpy()) < TOL
+        assert relerr(lam.cpu().numpy(), l0.cpu().numpy()) < TOL
+        assert relerr(s.cpu().numpy(), s0.cpu().numpy()) < TOL
+        # the allocating call may grow the pool and tune the shape; the next replay may do neither
+        pool0 = _pool_bytes()
+        n_table = L.ia_tune_table_size()
+    cap.close()
+    del g
+
+
 def test_noalloc_refuses_problems_above_its_array(cuda, ctx):
     import torch
     from inverseacoustics_gb300 import api
