@@ -59,6 +59,8 @@ typedef enum {
 #define IA_INFO_SINGULAR  2  /* zero pivot */
 #define IA_INFO_NONFINITE 4  /* NaN/Inf met */
 #define IA_INFO_TIMEOUT   8  /* a bounded device-side wait ran out (the entry's output is not written) */
+#define IA_INFO_PRECISION 16 /* mixed path: the bin's result failed the precision guard (see mixed_guard) and
+                                was not recomputed in FP64 (fallback off, or the stream was capturing) */
 
 enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
 enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };
@@ -100,6 +102,14 @@ typedef struct {
     int gemm_slices;       /* the mixed path's FP64-level complex products (IBEM refinement residual and
                               transfer product): 6..8 = tensor-core GEMM on that many BF16 slices per
                               operand (default 7); 0 = double-float CUDA-core GEMM */
+    double mixed_guard;    /* mixed solves: the smallest lambda / s_1 (TSVD: s_k / s_1) the mixed path
+                              answers (default 1e-3).  Below it the Gram-based mixed eigensolver does not
+                              resolve the singular values that decide the solution, so the bin fails the
+                              precision guard, as does a bin with any info flag or whose sum of s_i^2
+                              misses ||H||_F^2 by more than 1e-10 relative. */
+    int mixed_fallback;    /* 1 (default): bins that fail the guard are solved again by the FP64 path
+                              before the call returns (one host synchronisation per call; skipped while
+                              the stream is capturing, where such bins keep IA_INFO_PRECISION); 0: never */
 } ia_config;
 
 /* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,
@@ -229,6 +239,11 @@ long long ia_launch_count(const ia_context *ctx);
  * file.  ia_tune_reset forgets the table and re-reads the environment. */
 int ia_tune_table_size(void);
 void ia_tune_reset(void);
+
+/* Number of bins the last batched solve on ctx (ia_solve_batch and the
+ * ia_*_solve_batch pipelines) handed from the mixed path to the FP64 path
+ * (mixed_fallback); 0 after an FP64 call.  No reference counterpart. */
+int ia_last_fallback_bins(const ia_context *ctx);
 
 typedef struct ia_graph ia_graph;
 int ia_capture_begin(ia_context *ctx);

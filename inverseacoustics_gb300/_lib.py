@@ -16,7 +16,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "allocatio
           4: "Jacobi iteration did not converge", 5: "singular matrix", 6: "non-finite value",
           7: "invalid quadrature rule", 8: "size above the entry point's limit",
           9: "workspace would grow during stream capture"}
-IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE, IA_INFO_TIMEOUT = 1, 2, 4, 8
+IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE, IA_INFO_TIMEOUT, IA_INFO_PRECISION = 1, 2, 4, 8, 16
 IA_GCV_STANDARD, IA_GCV_REFERENCE = 0, 1
 IA_PREC_FP64, IA_PREC_MIXED = 0, 1
 IA_METHOD_TIKHONOV_GCV, IA_METHOD_TSVD, IA_METHOD_TIKHONOV_FIXED = 0, 1, 2
@@ -35,7 +35,8 @@ class Config(C.Structure):
                 ("gcv_points", C.c_int), ("gcv_lo", C.c_double), ("gcv_hi", C.c_double),
                 ("lambda_fixed", C.c_double), ("tsvd_k", C.c_int), ("precision", C.c_int),
                 ("svd_max_sweeps", C.c_int), ("refine_steps", C.c_int), ("mode_iters", C.c_int),
-                ("mode_oversample", C.c_int), ("gemm_slices", C.c_int)]
+                ("mode_oversample", C.c_int), ("gemm_slices", C.c_int),
+                ("mixed_guard", C.c_double), ("mixed_fallback", C.c_int)]
 
 
 IA_ADMM_L1, IA_ADMM_L2, IA_ADMM_LP = 1, 2, 3
@@ -83,6 +84,7 @@ _SIGS = {
     "ia_launch_count": (C.c_longlong, [_P]),
     "ia_tune_table_size": (_I, []),
     "ia_tune_reset": (None, []),
+    "ia_last_fallback_bins": (_I, [_P]),
     "ia_capture_begin": (_I, [_P]),
     "ia_capture_end": (_I, [_P, _PP]),
     "ia_graph_launch": (_I, [_P]),

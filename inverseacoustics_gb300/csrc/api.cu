@@ -5,6 +5,8 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <functional>
+#include <initializer_list>
 #include <mutex>
 #include <vector>
 #include "ia_common.cuh"
@@ -197,6 +199,8 @@ using namespace ia;
 // =========================================================================
 extern "C" {
 
+int ia_last_fallback_bins(const ia_context *ctx) { return ctx ? ctx->last_fallback : 0; }
+
 void ia_config_default(ia_config *cfg)
 {
     if (!cfg) return;
@@ -216,6 +220,8 @@ void ia_config_default(ia_config *cfg)
     cfg->mode_iters = 10;
     cfg->mode_oversample = 16;
     cfg->gemm_slices = TC_SLICES_DEFAULT;
+    cfg->mixed_guard = 1e-3;
+    cfg->mixed_fallback = 1;
 }
 
 void ia_admm_config_default(ia_admm_config *cfg)
@@ -778,8 +784,15 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
                       WsCursor &cur)
 {
     NvtxRange r("ia.solve");
-    if (use_mixed_wide(m, n, cfg))
-        return wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
+    if (use_mixed_wide(m, n, cfg)) {
+        // lambda and s feed the precision guard, so they exist even when the
+        // caller does not ask for them
+        double *lam = lambda ? lambda : cur.take<double>((size_t)nrhs * F);
+        double *s = s_out ? s_out : cur.take<double>((size_t)m * F);
+        int st = wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lam, s, info, cur);
+        if (st) return st;
+        return mixed_guard_batched(ctx, (size_t)m * n, F, A, m, s, nrhs, lam, cfg, info);
+    }
     if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;
@@ -791,6 +804,105 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
     int st = svd_batched(ctx, m, n, A, transposed, U, s, V, F, cfg->svd_max_sweeps, info, Y, Vacc);
     if (st) return st;
     return regularize_batched(ctx, m, n, p, F, U, s, V, nrhs, b, cfg, x, lambda);
+}
+
+// ---- FP64 fallback of mixed solves ----------------------------------------
+// A per-bin array of an entry point: bin f's data at base + f * bytes
+// (base null: the caller did not ask for that output).
+struct BinSpan {
+    const void *base;
+    size_t bytes;
+};
+
+// gather (dst bin j <- src bin idx[j]) or scatter (dst bin idx[j] <- src bin
+// j) of Fb bins of `words` 32-bit words each; grid.y runs over the bins
+__global__ void move_bins_kernel(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst, size_t words,
+                                 const int *__restrict__ idx, int scatter)
+{
+    const int j = blockIdx.y;
+    const size_t so = (size_t)(scatter ? j : idx[j]) * words, d0 = (size_t)(scatter ? idx[j] : j) * words;
+    for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x)
+        dst[d0 + w] = src[so + w];
+}
+
+static int move_bins(ia_context *ctx, const void *src, void *dst, size_t bytes, const int *d_idx, int Fb,
+                     bool scatter)
+{
+    const size_t words = bytes / 4;
+    int blocks = (int)((words + 255) / 256);
+    if (blocks > 64) blocks = 64;
+    move_bins_kernel<<<dim3(blocks, Fb), 256, 0, ctx->stream>>>((const uint32_t *)src, (uint32_t *)dst, words, d_idx,
+                                                                scatter ? 1 : 0);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+// redo(Fb, in, out, info): the entry point in FP64 on Fb compact bins
+using RedoFn = std::function<int(int, void *const *, void *const *, int *)>;
+
+// After a batched solve issued on ctx->stream: with the mixed path and
+// cfg->mixed_fallback, the bins whose info word is set (the precision guard's
+// IA_INFO_PRECISION or any solver flag) are solved again by the FP64 path on
+// compact copies of their per-bin inputs, and the FP64 outputs and info words
+// replace the mixed ones.  One host synchronisation (the info words); nothing
+// happens while the stream is capturing, where the flags stay for the caller.
+// The index list and compact copies live in one stream-ordered allocation
+// that is released before the call returns.
+static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_info, std::initializer_list<BinSpan> ins,
+                         std::initializer_list<BinSpan> outs, const RedoFn &redo)
+{
+    ctx->last_fallback = 0;
+    if (cfg->precision != IA_PREC_MIXED || !cfg->mixed_fallback) return IA_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    IA_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone || ctx->capturing) return IA_OK;
+    std::vector<int> h((size_t)F);
+    IA_CUDA_TRY(cudaMemcpyAsync(h.data(), d_info, sizeof(int) * (size_t)F, cudaMemcpyDeviceToHost, ctx->stream));
+    IA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    std::vector<int> idx;
+    for (int f = 0; f < F; ++f)
+        if (h[f]) idx.push_back(f);
+    if (idx.empty()) return IA_OK;
+    const int Fb = (int)idx.size();
+    size_t bytes = 2 * ws_round(sizeof(int) * (size_t)Fb);
+    for (const BinSpan &a : ins) bytes += ws_round(a.bytes * Fb);
+    for (const BinSpan &a : outs) bytes += a.base ? ws_round(a.bytes * Fb) : 0;
+    char *blk = nullptr;
+    IA_CUDA_TRY(cudaMallocAsync((void **)&blk, bytes, ctx->stream));
+    WsCursor cur{blk, 0, bytes};
+    int *d_idx = cur.take<int>((size_t)Fb);
+    int *c_info = cur.take<int>((size_t)Fb);
+    std::vector<void *> cin, cout;
+    int st = IA_OK;
+    cudaError_t e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(int) * (size_t)Fb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) st = cuda_status(e);
+    for (const BinSpan &a : ins) {
+        void *c = cur.take<char>(a.bytes * Fb);
+        cin.push_back(c);
+        if (!st) st = move_bins(ctx, a.base, c, a.bytes, d_idx, Fb, false);
+    }
+    for (const BinSpan &a : outs) cout.push_back(a.base ? (void *)cur.take<char>(a.bytes * Fb) : nullptr);
+    if (!st) st = redo(Fb, cin.data(), cout.data(), c_info);
+    size_t i = 0;
+    for (const BinSpan &a : outs) {
+        if (!st && a.base) st = move_bins(ctx, cout[i], const_cast<void *>(a.base), a.bytes, d_idx, Fb, true);
+        ++i;
+    }
+    if (!st) st = move_bins(ctx, c_info, d_info, sizeof(int), d_idx, Fb, true);
+    e = cudaFreeAsync(blk, ctx->stream);
+    if (!st && e != cudaSuccess) st = cuda_status(e);
+    // the index list's host copy must outlive its transfer
+    e = cudaStreamSynchronize(ctx->stream);
+    if (!st && e != cudaSuccess) st = cuda_status(e);
+    if (!st) ctx->last_fallback = Fb;
+    return st;
+}
+
+static ia_config fp64_config(const ia_config *cfg)
+{
+    ia_config c = *cfg;
+    c.precision = IA_PREC_FP64;
+    return c;
 }
 
 static size_t solve_ws_bytes(int m, int n, int F, int nrhs, const ia_config *cfg)
@@ -812,8 +924,18 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
-    return solve_core(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg, (double2 *)d_x,
-                      d_lambda, d_s, d_info, cur);
+    st = solve_core(ctx, m, n, F, (const double2 *)d_H, false, nrhs, (const double2 *)d_b, cfg, (double2 *)d_x,
+                    d_lambda, d_s, d_info, cur);
+    if (st) return st;
+    const int p = m < n ? m : n;
+    return fp64_fallback(
+        ctx, cfg, F, d_info, {{d_H, 16 * (size_t)m * n}, {d_b, 16 * (size_t)nrhs * m}},
+        {{d_x, 16 * (size_t)nrhs * n}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
+        [&](int Fb, void *const *in, void *const *out, int *info) {
+            const ia_config c64 = fp64_config(cfg);
+            return ia_solve_batch(ctx, m, n, Fb, (const ia_complex *)in[0], nrhs, (const ia_complex *)in[1], &c64,
+                                  (ia_complex *)out[0], (double *)out[1], (double *)out[2], info);
+        });
 }
 
 static size_t ibem_solve_ws_bytes(int m, int l, int F, int nrhs, const ia_config *cfg)
@@ -867,13 +989,25 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     int st = ws_reserve(ctx, need * parts);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
+    const int p = l < m ? l : m;
+    auto fallback = [&]() {
+        return fp64_fallback(
+            ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
+            {{d_x, 16 * (size_t)nrhs * m}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
+            [&](int Fb, void *const *in, void *const *out, int *info) {
+                const ia_config c64 = fp64_config(cfg);
+                return ia_ibem_solve_batch(ctx, mesh, l, d_mics, Fb, (const double *)in[0], nrhs,
+                                           (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                           (double *)out[2], info);
+            });
+    };
     if (parts == 1) {
         WsCursor cur{(char *)ctx->ws, 0, ctx->ws_bytes};
-        return ibem_solve_part(ctx, mesh, l, d_mics, F, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x,
-                               d_lambda, d_s, d_info, cur, nullptr);
+        st = ibem_solve_part(ctx, mesh, l, d_mics, F, d_k, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda,
+                             d_s, d_info, cur, nullptr);
+        return st ? st : fallback();
     }
     if ((st = ensure_side_stream(ctx))) return st;
-    const int p = l < m ? l : m;
     cudaStream_t main = ctx->stream;
     cudaError_t e = cudaSuccess;
     int q = 0;
@@ -897,7 +1031,8 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         if (e == cudaSuccess) e = ej;
     }
     if (st) return st;
-    return e == cudaSuccess ? IA_OK : cuda_status(e);
+    if (e != cudaSuccess) return cuda_status(e);
+    return fallback();
 }
 
 int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, const double *d_src, int F,
@@ -914,8 +1049,19 @@ int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, cons
     double2 *G = cur.take<double2>((size_t)l * m * F);
     st = monopole_batched(ctx, l, m, F, d_mics, d_src, d_k, G);
     if (st) return st;
-    return solve_core(ctx, l, m, F, G, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
-                      cur);
+    st = solve_core(ctx, l, m, F, G, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
+                    cur);
+    if (st) return st;
+    const int p = l < m ? l : m;
+    return fp64_fallback(
+        ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
+        {{d_x, 16 * (size_t)nrhs * m}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
+        [&](int Fb, void *const *in, void *const *out, int *info) {
+            const ia_config c64 = fp64_config(cfg);
+            return ia_esm_solve_batch(ctx, l, m, d_mics, d_src, Fb, (const double *)in[0], nrhs,
+                                      (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                      (double *)out[2], info);
+        });
 }
 
 int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, int F, const double *d_k, int nrhs,
@@ -933,8 +1079,19 @@ int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, i
     double2 *H = cur.take<double2>((size_t)l * nt * F);
     st = hels_batched(ctx, l, d_pts, n_sh, F, d_k, cfg->c, cfg->rho, H, nullptr);
     if (st) return st;
-    return solve_core(ctx, l, nt, F, H, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
-                      cur);
+    st = solve_core(ctx, l, nt, F, H, false, nrhs, (const double2 *)d_p, cfg, (double2 *)d_x, d_lambda, d_s, d_info,
+                    cur);
+    if (st) return st;
+    const int p = l < nt ? l : nt;
+    return fp64_fallback(
+        ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
+        {{d_x, 16 * (size_t)nrhs * nt}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
+        [&](int Fb, void *const *in, void *const *out, int *info) {
+            const ia_config c64 = fp64_config(cfg);
+            return ia_hels_solve_batch(ctx, l, d_pts, n_sh, Fb, (const double *)in[0], nrhs,
+                                       (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                       (double *)out[2], info);
+        });
 }
 
 int ia_sinc_resistance_batch(ia_context *ctx, int n, const double *d_x, int F, const double *d_k, double area,

@@ -20,6 +20,7 @@ struct ia_context {
     int sm_count;
     int capturing;         // between ia_capture_begin and ia_capture_end
     int no_tune;           // the autotuner may not time variants (allocation-free calls)
+    int last_fallback;     // bins the last batched solve recomputed in FP64 (mixed_fallback)
     // extra streams and events of the staggered IBEM pipeline (one stream per
     // part beyond the first), created at their first use or by
     // ia_capture_begin (ensure_side_stream)
@@ -166,6 +167,12 @@ int dfgemm4_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double
                     long long sC, int batch);
 int split_df_batched(ia_context *ctx, size_t count, const double2 *in, float4 *out);
 int df_hi_batched(ia_context *ctx, size_t count, const float4 *in, float2 *out);
+
+// precision guard of the mixed wide solve: sets IA_INFO_PRECISION in info[f]
+// for a bin whose lambda (TSVD: s_k) is below cfg->mixed_guard s_1, or whose
+// sum of s^2 misses ||A_f||_F^2 by more than 1e-10 relative
+int mixed_guard_batched(ia_context *ctx, size_t count, int F, const double2 *A, int p, const double *s, int nrhs,
+                        const double *lambda, const ia_config *cfg, int *info);
 
 // ---- tensor-core GEMM at FP64-level accuracy (tc_gemm.cu): operands cut
 // into S balanced base-64 BF16 slices (Ozaki scheme), pair products on the

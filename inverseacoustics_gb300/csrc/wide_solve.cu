@@ -1034,6 +1034,54 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     return IA_OK;
 }
 
+// One CTA per bin: ||A_f||_F^2 in FP64 against sum s_i^2, and the smallest
+// regularisation level against s_1.  The mixed eigensolver reaches FP64-level
+// eigenpairs of H H^H (errors ~eps s_1^2), so a Tikhonov solution is good to
+// ~eps (s_1 / lambda)^2 and needs lambda well above sqrt(eps) s_1; below
+// cfg->mixed_guard the bin is marked for the FP64 path.  A broken
+// eigen-decomposition (an eigenvalue lost or doubled) shows in the trace.
+__global__ void precision_guard_kernel(size_t count, const double2 *__restrict__ A, int p,
+                                       const double *__restrict__ s, int nrhs, const double *__restrict__ lam,
+                                       int method, int tsvd_k, double ratio, int *__restrict__ info)
+{
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    A += (size_t)f * count;
+    double a = 0.0;
+    for (size_t e = threadIdx.x; e < count; e += blockDim.x) a += zabs2(A[e]);
+    a = warp_sum(a);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) red[wid] = a;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double fro2 = 0.0;
+    for (int w = 0; w < nw; ++w) fro2 += red[w];
+    const double *sf = s + (size_t)f * p;
+    double s2 = 0.0, s1 = 0.0;
+    for (int i = 0; i < p; ++i) {
+        s2 += sf[i] * sf[i];
+        s1 = fmax(s1, sf[i]);
+    }
+    double level;
+    if (method == IA_METHOD_TSVD) {
+        level = sf[tsvd_k - 1];
+    } else {
+        level = lam[(size_t)f * nrhs];
+        for (int r = 1; r < nrhs; ++r) level = fmin(level, lam[(size_t)f * nrhs + r]);
+    }
+    const bool ok = fro2 > 0.0 && fro2 < INFINITY && fabs(s2 - fro2) <= 1e-10 * fro2 && level >= ratio * s1;
+    if (!ok) atomicOr(&info[f], IA_INFO_PRECISION);
+}
+
+int mixed_guard_batched(ia_context *ctx, size_t count, int F, const double2 *A, int p, const double *s, int nrhs,
+                        const double *lambda, const ia_config *cfg, int *info)
+{
+    precision_guard_kernel<<<F, 256, 0, ctx->stream>>>(count, A, p, s, nrhs, lambda, cfg->method, cfg->tsvd_k,
+                                                       cfg->mixed_guard, info);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                              const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
                              int *info, WsCursor &cur)
