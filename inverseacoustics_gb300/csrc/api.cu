@@ -784,15 +784,8 @@ static int solve_core(ia_context *ctx, int m, int n, int F, const double2 *A, bo
                       WsCursor &cur)
 {
     NvtxRange r("ia.solve");
-    if (use_mixed_wide(m, n, cfg)) {
-        // lambda and s feed the precision guard, so they exist even when the
-        // caller does not ask for them
-        double *lam = lambda ? lambda : cur.take<double>((size_t)nrhs * F);
-        double *s = s_out ? s_out : cur.take<double>((size_t)m * F);
-        int st = wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lam, s, info, cur);
-        if (st) return st;
-        return mixed_guard_batched(ctx, (size_t)m * n, F, A, m, s, nrhs, lam, cfg, info);
-    }
+    if (use_mixed_wide(m, n, cfg))
+        return wide_solve_mixed_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     if (m <= n) return wide_solve_batched(ctx, m, n, F, A, transposed, nrhs, b, cfg, x, lambda, s_out, info, cur);
     const int p = m < n ? m : n;
     const int M = m >= n ? m : n;

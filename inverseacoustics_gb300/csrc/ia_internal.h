@@ -168,12 +168,6 @@ int dfgemm4_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, double
 int split_df_batched(ia_context *ctx, size_t count, const double2 *in, float4 *out);
 int df_hi_batched(ia_context *ctx, size_t count, const float4 *in, float2 *out);
 
-// precision guard of the mixed wide solve: sets IA_INFO_PRECISION in info[f]
-// for a bin whose lambda (TSVD: s_k) is below cfg->mixed_guard s_1, or whose
-// sum of s^2 misses ||A_f||_F^2 by more than 1e-10 relative
-int mixed_guard_batched(ia_context *ctx, size_t count, int F, const double2 *A, int p, const double *s, int nrhs,
-                        const double *lambda, const ia_config *cfg, int *info);
-
 // ---- tensor-core GEMM at FP64-level accuracy (tc_gemm.cu): operands cut
 // into S balanced base-64 BF16 slices (Ozaki scheme), pair products on the
 // tcgen05 pipe with exact FP32 level sums in TMEM
@@ -231,8 +225,10 @@ int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *
                        WsCursor &cur);
 // mixed solve: eigenvectors X and eigenvalues of H H^H from an FP32 QR +
 // one-sided Jacobi start, double-float Ogita-Aishima steps, Newton-Schulz and
-// an FP64 two-sided Jacobi on X^H (H H^H) X; then s, U^H b, GCV and the
-// back-projection
+// an FP64 two-sided Jacobi on X^H (H H^H) X; then s, U^H b, GCV, the
+// back-projection and the precision guard (IA_INFO_PRECISION in info[f] for
+// a bin whose lambda (TSVD: s_k) is below cfg->mixed_guard s_1, whose sum of
+// s^2 misses ||H_f||_F^2 by more than 1e-10 relative)
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                              const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,

@@ -833,12 +833,15 @@ __global__ void eig_backproject_kernel(int m, int n, int N, const double2 *H, in
     }
 }
 
+// CTAs per bin of the statistics pass (bin_stats_kernel)
+constexpr int BIN_STAT_BLOCKS = 16;
+
 static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
 {
     const size_t F = batch, N = m, M = n;
     return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
            7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + ws_round(4 * N * F) + ws_round(16 * M * N * F) +
-           ws_round(4 * F) + 4096;
+           ws_round(4 * F) + ws_round(8 * F) + 2 * ws_round(8 * (size_t)BIN_STAT_BLOCKS * F) + 4096;
 }
 
 // Range of the FP32 and double-float stages.  Their high words are FP32, so
@@ -849,34 +852,68 @@ static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
 // times 2^-e_f (bitwise, wherever the unscaled one stays in range).  The
 // eigenvalues come back multiplied by 4^e_f; everything after (s, beta, GCV,
 // x) works on the caller's A in FP64.
-__global__ void bin_exponent_kernel(size_t count, const double2 *__restrict__ A, int *__restrict__ ex)
+// Per-bin statistics of A in one pass over all SMs: BIN_STAT_BLOCKS CTAs per
+// bin, each over a contiguous chunk, write the chunk's largest |Re|, |Im| (as
+// an order-preserving key) and its sum of |a|^2; bin_stats_finish_kernel
+// combines the chunks in chunk order (deterministic) into the exponent e_f
+// with max(|Re|, |Im|) < 2^e_f and ||A_f||_F^2.
+
+__global__ void bin_stats_kernel(size_t count, const double2 *__restrict__ A, unsigned long long *__restrict__ keys,
+                                 double *__restrict__ sums)
 {
-    __shared__ unsigned long long s_key;
-    const int f = blockIdx.x;
+    __shared__ unsigned long long s_key[8];
+    __shared__ double s_sum[8];
+    const int f = blockIdx.y, c = blockIdx.x;
+    const size_t chunk = (count + BIN_STAT_BLOCKS - 1) / BIN_STAT_BLOCKS;
+    const size_t e0 = (size_t)c * chunk, e1 = e0 + chunk < count ? e0 + chunk : count;
     A += (size_t)f * count;
-    if (threadIdx.x == 0) s_key = 0ull;
-    __syncthreads();
     unsigned long long key = 0ull;
-    for (size_t e = threadIdx.x; e < count; e += blockDim.x) {
+    double sum = 0.0;
+    for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const double2 v = A[e];
         const unsigned long long a = __double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
         const unsigned long long b = __double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
         key = a > key ? a : key;
         key = b > key ? b : key;
+        sum += v.x * v.x + v.y * v.y;
     }
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
         key = k2 > key ? k2 : key;
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
     }
-    if ((threadIdx.x & 31) == 0) atomicMax(&s_key, key);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_key[wid] = key;
+        s_sum[wid] = sum;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned long long k = s_key;
-        // exponent of the largest magnitude (non-finite input keeps e = 0 and
-        // surfaces downstream as IA_INFO_NONFINITE)
-        const int e = (k && k < 0x7FF0000000000000ull) ? (int)(k >> 52) - 1022 : 0;
-        ex[f] = e;
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            key = s_key[w] > key ? s_key[w] : key;
+            sum += s_sum[w];
+        }
+        keys[(size_t)f * BIN_STAT_BLOCKS + c] = key;
+        sums[(size_t)f * BIN_STAT_BLOCKS + c] = sum;
     }
+}
+
+__global__ void bin_stats_finish_kernel(int F, const unsigned long long *__restrict__ keys,
+                                        const double *__restrict__ sums, int *__restrict__ ex, double *__restrict__ fro2)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    unsigned long long k = 0ull;
+    double sum = 0.0;
+    for (int c = 0; c < BIN_STAT_BLOCKS; ++c) {
+        const unsigned long long kc = keys[(size_t)f * BIN_STAT_BLOCKS + c];
+        k = kc > k ? kc : k;
+        sum += sums[(size_t)f * BIN_STAT_BLOCKS + c];
+    }
+    // exponent of the largest magnitude (non-finite input keeps e = 0 and
+    // surfaces downstream as IA_INFO_NONFINITE or in the guard's trace check)
+    ex[f] = (k && k < 0x7FF0000000000000ull) ? (int)(k >> 52) - 1022 : 0;
+    fro2[f] = sum;
 }
 
 __global__ void scale_bins_kernel(size_t count, const double2 *__restrict__ A, const int *__restrict__ ex,
@@ -913,7 +950,8 @@ size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch)
 // Newton-Schulz, FP64 S = X^H E X and the two-sided Jacobi on its coupled
 // pairs.  *Xout and *lam_out point into the workspace taken from cur.
 static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed,
-                          const ia_config *cfg, double2 **Xout, double **lam_out, int *info, WsCursor &cur)
+                          const ia_config *cfg, double2 **Xout, double **lam_out, double **fro2_out, int *info,
+                          WsCursor &cur)
 {
     const int N = m, Mr = n;
     const bool qr = n > m;
@@ -934,11 +972,17 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     int *perm = qr ? cur.take<int>((size_t)N * batch) : nullptr;
     double2 *As = cur.take<double2>((size_t)m * n * batch);
     int *ex = cur.take<int>((size_t)batch);
+    double *fro2 = cur.take<double>((size_t)batch);
+    unsigned long long *keys = cur.take<unsigned long long>((size_t)BIN_STAT_BLOCKS * batch);
+    double *sums = cur.take<double>((size_t)BIN_STAT_BLOCKS * batch);
     const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
     // the FP32 and double-float stages (1-3) work on A 2^-e_f
-    bin_exponent_kernel<<<batch, 256, 0, ctx->stream>>>((size_t)sA, A, ex);
+    bin_stats_kernel<<<dim3(BIN_STAT_BLOCKS, batch), 256, 0, ctx->stream>>>((size_t)sA, A, keys, sums);
     IA_LAUNCH_CHECK(ctx);
+    bin_stats_finish_kernel<<<(batch + 127) / 128, 128, 0, ctx->stream>>>(batch, keys, sums, ex, fro2);
+    IA_LAUNCH_CHECK(ctx);
+    *fro2_out = fro2;
     {
         int blocks = (int)((sA + 255) / 256);
         if (blocks > 256) blocks = 256;
@@ -1034,28 +1078,19 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     return IA_OK;
 }
 
-// One CTA per bin: ||A_f||_F^2 in FP64 against sum s_i^2, and the smallest
-// regularisation level against s_1.  The mixed eigensolver reaches FP64-level
-// eigenpairs of H H^H (errors ~eps s_1^2), so a Tikhonov solution is good to
-// ~eps (s_1 / lambda)^2 and needs lambda well above sqrt(eps) s_1; below
-// cfg->mixed_guard the bin is marked for the FP64 path.  A broken
-// eigen-decomposition (an eigenvalue lost or doubled) shows in the trace.
-__global__ void precision_guard_kernel(size_t count, const double2 *__restrict__ A, int p,
-                                       const double *__restrict__ s, int nrhs, const double *__restrict__ lam,
-                                       int method, int tsvd_k, double ratio, int *__restrict__ info)
+// Precision guard, one thread per bin: ||A_f||_F^2 (from the statistics pass)
+// against sum s_i^2, and the smallest regularisation level against s_1.  The
+// mixed eigensolver reaches FP64-level eigenpairs of H H^H (errors ~eps
+// s_1^2), so a Tikhonov solution is good to ~eps (s_1 / lambda)^2 and needs
+// lambda well above sqrt(eps) s_1; below cfg->mixed_guard the bin is marked
+// for the FP64 path.  A broken eigen-decomposition (an eigenvalue lost or
+// doubled) shows in the trace.
+__global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, int p, const double *__restrict__ s,
+                                       int nrhs, const double *__restrict__ lam, int method, int tsvd_k,
+                                       double ratio, int *__restrict__ info)
 {
-    __shared__ double red[32];
-    const int f = blockIdx.x;
-    A += (size_t)f * count;
-    double a = 0.0;
-    for (size_t e = threadIdx.x; e < count; e += blockDim.x) a += zabs2(A[e]);
-    a = warp_sum(a);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0) red[wid] = a;
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    double fro2 = 0.0;
-    for (int w = 0; w < nw; ++w) fro2 += red[w];
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
     const double *sf = s + (size_t)f * p;
     double s2 = 0.0, s1 = 0.0;
     for (int i = 0; i < p; ++i) {
@@ -1069,17 +1104,9 @@ __global__ void precision_guard_kernel(size_t count, const double2 *__restrict__
         level = lam[(size_t)f * nrhs];
         for (int r = 1; r < nrhs; ++r) level = fmin(level, lam[(size_t)f * nrhs + r]);
     }
-    const bool ok = fro2 > 0.0 && fro2 < INFINITY && fabs(s2 - fro2) <= 1e-10 * fro2 && level >= ratio * s1;
-    if (!ok) atomicOr(&info[f], IA_INFO_PRECISION);
-}
-
-int mixed_guard_batched(ia_context *ctx, size_t count, int F, const double2 *A, int p, const double *s, int nrhs,
-                        const double *lambda, const ia_config *cfg, int *info)
-{
-    precision_guard_kernel<<<F, 256, 0, ctx->stream>>>(count, A, p, s, nrhs, lambda, cfg->method, cfg->tsvd_k,
-                                                       cfg->mixed_guard, info);
-    IA_LAUNCH_CHECK(ctx);
-    return IA_OK;
+    const double a2 = fro2[f];
+    const bool ok = a2 > 0.0 && a2 < INFINITY && fabs(s2 - a2) <= 1e-10 * a2 && level >= ratio * s1;
+    if (!ok) info[f] |= IA_INFO_PRECISION;
 }
 
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
@@ -1089,7 +1116,8 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     const int N = m;
     double2 *X;
     double *lam_e;
-    int st = gram_eig_mixed(ctx, m, n, batch, A, transposed, cfg, &X, &lam_e, info, cur);
+    double *fro2;
+    int st = gram_eig_mixed(ctx, m, n, batch, A, transposed, cfg, &X, &lam_e, &fro2, info, cur);
     if (st) return st;
     double *s = s_out ? s_out : cur.take<double>((size_t)N * batch);
     int *rank = cur.take<int>((size_t)N * batch);
@@ -1104,6 +1132,10 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     size_t smem = sizeof(double2) * ((size_t)N + (size_t)m);
     eig_backproject_kernel<<<dim3(batch, nrhs), 256, smem, ctx->stream>>>(m, n, N, A, transposed ? 1 : 0, X,
                                                                          transposed ? 1 : 0, rank, s, z, nrhs, x);
+    IA_LAUNCH_CHECK(ctx);
+    // 6. precision guard (IA_INFO_PRECISION for the FP64 fallback)
+    precision_guard_kernel<<<(batch + 127) / 128, 128, 0, ctx->stream>>>(batch, fro2, N, s, nrhs, lam, cfg->method,
+                                                                         cfg->tsvd_k, cfg->mixed_guard, info);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }

@@ -80,7 +80,11 @@ def test_ibem_headline_mixed_every_bin_matches_oracle(cuda, ctx, ibem_case):
 # at FP64 rounding level.  Parity therefore has three tiers:
 #  * every bin: no info flag; s within 1e-13 s_1 of LAPACK's; (x, lambda)
 #    solves the Tikhonov normal equations (H^H H + lambda^2 I) x = H^H b to
-#    FP64 backward error;
+#    within max(1e-12, 100 eps kappa) relative to s_1^2 |x| + s_1 |b|.  The
+#    kappa = s_1 / lambda factor is the data-space form's: x = H^H w with
+#    w = U (S^2 + lambda^2)^-1 U^H b leaves the residual H^H E w, E ~ eps s_1^2
+#    the eigen-decomposition's backward error, |w| ~ |b| / lambda^2 (LAPACK's
+#    V-space form has O(eps) here; both have forward errors O(eps kappa));
 #  * every bin whose GCV choice the arithmetic determines -- LAPACK's gesdd
 #    and gesvd drivers agree on lambda to 1e-8, and the GCV minimum beats the
 #    best grid value in the rounding region (lambda < 1e3 16 eps s_1) by 1.5x
@@ -120,9 +124,14 @@ def hels_case():
     return w, pts, p, ref
 
 
-def _hels_matrices(w, pts):
+def _hels_backward(args):
+    """Relative residual of the Tikhonov normal equations for (x, lambda)."""
     from oracle import ia_oracle as O
-    return [O.hels(pts, pts, k, w.params["order"], 343.0, 1.21)[1] for k in w.k]
+    pts, k, order, b, x, lam = args
+    _, H, _ = O.hels(pts, pts, k, order, 343.0, 1.21)
+    s1 = np.linalg.norm(H, 2)
+    r = H.conj().T @ (H @ x - b) + lam * lam * x
+    return np.linalg.norm(r) / (s1 * s1 * np.linalg.norm(x) + s1 * np.linalg.norm(b))
 
 
 def _hels_check(w, pts, p, ref, x, lam, s, info, label, mixed_bins=None):
@@ -134,13 +143,10 @@ def _hels_check(w, pts, p, ref, x, lam, s, info, label, mixed_bins=None):
     assert len(flagged) == 0, f"{label}: info flags at bins {flagged[:16]}"
     s_or = np.array([r[2] for r in ref])
     ds = (np.abs(s - s_or).max(axis=1) / s_or[:, 0])
-    Hs = _hels_matrices(w, pts)
-    back = np.empty(F)
-    for f in range(F):
-        H, b, xf, lf = Hs[f], p[f, 0], x[f, 0], lam[f, 0]
-        s1 = s_or[f, 0]
-        r = H.conj().T @ (H @ xf - b) + lf * lf * xf
-        back[f] = np.linalg.norm(r) / (s1 * s1 * np.linalg.norm(xf) + s1 * np.linalg.norm(b))
+    order = w.params["order"]
+    back = np.array(CP.map_bins(_hels_backward, [(pts, w.k[f], order, p[f, 0], x[f, 0], lam[f, 0])
+                                                 for f in range(F)]))
+    back_bound = np.maximum(1e-12, 100 * EPS * s_or[:, 0] / lam[:, 0])
     det = np.array([r[3] for r in ref]) & fp64_bins
     lam_or = np.array([r[1] for r in ref])
     kappa = s_or[:, 0] / lam_or
@@ -150,12 +156,13 @@ def _hels_check(w, pts, p, ref, x, lam, s, info, label, mixed_bins=None):
     r = np.linalg.norm(w.arrays["mics"], axis=0).min()
     print(f"\nHELS N={w.params['order']} {label}, {F} bins (kr {w.k[0] * r:.3f}..{w.k[-1] * r:.2f}): "
           f"{fp64_bins.sum()} FP64 bins: s max {ds[fp64_bins].max():.2e} s_1, normal-equation residual max "
-          f"{back[fp64_bins].max():.2e}; "
+          f"{back[fp64_bins].max():.2e} ({(back / back_bound)[fp64_bins].max():.3f} of its bound; "
+          f"{int((back[fp64_bins] < 1e-12).sum())} bins below 1e-12); "
           f"{det.sum()} determined bins: x max {ex[det].max():.2e}, lambda max {el[det].max():.2e}, "
           f"max err / bound {max((ex / bound)[det].max(), (el / bound)[det].max()):.3f}; "
           f"bins with x, lambda within 1e-10: {int(((ex < 1e-10) & (el < 1e-10)).sum())}")
     assert ds[fp64_bins].max() < 1e-13
-    assert back[fp64_bins].max() < 1e-12
+    assert (back[fp64_bins] < back_bound[fp64_bins]).all()
     assert (ex[det] < bound[det]).all()
     assert (el[det] < bound[det]).all()
     return ex, el, ds
@@ -179,9 +186,12 @@ def test_hels_full_size_fp64_matches_oracle(cuda, ctx, hels_case):
 
 
 def test_hels_full_size_mixed_matches_oracle(cuda, ctx, hels_case):
-    """Mixed path: bins with lambda >= 1e-3 s_1 stay on the mixed path and must
-    be within 1e-6 of the oracle; the others fail its precision guard and are
-    solved again in FP64, identically to the FP64 run."""
+    """Mixed path: bins that pass its precision guard stay on it and must be
+    within 1e-6 of the oracle; the others are solved again by the FP64 path,
+    identically to the FP64 run.  On this workload no bin passes: lambda is
+    below 1e-3 s_1 in all but the 32 lowest bins, and there (lambda = s_1,
+    17 decades of singular values) the Gram eigensolver loses the spectrum
+    (the trace check)."""
     w, pts, p, ref = hels_case
     x, lam, s, info, fb = _hels_run(ctx, cuda, w, pts, p, 1)
     x64, lam64, s64, _, _ = _hels_run(ctx, cuda, w, pts, p, 0)
