@@ -346,6 +346,81 @@ def _bench_selectors(ctx, dev, stream, flush, mesh, w, p_np, reps=3):
             "note": "dsvd_* runs the FP64 solve under IA_PREC_MIXED", "methods": res}
 
 
+def _bench_hels(ctx, dev, stream, flush, reps=2):
+    """HELS (CUDA/hels.cuh:222): order 15 (256 terms), 256 microphones on a
+    16 x 16 plane at z = 0.15 m, 40 seeded monopoles, 512 bins 50-3000 Hz,
+    25 dB: expansion matrices and Tikhonov-GCV for all 512 bins per step.
+    The operators span 17 decades of singular values and GCV's lambda falls to
+    1e-14 s_1, so every bin fails the mixed path's precision guard and the
+    mixed call hands it to the FP64 path; both precisions are timed."""
+    import numpy as np
+    import torch
+
+    from inverseacoustics_gb300 import _lib, api
+    from inverseacoustics_gb300 import geometry as g
+    w = g.hels_plane(n_freq=512)
+    p = g.hels_plane_pressures(w)
+    pts = torch.as_tensor(np.ascontiguousarray(g.cartesian_to_spherical(w.arrays["mics"])), device=dev)
+    k = torch.as_tensor(w.k, device=dev)
+    pd = torch.as_tensor(p, device=dev)
+    order, F = w.params["order"], len(w.k)
+    res = {}
+    outs = {}
+    for name, prec in (("mixed", 1), ("fp64", 0)):
+        cfg = api.default_config(precision=prec)
+        api.hels_solve_batch(ctx, pts, order, k, pd, cfg)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            x, lam, s_, info = api.hels_solve_batch(ctx, pts, order, k, pd, cfg)
+            e.record(stream)
+            e.synchronize()
+            times.append(a.elapsed_time(e))
+        ms = sum(times) / reps
+        outs[name] = (x, lam)
+        res[name] = {"value": F / (ms / 1000.0), "ms_per_step": ms,
+                     "fallback_bins": int(_lib.lib().ia_last_fallback_bins(ctx.handle)),
+                     "info_clean": int(info.abs().sum()) == 0}
+    (x1, l1), (x0, l0) = outs["mixed"], outs["fp64"]
+    res["mixed_equals_fp64"] = bool(torch.equal(x1, x0) and torch.equal(l1, l0))
+    res["mixed_speedup"] = res["mixed"]["value"] / res["fp64"]["value"]
+    return {"workload": f"hels_N{order}_256mic_F{F}", "unit": "freq-solves/s (assembly + solve)",
+            "parity": "tests/test_gpu_fullsize.py: s 3e-14 s_1; x, lambda within 100 eps s_1/lambda of the oracle "
+                      "on the bins whose GCV choice FP64 arithmetic determines", **res}
+
+
+def _tc_product(ctx, dev, stream, flush, reps=5):
+    """The mixed transfer's FP64-level product on the tensor cores, alone:
+    ia_zgemm_batch (BF16 slicing of both operands + the tcgen05 GEMM) at the
+    workload's shape, 642 x 120 x 642 complex, 64 bins, 7 slices; CUDA
+    events on the launching stream."""
+    import torch
+
+    from inverseacoustics_gb300 import api
+    F, M, N, K = N_FREQ, 642, 120, 642
+    g = torch.Generator(device=dev).manual_seed(7)
+    A = torch.randn((F, K, M), dtype=torch.complex128, device=dev, generator=g)
+    B = torch.randn((F, N, K), dtype=torch.complex128, device=dev, generator=g)
+    C = torch.zeros((F, N, M), dtype=torch.complex128, device=dev)
+    api.zgemm_batch(ctx, "N", "N", M, N, K, A, B, C, precision=1, slices=7)
+    torch.cuda.synchronize()
+    acc = 0.0
+    for _ in range(reps):
+        flush.zero_()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        api.zgemm_batch(ctx, "N", "N", M, N, K, A, B, C, precision=1, slices=7)
+        e.record(stream)
+        e.synchronize()
+        acc += a.elapsed_time(e)
+    ms = acc / reps
+    S, Kp = 7, (2 * K + 7) & ~7
+    return ms, 8.0 * M * N * K * F, S * (S + 1) / 2 * 2.0 * M * (2 * N) * Kp * F
+
+
 def _bench_admm(ctx, dev, stream, flush, w, fp64_peak, reps=2):
     """ADMM L1 inversion (MATLAB/ADMMG.m) of the sphere's monopole transfer
     matrices: 120 microphones, 642 equivalent sources, 64 frequencies, Nm = 50
@@ -415,7 +490,7 @@ def run_ours(args):
     import numpy as np
     import torch
 
-    from inverseacoustics_gb300 import api
+    from inverseacoustics_gb300 import _lib, api
 
     rank, world, local = _dist()
     torch.cuda.set_device(local)
@@ -496,6 +571,8 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         total_ms = timed(graph.launch, args.steps)
     launches = graph.kernel_count() * args.steps
+    api.ibem_solve_batch(ctx, mesh, mics_d, k_d, p_d, cfg)
+    fallback_bins = _lib.lib().ia_last_fallback_bins(ctx.handle)
     x, lam, s, info = out
     value = world * N_FREQ * args.steps / (total_ms / 1000.0)
     err_x = float(((x - x64).abs().pow(2).sum(dim=(1, 2)).sqrt() / x64.abs().pow(2).sum(dim=(1, 2)).sqrt()).max())
@@ -552,42 +629,62 @@ def run_ours(args):
         del a64
     except Exception:
         pass
-    # DRAM bytes (read + write) of the mixed-path assembly kernel per 64
-    # frequencies, from the ncu launch list in
-    # profiles/ibem_pipeline_mixed_launches_F64.txt (1535.7 MB over 2 passes)
-    asm_traffic = 767.9e6
-    # FP32-pipe view of the same kernel: warp instructions of the captured
-    # 8-frequency launch (762 rows x 8 = 6096 CTAs; a 16-bin call runs as two
-    # staggered parts) from the ncu capture in
-    # profiles/ibem_rows_kernel_dfl_F16.txt (smsp__inst_executed.sum 1.2536e9;
-    # the work per (row, frequency) CTA is fixed, so a 64-frequency launch
-    # issues 8x that), against the SMs' issue rate of one warp instruction per
-    # SM sub-partition per clock at the sampled SM clock
+    # The dominant kernel of the pass (16 % of the serialised launch list,
+    # profiles/ibem_pipeline_mixed_launches_F64.txt) is the mixed-path
+    # assembly, ibem_rows_kernel<dfl>.  Its bound is FP32 instruction issue,
+    # not HBM: warp instructions per 64-frequency launch scaled from the ncu
+    # capture of the same kernel in profiles/ibem_rows_kernel_dfl_F16.txt
+    # (smsp__inst_executed.sum 1.2536e9 for an 8-frequency launch; the work
+    # per (row, frequency) CTA is fixed, so 64 frequencies issue 8x that),
+    # against one warp instruction per SM sub-partition per clock at the
+    # sampled SM clock; its DRAM bytes (read + write, 767.9 MB per 64
+    # frequencies) come from the launch list's capture.
     asm_warp_instr = 8 * 1.25363e9
+    asm_traffic = 767.9e6
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = props.multi_processor_count * 4 * sm_mhz * 1e6
     issue_achieved = asm_warp_instr / (t_asm / 1000.0)
-    roofline = {"kernel": "ibem_rows_kernel<dfl> (mixed-path assembly)", "bound": "hbm",
-                "achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "traffic": asm_traffic,
-                "peak_kind": peak_kind,
-                "note": "instruction-issue bound on the FP32 pipe, not HBM bound (ncu: issue 75%, FMA pipe 66%, "
-                        "FP64 pipe 26%, 734 FP32 lane instructions per quadrature-point evaluation); DRAM "
-                        "traffic is below the algorithmic output (rows partly stay in L2)",
-                "issue": {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
-                          "frac": issue_achieved / issue_peak, "instructions_per_launch": asm_warp_instr,
-                          "sm_mhz": sm_mhz},
-                "compute": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
-                            "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
-                            "peak_dgemm_measured": fp64_tflops_dgemm}}
+    # the tensor-core product (slicing + tcgen05 GEMM) alone, CUDA events
+    tc_ms, tc_flops, tc_bf16 = _tc_product(ctx, dev, stream, flush)
+    # FP64 path's dense work: LU + solves + transfer GEMM, and the SVD of
+    # the 120 x 642 transfer matrices (4 (6 M N^2 + 20 N^3), M = 642, N = 120)
+    svd_flops = N_FREQ * 4.0 * (6.0 * m * l * l + 20.0 * l ** 3)
+    roofline = {"kernel": "ibem_rows_kernel<dfl> (mixed-path assembly; the largest share of the pass)",
+                "bound": "issue", "achieved": issue_achieved / 1e9, "peak": issue_peak / 1e9,
+                "unit": "G warp-instructions/s", "frac": issue_achieved / issue_peak, "traffic": asm_traffic,
+                "sm_mhz": sm_mhz,
+                "instructions_per_launch": asm_warp_instr,
+                "instructions_source": "scaled from the ncu capture in profiles/ibem_rows_kernel_dfl_F16.txt",
+                "hbm": {"achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "peak_kind": peak_kind,
+                        "algorithmic_bytes": asm_bytes},
+                "note": "FP32-issue bound (ncu: issue 75 %, FMA pipe 66 %, 734 FP32 lane instructions per "
+                        "quadrature-point evaluation); HBM is not its bound"}
+    roofline_tensor = {"kernel": "tc_slice_kernel x2 + tc_gemm_kernel<7> (the transfer's FP64-level products, "
+                                 "642 x 120 x 642 complex, 64 bins)",
+                       "bound": "tensor", "achieved": tc_flops / (tc_ms / 1000.0) / 1e12, "peak": bf16_peak,
+                       "unit": "TFLOP/s", "frac": tc_flops / (tc_ms / 1000.0) / 1e12 / bf16_peak,
+                       "peak_kind": peak_kind, "ms": tc_ms,
+                       "algorithmic_flops": tc_flops, "flops_convention": "complex GEMM 8 M N K (FP64-equivalent)",
+                       "executed_bf16": {"flops": tc_bf16, "achieved": tc_bf16 / (tc_ms / 1000.0) / 1e12,
+                                         "frac": tc_bf16 / (tc_ms / 1000.0) / 1e12 / bf16_peak,
+                                         "note": "28 slice-pair products of 642 x 240 x 1288 real per bin"},
+                       "ncu": "profiles/tc_gemm_kernel_7_ibem_F16.txt"}
+    compute = {"fp64_transfer": {"stage": "FP64 path: LU + solves + transfer GEMM", "unit": "FP64 TFLOP/s",
+                                 "achieved": lu_flops / ((t_transfer64 - t_asm) / 1000.0) / 1e12,
+                                 "peak_dgemm_measured": fp64_tflops_dgemm},
+               "fp64_solve": {"stage": "FP64 path: pivoted QR + one-sided Jacobi SVD + GCV + Tikhonov",
+                              "unit": "FP64 TFLOP/s", "achieved": svd_flops / (t_solve64 / 1000.0) / 1e12,
+                              "peak_dgemm_measured": fp64_tflops_dgemm}}
     other = {}
     if world == 1:
         side = (("radiation_modes", lambda: _bench_radiation(ctx, dev, stream, flush)),
                 ("esm_design_adjoint", lambda: _bench_design(ctx, dev, stream, flush)),
                 ("bem_modes", lambda: _bench_bem_modes(ctx, dev, stream, flush, mesh, w)),
                 ("lambda_selectors", lambda: _bench_selectors(ctx, dev, stream, flush, mesh, w, p_np)),
-                ("admm_l1", lambda: _bench_admm(ctx, dev, stream, flush, w, fp64_tflops_dgemm)))
+                ("admm_l1", lambda: _bench_admm(ctx, dev, stream, flush, w, fp64_tflops_dgemm)),
+                ("hels", lambda: _bench_hels(ctx, dev, stream, flush)))
         for name, fn in side:
             try:
                 other[name] = fn()
@@ -605,8 +702,8 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "mixed: f64 assembly, f32 LU/QR/Jacobi, double-float (f32 pair) refinement GEMMs, "
-                         "f64 GCV and Tikhonov refinement",
+                "dtype": "mixed: double-float assembly, f32 LU/QR/Jacobi, bf16-sliced tensor-core (Ozaki) "
+                         "FP64-level transfer products, double-float eigen-refinement, f64 GCV and Tikhonov",
                 "precision_path": "mixed", "data": "synthetic (seeded)",
                 "config": _config(world),
                 "execution": "one CUDA graph replay per step (graph of the whole batched solve), L2 flushed "
@@ -615,10 +712,13 @@ def run_ours(args):
                               "mixed_speedup": value / fp64_value},
                 "direct_calls": {"value": direct_value, "unit": UNIT, "note": "same solve without the graph"},
                 "accuracy": {"max_rel_err_x_vs_fp64": err_x, "max_rel_err_lambda_vs_fp64": err_lam,
-                             "bound": 1e-6, "note": "FP64 path parity-tested against the oracle at 1e-10"},
+                             "bound": 1e-6, "fallback_bins": int(fallback_bins),
+                             "note": "both paths parity-tested against the oracle on this workload, all 64 bins "
+                                     "(tests/test_gpu_fullsize.py): FP64 at 1e-10, mixed at 1e-6"},
                 "stages_ms": {"assembly": t_asm, "transfer_incl_assembly": t_transfer, "svd_gcv_tikhonov": t_solve,
                               "fp64_transfer_incl_assembly": t_transfer64, "fp64_svd_gcv_tikhonov": t_solve64},
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "roofline": roofline, "roofline_tensor": roofline_tensor, "compute": compute, "cpu_baseline": cpu,
+                "clocks": clk.summary(),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(p_np.nbytes),
                         "d2h_bytes_per_step": int(x_h.numel() * 16 + lam_h.numel() * 8)},
                 "gpu_launches": int(launches), "other_workloads": other}

@@ -833,6 +833,48 @@ __global__ void eig_backproject_kernel(int m, int n, int N, const double2 *H, in
     }
 }
 
+// FP64-level products of the mixed eigensolver (E = H H^H and the
+// Ogita-Aishima / Newton-Schulz products): the tensor-core GEMM on 8 BF16
+// slices when cfg->gemm_slices turns the tensor cores on and the product's K
+// keeps the slice sums exact (K <= 1024 at 8 slices), else the double-float
+// CUDA-core GEMM.  E's error reaches x as |dE| / lambda^2, so these products
+// take 8 slices (bound 1.4e-13 of the row and column maxima per term) whatever
+// the transfer uses.  The slice planes of both operands live in one scratch
+// region that each product reuses (products run in stream order).
+constexpr int EIG_SLICES = 8;
+
+static bool eig_tc(const ia_config *cfg, int K)
+{
+    return cfg->gemm_slices >= TC_SLICES_MIN && cfg->gemm_slices <= TC_SLICES_MAX &&
+           (long long)EIG_SLICES * 1024 * ((2 * K + 7) & ~7) <= (1ll << 24);
+}
+
+static size_t eig_gemm_ws_bytes(int N, int K, int batch)
+{
+    return tc_planes_bytes(N, K, EIG_SLICES, false, batch) + tc_planes_bytes(N, K, EIG_SLICES, true, batch) + 1024;
+}
+
+struct EigGemm {
+    ia_context *ctx;
+    const ia_config *cfg;
+    char *ws;
+    size_t bytes;
+    int *info;
+    int operator()(Op opa, Op opb, int M, int N, int K, double alpha, const double2 *A, int lda, long long sA,
+                   const double2 *B, int ldb, long long sB, double beta, double2 *C, int ldc, long long sC,
+                   int batch) const
+    {
+        if (!eig_tc(cfg, K))
+            return dfgemm_batched(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
+        WsCursor cur{ws, 0, bytes};
+        TcPlanes Pa{}, Pb{};
+        int st = tc_slice(ctx, false, opa, A, lda, sA, M, K, EIG_SLICES, batch, Pa, cur);
+        if (!st) st = tc_slice(ctx, true, opb, B, ldb, sB, N, K, EIG_SLICES, batch, Pb, cur);
+        if (!st) st = tc_gemm(ctx, Pa, Pb, M, N, alpha, beta, C, ldc, sC, batch, info);
+        return st;
+    }
+};
+
 // CTAs per bin of the statistics pass (bin_stats_kernel)
 constexpr int BIN_STAT_BLOCKS = 16;
 
@@ -841,7 +883,8 @@ static size_t gram_eig_mixed_ws_bytes(int m, int n, int batch)
     const size_t F = batch, N = m, M = n;
     return ws_round(16 * M * N * F) + ws_round(8 * M * N * F) + ws_round(8 * N * F) + 2 * ws_round(8 * N * N * F) +
            7 * ws_round(16 * N * N * F) + ws_round(8 * N * F) + ws_round(4 * N * F) + ws_round(16 * M * N * F) +
-           ws_round(4 * F) + ws_round(8 * F) + 2 * ws_round(8 * (size_t)BIN_STAT_BLOCKS * F) + 4096;
+           ws_round(4 * F) + ws_round(8 * F) + 2 * ws_round(8 * (size_t)BIN_STAT_BLOCKS * F) +
+           eig_gemm_ws_bytes(m, n > m ? n : m, batch) + 4096;
 }
 
 // Range of the FP32 and double-float stages.  Their high words are FP32, so
@@ -975,6 +1018,9 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     double *fro2 = cur.take<double>((size_t)batch);
     unsigned long long *keys = cur.take<unsigned long long>((size_t)BIN_STAT_BLOCKS * batch);
     double *sums = cur.take<double>((size_t)BIN_STAT_BLOCKS * batch);
+    const size_t eg_bytes = eig_gemm_ws_bytes(N, n > m ? n : m, batch);
+    const EigGemm eg{ctx, cfg, cur.take<char>(eg_bytes), eg_bytes, info};
+    if (cur.off > cur.cap) return IA_ERR_ALLOC;
     const long long sA = (long long)m * n, sY = (long long)Mr * N, sN = (long long)NN;
     int st;
     // the FP32 and double-float stages (1-3) work on A 2^-e_f
@@ -1020,8 +1066,8 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     // H reaches this path from the double-float transfer (~1e-13 relative), so
     // an FP64 product would not make E more accurate.
     const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
-    if (transposed) st = dfgemm_batched(ctx, OP_C, OP_N, N, N, n, 1.0, A, n, sA, A, n, sA, 0.0, E, N, sN, batch);
-    else st = dfgemm_batched(ctx, OP_N, OP_C, N, N, n, 1.0, A, m, sA, A, m, sA, 0.0, E, N, sN, batch);
+    if (transposed) st = eg(OP_C, OP_N, N, N, n, 1.0, A, n, sA, A, n, sA, 0.0, E, N, sN, batch);
+    else st = eg(OP_N, OP_C, N, N, n, 1.0, A, m, sA, A, m, sA, 0.0, E, N, sN, batch);
     if (st) return st;
     // 3. eigen-refinement from X = J (conj(J) for H^T input)
     if ((st = copy2d_batched<float2, double2>(ctx, N, N, J32, N, sN, X, N, sN, transposed, batch))) return st;
@@ -1035,13 +1081,13 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     // (measured 14.3 -> 14.9 ms per 64-bin solve).
     const int steps = cfg->refine_steps > 2 ? cfg->refine_steps : 2;
     for (int it = 0; it < steps; ++it) {
-        if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
-        if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, T1, N, sN, 0.0, Sm, N, sN, batch))) return st;
-        if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
+        if ((st = eg(OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
+        if ((st = eg(OP_C, OP_N, N, N, N, 1.0, X, N, sN, T1, N, sN, 0.0, Sm, N, sN, batch))) return st;
+        if ((st = eg(OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
         oa_update_kernel<<<batch, OA_THREADS, sizeof(double) * (size_t)N, ctx->stream>>>(N, Sm, Rm, Fc, lam_e);
         IA_LAUNCH_CHECK(ctx);
         if ((st = zcopy2d_batched(ctx, N, N, X, N, sN, Xn, N, sN, false, batch))) return st;
-        if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, 1.0, X, N, sN, Fc, N, sN, 1.0, Xn, N, sN, batch))) return st;
+        if ((st = eg(OP_N, OP_N, N, N, N, 1.0, X, N, sN, Fc, N, sN, 1.0, Xn, N, sN, batch))) return st;
         double2 *t = X;
         X = Xn;
         Xn = t;
@@ -1053,9 +1099,9 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     // Suited to spectra with few clusters (a transfer matrix's decaying
     // singular values): on a dense clustered spectrum (the radiation operator
     // of a sphere) the first-order steps stall and the Jacobi does a full sweep.
-    if ((st = dfgemm_batched(ctx, OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
+    if ((st = eg(OP_C, OP_N, N, N, N, 1.0, X, N, sN, X, N, sN, 0.0, Rm, N, sN, batch))) return st;
     if ((st = zcopy2d_batched(ctx, N, N, X, N, sN, Xn, N, sN, false, batch))) return st;
-    if ((st = dfgemm_batched(ctx, OP_N, OP_N, N, N, N, -0.5, X, N, sN, Rm, N, sN, 1.5, Xn, N, sN, batch))) return st;
+    if ((st = eg(OP_N, OP_N, N, N, N, -0.5, X, N, sN, Rm, N, sN, 1.5, Xn, N, sN, batch))) return st;
     {
         double2 *t = X;
         X = Xn;
