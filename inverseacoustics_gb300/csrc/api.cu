@@ -168,18 +168,32 @@ static bool all_finite(const double *p, size_t n)
 int ensure_side_stream(ia_context *ctx)
 {
     if (ctx->side[0]) return IA_OK;
-    constexpr int NS = IA_SPLIT_PARTS - 1, NE = IA_SPLIT_PARTS;
+    constexpr int NS = IA_SPLIT_PARTS, NE = IA_SPLIT_PARTS;
     cudaStream_t s[NS] = {};
-    cudaEvent_t er[NE] = {}, ed[NE] = {};
-    cudaError_t e = cudaSuccess;
-    for (int i = 0; i < NS && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking);
+    cudaEvent_t er[NE] = {}, ed[NE] = {}, ef = nullptr;
+    // Part q's stream gets the q-th highest priority: the block scheduler then
+    // hands a freed SM to part q's latency-bound chain (LU panels, solves,
+    // Jacobi: one CTA per bin) before part q+1's assembly, whose thousands of
+    // CTAs would otherwise be dispatched first because they were launched
+    // first.  IA_STREAM_PRIORITY=0 creates them all at the default priority.
+    int least = 0, greatest = 0;
+    const char *env = getenv("IA_STREAM_PRIORITY");
+    const bool prio = !(env && env[0] == '0');
+    cudaError_t e = prio ? cudaDeviceGetStreamPriorityRange(&least, &greatest) : cudaSuccess;
+    for (int i = 0; i < NS && e == cudaSuccess; ++i) {
+        int pr = greatest + i;
+        if (pr > least) pr = least;
+        e = cudaStreamCreateWithPriority(&s[i], cudaStreamNonBlocking, prio ? pr : 0);
+    }
     for (int i = 0; i < NE && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&er[i], cudaEventDisableTiming);
     for (int i = 0; i < NE && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ed[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ef, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         for (int i = 0; i < NE; ++i) {
             if (er[i]) cudaEventDestroy(er[i]);
             if (ed[i]) cudaEventDestroy(ed[i]);
         }
+        if (ef) cudaEventDestroy(ef);
         for (int i = 0; i < NS; ++i)
             if (s[i]) cudaStreamDestroy(s[i]);
         return cuda_status(e);
@@ -189,6 +203,7 @@ int ensure_side_stream(ia_context *ctx)
         ctx->ev_rows[i] = er[i];
         ctx->ev_done[i] = ed[i];
     }
+    ctx->ev_fork = ef;
     return IA_OK;
 }
 
@@ -280,7 +295,7 @@ int ia_create(ia_context **out, int device, void *stream)
 int ia_destroy(ia_context *ctx)
 {
     if (!ctx) return IA_OK;
-    for (int i = 0; i < IA_SPLIT_PARTS - 1; ++i)
+    for (int i = 0; i < IA_SPLIT_PARTS; ++i)
         if (ctx->side[i]) cudaStreamSynchronize(ctx->side[i]);
     if (ctx->ws) {
         cudaFreeAsync(ctx->ws, ctx->stream);
@@ -291,7 +306,8 @@ int ia_destroy(ia_context *ctx)
             cudaEventDestroy(ctx->ev_rows[i]);
             cudaEventDestroy(ctx->ev_done[i]);
         }
-        for (int i = 0; i < IA_SPLIT_PARTS - 1; ++i) cudaStreamDestroy(ctx->side[i]);
+        cudaEventDestroy(ctx->ev_fork);
+        for (int i = 0; i < IA_SPLIT_PARTS; ++i) cudaStreamDestroy(ctx->side[i]);
     }
     free(ctx);
     return IA_OK;
@@ -1002,12 +1018,14 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     }
     if ((st = ensure_side_stream(ctx))) return st;
     cudaStream_t main = ctx->stream;
-    cudaError_t e = cudaSuccess;
+    // fork: every part runs on its own prioritised stream, after the work
+    // already queued on the caller's stream
+    cudaError_t e = cudaEventRecord(ctx->ev_fork, main);
     int q = 0;
-    for (; q < parts && !st; ++q) {
+    for (; q < parts && !st && e == cudaSuccess; ++q) {
         const int f0 = q * Fp;
-        cudaStream_t sq = q == 0 ? main : ctx->side[q - 1];
-        if (q > 0 && (e = cudaStreamWaitEvent(sq, ctx->ev_rows[q - 1], 0)) != cudaSuccess) break;
+        cudaStream_t sq = ctx->side[q];
+        if ((e = cudaStreamWaitEvent(sq, q == 0 ? ctx->ev_fork : ctx->ev_rows[q - 1], 0)) != cudaSuccess) break;
         ctx->stream = sq;
         WsCursor cur{(char *)ctx->ws + need * q, 0, need};
         st = ibem_solve_part(ctx, mesh, l, d_mics, Fp, d_k + f0, nrhs, (const double2 *)d_p + (size_t)f0 * nrhs * l,
@@ -1017,9 +1035,9 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         ctx->stream = main;
         if (!st && cur.off > need) st = IA_ERR_ALLOC;   // workspace accounting broken: the parts would overlap
     }
-    // join every started side stream back into the caller's stream
-    for (int j = 1; j < q; ++j) {
-        cudaError_t ej = cudaEventRecord(ctx->ev_done[j], ctx->side[j - 1]);
+    // join every started part's stream back into the caller's stream
+    for (int j = 0; j < q; ++j) {
+        cudaError_t ej = cudaEventRecord(ctx->ev_done[j], ctx->side[j]);
         if (ej == cudaSuccess) ej = cudaStreamWaitEvent(main, ctx->ev_done[j], 0);
         if (e == cudaSuccess) e = ej;
     }

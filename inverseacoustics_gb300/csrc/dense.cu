@@ -220,13 +220,14 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_kernel(int n, T *A, in
                 A[i + (size_t)j * lda] = zmul(A[i + (size_t)j * lda], inv);
         }
         __syncthreads();
-        const int rows = n - j - 1, ncols = kend - j - 1;
-        for (int idx = tid; idx < rows * ncols; idx += PANEL_THREADS) {
-            int r = j + 1 + idx % rows;
-            int c = j + 1 + idx / rows;
-            T v = A[r + (size_t)c * lda];
-            zfms(v, A[r + (size_t)j * lda], A[j + (size_t)c * lda]);
-            A[r + (size_t)c * lda] = v;
+        // rank-1 update, thread per row (coalesced down each column)
+        for (int r = j + 1 + tid; r < n; r += PANEL_THREADS) {
+            const T l = A[r + (size_t)j * lda];
+            for (int c = j + 1; c < kend; ++c) {
+                T v = A[r + (size_t)c * lda];
+                zfms(v, l, A[j + (size_t)c * lda]);
+                A[r + (size_t)c * lda] = v;
+            }
         }
         __syncthreads();
     }
@@ -309,22 +310,32 @@ __global__ void __launch_bounds__(PANEL_THREADS) lu_panel_smem_kernel(int n, T *
             for (int i = j + 1 + tid; i < n; i += PANEL_THREADS) cj[i - k0] = zmul(cj[i - k0], inv);
         }
         __syncthreads();
-        const int rows = n - j - 1, ncols = kend - j - 1;
+        // rank-1 update, thread per row: the row's multiplier once, then the
+        // remaining columns in order (each element sees the same operations
+        // in the same order as any other work split)
+        const int ncols = kend - j - 1;
         R best = -1;
         int bi = n;
-        for (int idx = tid; idx < rows * ncols; idx += PANEL_THREADS) {
-            int r = j + 1 + idx % rows;
-            int c = j + 1 + idx / rows;
-            T *pc = P + (size_t)(c - k0) * pr;
-            T v = pc[r - k0];
-            zfms(v, cj[r - k0], pc[j - k0]);
-            pc[r - k0] = v;
-            if (c == j + 1) {
-                R av = fabs(v.x) + fabs(v.y);
-                if (av > best) { best = av; bi = r; }
+        if (ncols > 0) {
+            for (int r = j + 1 + tid; r < n; r += PANEL_THREADS) {
+                const T l = cj[r - k0];
+                {
+                    T *pc = P + (size_t)(j + 1 - k0) * pr;
+                    T v = pc[r - k0];
+                    zfms(v, l, pc[j - k0]);
+                    pc[r - k0] = v;
+                    const R av = fabs(v.x) + fabs(v.y);
+                    if (av > best) { best = av; bi = r; }
+                }
+                for (int c = j + 2; c < kend; ++c) {
+                    T *pc = P + (size_t)(c - k0) * pr;
+                    T v = pc[r - k0];
+                    zfms(v, l, pc[j - k0]);
+                    pc[r - k0] = v;
+                }
             }
+            warp_best(best, bi);
         }
-        if (ncols > 0) warp_best(best, bi);
         __syncthreads();
     }
     for (int e = tid; e < pr * nb; e += PANEL_THREADS) {
@@ -550,13 +561,20 @@ __global__ void __launch_bounds__(GETRS_THREADS) getrs_fused_kernel(int n, int n
         }
         __syncthreads();
         for (int i = kend + tid; i < n; i += blockDim.x) {
+            // the row's LU_NB entries of L first, all loads in flight at once
+            // (one L2 round trip per row instead of one per entry)
+            float2 lrow[LU_NB];
+#pragma unroll
+            for (int t = 0; t < LU_NB; ++t) lrow[t] = t < nb ? LU[i + (size_t)(k0 + t) * lda] : zero;
             float2 acc[GETRS_RB];
 #pragma unroll
             for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
-            for (int t = 0; t < nb; ++t) {
-                const float2 l = LU[i + (size_t)(k0 + t) * lda];
 #pragma unroll
-                for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], l, X[k0 + t + (size_t)c * n]);
+            for (int t = 0; t < LU_NB; ++t) {
+                if (t < nb) {
+#pragma unroll
+                    for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], lrow[t], X[k0 + t + (size_t)c * n]);
+                }
             }
 #pragma unroll
             for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];
@@ -583,13 +601,18 @@ __global__ void __launch_bounds__(GETRS_THREADS) getrs_fused_kernel(int n, int n
         }
         __syncthreads();
         for (int i = tid; i < k0; i += blockDim.x) {
+            float2 urow[LU_NB];
+#pragma unroll
+            for (int t = 0; t < LU_NB; ++t) urow[t] = t < nb ? LU[i + (size_t)(k0 + t) * lda] : zero;
             float2 acc[GETRS_RB];
 #pragma unroll
             for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
-            for (int t = 0; t < nb; ++t) {
-                const float2 u = LU[i + (size_t)(k0 + t) * lda];
 #pragma unroll
-                for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], u, X[k0 + t + (size_t)c * n]);
+            for (int t = 0; t < LU_NB; ++t) {
+                if (t < nb) {
+#pragma unroll
+                    for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], urow[t], X[k0 + t + (size_t)c * n]);
+                }
             }
 #pragma unroll
             for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];

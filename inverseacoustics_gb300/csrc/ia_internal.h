@@ -21,11 +21,12 @@ struct ia_context {
     int capturing;         // between ia_capture_begin and ia_capture_end
     int no_tune;           // the autotuner may not time variants (allocation-free calls)
     int last_fallback;     // bins the last batched solve recomputed in FP64 (mixed_fallback)
-    // extra streams and events of the staggered IBEM pipeline (one stream per
-    // part beyond the first), created at their first use or by
+    // streams and events of the staggered IBEM pipeline (one stream per part,
+    // part q at the q-th highest stream priority; ev_fork orders them after
+    // the caller's stream), created at their first use or by
     // ia_capture_begin (ensure_side_stream)
-    cudaStream_t side[IA_SPLIT_PARTS - 1];
-    cudaEvent_t ev_rows[IA_SPLIT_PARTS], ev_done[IA_SPLIT_PARTS];
+    cudaStream_t side[IA_SPLIT_PARTS];
+    cudaEvent_t ev_rows[IA_SPLIT_PARTS], ev_done[IA_SPLIT_PARTS], ev_fork;
 };
 
 namespace ia {
