@@ -40,6 +40,8 @@ def _parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side-workloads", action="store_true",
+                    help="headline workload only (skip the other configurations' sub-objects)")
     return ap.parse_args()
 
 
@@ -678,7 +680,7 @@ def run_ours(args):
                               "unit": "FP64 TFLOP/s", "achieved": svd_flops / (t_solve64 / 1000.0) / 1e12,
                               "peak_dgemm_measured": fp64_tflops_dgemm}}
     other = {}
-    if world == 1:
+    if world == 1 and not args.no_side_workloads:
         side = (("radiation_modes", lambda: _bench_radiation(ctx, dev, stream, flush)),
                 ("esm_design_adjoint", lambda: _bench_design(ctx, dev, stream, flush)),
                 ("bem_modes", lambda: _bench_bem_modes(ctx, dev, stream, flush, mesh, w)),
