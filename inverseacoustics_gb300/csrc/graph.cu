@@ -55,9 +55,7 @@ int ia_capture_end(ia_context *ctx, ia_graph **out)
         free(nodes);
     }
     cudaGraphExec_t exec = nullptr;
-    // kernel nodes keep the priority of the stream they were captured from
-    // (the staggered IBEM parts' chains over the next part's assembly)
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(g);
         return cuda_status(e);

@@ -21,10 +21,9 @@ struct ia_context {
     int capturing;         // between ia_capture_begin and ia_capture_end
     int no_tune;           // the autotuner may not time variants (allocation-free calls)
     int last_fallback;     // bins the last batched solve recomputed in FP64 (mixed_fallback)
-    // streams and events of the staggered IBEM pipeline (one stream per part,
-    // part q at the q-th highest stream priority; ev_fork orders them after
-    // the caller's stream), created at their first use or by
-    // ia_capture_begin (ensure_side_stream)
+    // streams and events of the staggered IBEM pipeline (one stream per part;
+    // ev_fork orders them after the caller's stream), created at their first
+    // use or by ia_capture_begin (ensure_side_stream)
     cudaStream_t side[IA_SPLIT_PARTS];
     cudaEvent_t ev_rows[IA_SPLIT_PARTS], ev_done[IA_SPLIT_PARTS], ev_fork;
 };
