@@ -107,6 +107,9 @@ typedef struct {
                               resolve the singular values that decide the solution, so the bin fails the
                               precision guard, as does a bin with any info flag or whose sum of s_i^2
                               misses ||H||_F^2 by more than 1e-10 relative. */
+    int pipeline_parts;    /* IBEM batches: staggered parts, one stream each (0 = automatic: 4 when F is a
+                              multiple of 16 and >= 32, 2 when a multiple of 8 and >= 16, else 1;
+                              explicit: 1..8 dividing F into parts of a multiple of 4 bins) */
     int mixed_fallback;    /* 1 (default): bins that fail the guard are solved again by the FP64 path
                               before the call returns (one host synchronisation per call; skipped while
                               the stream is capturing, where such bins keep IA_INFO_PRECISION); 0: never */

@@ -36,7 +36,7 @@ class Config(C.Structure):
                 ("lambda_fixed", C.c_double), ("tsvd_k", C.c_int), ("precision", C.c_int),
                 ("svd_max_sweeps", C.c_int), ("refine_steps", C.c_int), ("mode_iters", C.c_int),
                 ("mode_oversample", C.c_int), ("gemm_slices", C.c_int),
-                ("mixed_guard", C.c_double), ("mixed_fallback", C.c_int)]
+                ("mixed_guard", C.c_double), ("pipeline_parts", C.c_int), ("mixed_fallback", C.c_int)]
 
 
 IA_ADMM_L1, IA_ADMM_L2, IA_ADMM_LP = 1, 2, 3

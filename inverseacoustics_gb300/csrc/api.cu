@@ -898,10 +898,13 @@ static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_in
     return st;
 }
 
+// the configuration of the fallback solve: FP64, and the automatic part
+// split (the caller's explicit split need not divide the fallback's bins)
 static ia_config fp64_config(const ia_config *cfg)
 {
     ia_config c = *cfg;
     c.precision = IA_PREC_FP64;
+    c.pipeline_parts = 0;
     return c;
 }
 
@@ -983,7 +986,11 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     // blocks (4 bins in FP64, 1 in double-float; parts are multiples of 4)
     // and every later kernel works per frequency, so the results are bitwise
     // those of one F-bin pass.
-    const int parts = (F >= 32 && F % 16 == 0) ? 4 : (F >= 16 && F % 8 == 0) ? 2 : 1;
+    int parts = (F >= 32 && F % 16 == 0) ? 4 : (F >= 16 && F % 8 == 0) ? 2 : 1;
+    if (cfg->pipeline_parts) {
+        parts = cfg->pipeline_parts;
+        if (parts < 1 || parts > IA_SPLIT_PARTS || F % parts || (parts > 1 && (F / parts) % 4)) return IA_ERR_ARG;
+    }
     const int Fp = F / parts;
     const size_t need = ibem_solve_ws_bytes(m, l, Fp, nrhs, cfg);
     int st = ws_reserve(ctx, need * parts);

@@ -7,9 +7,9 @@
 #include <stdint.h>
 #include "../../include/ia.h"
 
-// staggered parts of a large IBEM batch, one stream each (8 measured slower
-// than 4 on the 64-bin bench workload: 1548 vs 1566 freq-solves/s)
-#define IA_SPLIT_PARTS 4
+// staggered parts of a large IBEM batch, one stream each: at most
+// IA_SPLIT_PARTS (ia_config.pipeline_parts), 4 by default for F >= 32
+#define IA_SPLIT_PARTS 8
 
 struct ia_context {
     int device;
