@@ -250,9 +250,15 @@ static __device__ double select_lambda(const double *s, const double *b2, int p,
         rpm = fmax(s[p - 1], s1 * 16.0 * 2.220446049250313e-16);
         ratio = pow(s1 / rpm, 1.0 / (np - 1));
     }
+    // grid values first, one pow per thread (a warp-uniform pow per grid point
+    // would run on all 32 lanes of the slow FP64 pipe); each slot then holds
+    // its G value, written by the one warp that read its lambda
+    for (int t = threadIdx.x; t < np; t += blockDim.x) gval[t] = gcv_grid_point(fixed, lhi, llo, ratio, rpm, np, t);
+    __syncthreads();
     for (int t = wid; t < np; t += nw) {
-        double lt = gcv_grid_point(fixed, lhi, llo, ratio, rpm, np, t);
-        double g = gcv_value(d, lt, cfg.gcv_mode, true, lane);
+        const double lt = gval[t];
+        const double g = gcv_value(d, lt, cfg.gcv_mode, true, lane);
+        __syncwarp();
         if (lane == 0) gval[t] = g;
     }
     __syncthreads();
@@ -287,8 +293,11 @@ static __device__ double grid_brent(const Obj &obj, double s1, double rpm, int n
     __shared__ int s_jmin;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const double ratio = pow(s1 / rpm, 1.0 / (np - 1));
+    for (int t = threadIdx.x; t < np; t += blockDim.x) gval[t] = pow(ratio, (double)(np - 1 - t)) * rpm;
+    __syncthreads();
     for (int t = wid; t < np; t += nw) {
-        const double g = obj(pow(ratio, (double)(np - 1 - t)) * rpm);
+        const double g = obj(gval[t]);
+        __syncwarp();
         if (lane == 0) gval[t] = g;
     }
     __syncthreads();

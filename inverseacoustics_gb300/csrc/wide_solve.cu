@@ -1062,10 +1062,9 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     if (st) return st;
     normalize_cols_kernel<<<batch, 256, 0, ctx->stream>>>(N, R32, J32, perm);
     IA_LAUNCH_CHECK(ctx);
-    // 2. E = H H^H (or its conjugate for H^T input) by the double-float GEMM:
-    // H reaches this path from the double-float transfer (~1e-13 relative), so
-    // an FP64 product would not make E more accurate.
-    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
+    // 2. E = H H^H (or its conjugate for H^T input) at FP64 level (EigGemm):
+    // H reaches this path from the mixed transfer (~1e-11 relative), so an
+    // FP64 product would not make E more accurate.
     if (transposed) st = eg(OP_C, OP_N, N, N, n, 1.0, A, n, sA, A, n, sA, 0.0, E, N, sN, batch);
     else st = eg(OP_N, OP_C, N, N, n, 1.0, A, m, sA, A, m, sA, 0.0, E, N, sN, batch);
     if (st) return st;
@@ -1094,7 +1093,8 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     }
     // 4. pairs of near-equal eigenvalues stay coupled through the first-order
     // steps (the refinement treats them as a cluster): orthonormalise X
-    // (Newton-Schulz, X <- 1.5 X - 0.5 X X^H X), form S = X^H E X in FP64 and
+    // (Newton-Schulz, X <- 1.5 X - 0.5 X X^H X), form S = X^H E X at FP64
+    // level (EigGemm; FP64 CUDA-core GEMMs cost 0.5 ms per 16 bins here) and
     // rotate the coupled pairs apart with two-sided Jacobi; lam_e <- diag(S).
     // Suited to spectra with few clusters (a transfer matrix's decaying
     // singular values): on a dense clustered spectrum (the radiation operator
@@ -1107,8 +1107,8 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
         X = Xn;
         Xn = t;
     }
-    if ((st = zgemm_batched(ctx, OP_N, OP_N, N, N, N, one, E, N, sN, X, N, sN, zero, T1, N, sN, batch))) return st;
-    if ((st = zgemm_batched(ctx, OP_C, OP_N, N, N, N, one, X, N, sN, T1, N, sN, zero, Sm, N, sN, batch))) return st;
+    if ((st = eg(OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
+    if ((st = eg(OP_C, OP_N, N, N, N, 1.0, X, N, sN, T1, N, sN, 0.0, Sm, N, sN, batch))) return st;
     {
         const int P = (N + (N & 1)) / 2;
         const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
