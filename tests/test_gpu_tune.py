@@ -35,7 +35,9 @@ def test_tuned_equals_untuned(cuda, ctx, tmp_path, monkeypatch):
     tuned = api.ibem_solve_batch(ctx, mesh, *args, cfg)
     torch.cuda.synchronize()
     n = L.ia_tune_table_size()
-    assert n > 5
+    # one entry per GEMM shape of the 162-node LU's trailing updates (the
+    # FP64-level products run on the tensor-core GEMM, which is not tuned)
+    assert n >= 4
     lines = tune_file.read_text().split("\n")
     assert len([x for x in lines if x.strip()]) == n
     monkeypatch.setenv("IA_TUNE", "0")
