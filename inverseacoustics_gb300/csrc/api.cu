@@ -300,6 +300,7 @@ int ia_destroy(ia_context *ctx)
         cudaEventDestroy(ctx->ev_fork);
         for (int i = 0; i < IA_SPLIT_PARTS; ++i) cudaStreamDestroy(ctx->side[i]);
     }
+    if (ctx->dcount) cudaFree(ctx->dcount);
     free(ctx);
     return IA_OK;
 }

@@ -363,6 +363,162 @@ __global__ void identity_kernel(int N, T *V, long long sV)
     }
 }
 
+// ---- GPU-wide Jacobi for large systems (M > 256) ------------------------
+// One launch per round of the circle ordering, one CTA per (pair, bin), so a
+// few large systems (the 642 x 642 G Z of the drop-in invr() with n_am = m)
+// spread over every SM instead of holding one SM each through ~10 sweeps of
+// 641 rounds.  A bin's CTAs skip the rounds of a sweep once its previous sweep
+// rotated nothing; the host reads the per-sweep total after each sweep (one
+// synchronisation per sweep) and stops when every bin is done.  Same
+// rotations, tolerance and ordering as the one-CTA kernels; the column dot
+// products reduce over the CTA in a fixed order.
+constexpr int WIDE_THREADS = 256;
+
+template <class T>
+__global__ void __launch_bounds__(WIDE_THREADS)
+    jacobi_round_kernel(int M, int Mdot, int N, T *Y, long long sY, T *V, long long sV, int round,
+                        typename ctraits<T>::R tol, const int *__restrict__ active, int *__restrict__ rot)
+{
+    typedef typename ctraits<T>::R R;
+    __shared__ R red[4][WIDE_THREADS / 32];
+    __shared__ R s_c;
+    __shared__ T s_sp;
+    __shared__ int s_do;
+    const int f = blockIdx.y;
+    if (!active[f]) return;
+    const int N2 = N + (N & 1);
+    int i, j;
+    rr_pair(N2, round, blockIdx.x, i, j);
+    if (j >= N) return;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    T *yi = Y + f * sY + (size_t)i * M, *yj = Y + f * sY + (size_t)j * M;
+    R a = 0, b = 0;
+    T g = ctraits<T>::make(0, 0);
+    for (int r = tid; r < Mdot; r += WIDE_THREADS) {
+        const T u = yi[r], v = yj[r];
+        a += zabs2(u);
+        b += zabs2(v);
+        zcfma(g, u, v);
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    g.x = warp_sum(g.x);
+    g.y = warp_sum(g.y);
+    if (lane == 0) {
+        red[0][wid] = a;
+        red[1][wid] = b;
+        red[2][wid] = g.x;
+        red[3][wid] = g.y;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        a = red[0][0];
+        b = red[1][0];
+        g = ctraits<T>::make(red[2][0], red[3][0]);
+        for (int w = 1; w < WIDE_THREADS / 32; ++w) {
+            a += red[0][w];
+            b += red[1][w];
+            g.x += red[2][w];
+            g.y += red[3][w];
+        }
+        R c;
+        T sp;
+        s_do = jacobi_rotation(a, b, g, tol, c, sp) ? 1 : 0;
+        s_c = c;
+        s_sp = sp;
+        if (s_do) atomicAdd(&rot[f], 1);
+    }
+    __syncthreads();
+    if (!s_do) return;
+    const R c = s_c;
+    const T sp = s_sp;
+    for (int r = tid; r < M; r += WIDE_THREADS) {
+        T u = yi[r], v = yj[r];
+        rotate_pair(u, v, c, sp);
+        yi[r] = u;
+        yj[r] = v;
+    }
+    if (V) {
+        T *vi = V + f * sV + (size_t)i * N, *vj = V + f * sV + (size_t)j * N;
+        for (int r = tid; r < N; r += WIDE_THREADS) {
+            T u = vi[r], v = vj[r];
+            rotate_pair(u, v, c, sp);
+            vi[r] = u;
+            vj[r] = v;
+        }
+    }
+}
+
+// counters: active[batch], rot[batch], total.  reset: every bin active.
+__global__ void jacobi_wide_reset_kernel(int batch, int *cnt)
+{
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < batch; f += gridDim.x * blockDim.x) {
+        cnt[f] = 1;
+        cnt[batch + f] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[2 * batch] = 0;
+}
+
+// end of a sweep: a bin stays active while it rotated; total = active bins
+__global__ void jacobi_wide_sweep_kernel(int batch, int *cnt)
+{
+    __shared__ int s_tot;
+    if (threadIdx.x == 0) s_tot = 0;
+    __syncthreads();
+    int n = 0;
+    for (int f = threadIdx.x; f < batch; f += blockDim.x) {
+        const int act = cnt[f] && cnt[batch + f] > 0;
+        cnt[f] = act;
+        cnt[batch + f] = 0;
+        n += act;
+    }
+    atomicAdd(&s_tot, n);
+    __syncthreads();
+    if (threadIdx.x == 0) cnt[2 * batch] = s_tot;
+}
+
+__global__ void jacobi_wide_flag_kernel(int batch, const int *cnt, int *info)
+{
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < batch; f += gridDim.x * blockDim.x)
+        if (cnt[f] && info) atomicOr(&info[f], IA_INFO_NOCONV);
+}
+
+template <class T>
+static int jacobi_wide(ia_context *ctx, int M, int Mdot, int N, T *Y, long long sY, T *V, long long sV, int batch,
+                       int max_sweeps, typename ctraits<T>::R tol, int *info)
+{
+    const size_t need = 2 * (size_t)batch + 1;
+    if (ctx->dcount_n < need) {
+        if (ctx->dcount) IA_CUDA_TRY(cudaFree(ctx->dcount));
+        ctx->dcount = nullptr;
+        ctx->dcount_n = 0;
+        IA_CUDA_TRY(cudaMalloc((void **)&ctx->dcount, sizeof(int) * need));
+        ctx->dcount_n = need;
+    }
+    int *cnt = ctx->dcount;
+    jacobi_wide_reset_kernel<<<(batch + 255) / 256, 256, 0, ctx->stream>>>(batch, cnt);
+    IA_LAUNCH_CHECK(ctx);
+    const int N2 = N + (N & 1), pairs = N2 / 2;
+    int total = batch;
+    int sweep = 0;
+    for (; sweep < max_sweeps && total > 0; ++sweep) {
+        for (int round = 0; round < N2 - 1; ++round) {
+            jacobi_round_kernel<T><<<dim3(pairs, batch), WIDE_THREADS, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV,
+                                                                                         round, tol, cnt, cnt + batch);
+            IA_LAUNCH_CHECK(ctx);
+        }
+        jacobi_wide_sweep_kernel<<<1, 256, 0, ctx->stream>>>(batch, cnt);
+        IA_LAUNCH_CHECK(ctx);
+        IA_CUDA_TRY(cudaMemcpyAsync(&total, cnt + 2 * batch, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        IA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    }
+    if (total > 0) {
+        jacobi_wide_flag_kernel<<<(batch + 255) / 256, 256, 0, ctx->stream>>>(batch, cnt, info);
+        IA_LAUNCH_CHECK(ctx);
+    }
+    return IA_OK;
+}
+
 template <class T>
 int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int batch, int max_sweeps, int *info)
 {
@@ -409,8 +565,15 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
         jacobi_kernel<T, 4><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
     else if (M <= 256)
         jacobi_kernel<T, 8><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
-    else
+    else {
+        // large systems: over the whole GPU, round by round, where the host may
+        // synchronise (not under stream capture)
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        IA_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
+        if (cs == cudaStreamCaptureStatusNone && !ctx->capturing)
+            return jacobi_wide<T>(ctx, M, Mdot, N, Y, sY, V, sV, batch, max_sweeps, tol, info);
         jacobi_kernel<T, 0><<<batch, nw * 32, 0, ctx->stream>>>(M, Mdot, N, Y, sY, V, sV, max_sweeps, tol, info);
+    }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }

@@ -230,3 +230,38 @@ def test_bem_modes_complex_mixed_many_modes(cuda, ctx, ellipsoid):
         assert np.max(np.abs(s1[f] - s0[f])) <= 1e-10 * s0[f][0]
         X = U1[f].T
         assert np.max(np.abs(X.conj().T @ X - np.eye(nm))) < 1e-12
+
+
+def test_bem_modes_complex_all_modes_full_sphere(cuda, ctx):
+    """FP64 complex variant with every mode (n_am = m, the drop-in invr()'s
+    natural call) on the 642-node sphere: the SVD of the whole 642 x 642 G Z.
+    It runs round by round over the whole GPU (one CTA per column pair and
+    bin); the test prints its time.  s within 1e-11 s_1 of LAPACK's, columns
+    orthonormal to 1e-12, residuals ||(G Z)(G Z)^H u - s^2 u|| within
+    1e-11 s_1^2."""
+    import time
+    import torch
+    from inverseacoustics_gb300 import api
+    nodes, elems = g.icosphere(3, 0.1)
+    m = nodes.shape[1]
+    mics = g.hemisphere_array(np.random.default_rng(11), 48, 0.5)
+    ks = 2 * np.pi * np.array([900.0]) / C
+    mesh = api.Mesh(ctx, nodes, elems)
+    args = (T(mics, cuda), T(ks, cuda), m, api.default_config(precision=0))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = api.bem_modes_batch(ctx, mesh, *args, complex_modes=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    s, U, Hr, Pr, info = (a.cpu().numpy() for a in out)
+    mesh.close()
+    print(f"\ncomplex BEM modes, all {m} of the 642-node sphere, FP64: {dt:.3f} s per frequency")
+    assert int(np.abs(info).sum()) == 0
+    reg, sing = Q.builtin()
+    so, Uo, _, _, Zo, Go = O.bem_modes_complex(nodes, elems, mics, ks[0], reg, sing, C, RHO, m)
+    Y = Go @ Zo
+    X = U[0].T
+    assert np.max(np.abs(s[0] - so)) <= 1e-11 * so[0]
+    assert np.max(np.abs(X.conj().T @ X - np.eye(m))) < 1e-12
+    res = np.linalg.norm(Y @ (Y.conj().T @ X) - X * s[0] ** 2, axis=0)
+    assert res.max() <= 1e-11 * so[0] ** 2
