@@ -500,15 +500,15 @@ int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int l
 // thread per row, the block's LU_NB columns of L or U read coalesced from
 // global memory (L2).  Replaces 2 n / LU_NB dependent small launches (a
 // diagonal-block solve and a GEMM update per step) by one.
-constexpr int GETRS_RB = 8;   // 4 and 16 measured slower (transfer stage 30.1 / 30.5 vs 29.5 ms per 64 bins)
-constexpr int GETRS_THREADS = 32 * GETRS_RB;   // a warp per column in the diagonal solves
+// right-hand sides per CTA: a warp per column in the diagonal solves
 
 __device__ __forceinline__ float2 shfl_c(float2 v, int src)
 {
     return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-__global__ void __launch_bounds__(GETRS_THREADS) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
+template <int GETRS_RB>
+__global__ void __launch_bounds__(32 * GETRS_RB) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
                                                                      int lda, long long sA,
                                                                      const int *__restrict__ ipiv, float2 *B, int ldb,
                                                                      long long sB)
@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(GETRS_THREADS) getrs_fused_kernel(int n, int n
     }
 }
 
-static size_t getrs_fused_smem(int n)
+static size_t getrs_fused_smem(int n, int GETRS_RB)
 {
     return sizeof(float2) * ((size_t)n * GETRS_RB + (size_t)LU_NB * (LU_NB + 1)) + sizeof(int) * (size_t)n;
 }
@@ -636,13 +636,15 @@ int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long l
 {
     if (n <= 0 || nrhs <= 0 || batch <= 0) return IA_OK;
     if constexpr (std::is_same<T, float2>::value) {
-        const size_t smem = getrs_fused_smem(n);
+        const char *env = getenv("IA_GETRS_RB");
+        const int rb = (env && atoi(env) == 16) ? 16 : 8;
+        const size_t smem = getrs_fused_smem(n, rb);
         if (smem <= 200 * 1024) {
+            auto kern = rb == 16 ? getrs_fused_kernel<16> : getrs_fused_kernel<8>;
             if (smem > 48 * 1024)
-                IA_CUDA_TRY(cudaFuncSetAttribute(getrs_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 200 * 1024));
-            dim3 gf((nrhs + GETRS_RB - 1) / GETRS_RB, batch);
-            getrs_fused_kernel<<<gf, GETRS_THREADS, smem, ctx->stream>>>(n, nrhs, LU, lda, sA, ipiv, B, ldb, sB);
+                IA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            dim3 gf((nrhs + rb - 1) / rb, batch);
+            kern<<<gf, 32 * rb, smem, ctx->stream>>>(n, nrhs, LU, lda, sA, ipiv, B, ldb, sB);
             IA_LAUNCH_CHECK(ctx);
             return IA_OK;
         }
