@@ -42,7 +42,9 @@ namespace ia {
 // accumulators of a block dominate the registers (244 at 4, 146 at 2, 96 at
 // 1) and the row buffers the shared memory, so one frequency per CTA runs 5
 // CTAs per SM instead of 2, which outweighs recomputing the geometry per
-// frequency (measured per 64-bin launch: 13.1 ms at 4, 11.7 at 2, 11.0 at 1).
+// frequency (measured per 64-bin launch: 13.1 ms at 4, 11.7 at 2, 11.0 at 1;
+// with the table-driven sin/cos the whole 64-bin pass still runs 28.2 ms at 2
+// against 27.9 at 1).
 constexpr int IBEM_FB_MAX = 4;
 template <class R> struct AsmBlock { static constexpr int FB = 4; };
 template <> struct AsmBlock<dfl> { static constexpr int FB = 1; };
