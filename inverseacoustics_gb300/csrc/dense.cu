@@ -411,75 +411,6 @@ __global__ void __launch_bounds__(128) trsm_block_kernel(int nbk, const T *Tm, i
         if (r < nbk) X[r + (size_t)col * ldx] = x[r];
 }
 
-// Trailing update of the blocked LU, A22 -= L21 U12 (rest x rest, K = nb <=
-// LU_NB): 64 x 64 outputs per CTA, 4 x 4 per thread; the whole K extent of
-// both operand tiles is staged in shared memory at once (one barrier), and
-// each output sums k in order before C - acc, so the factors are bitwise
-// those of gemm_kernel (alpha = -1, beta = 1) -- without its eight K-chunk
-// stages, runtime transposition branches and per-element bounds checks.
-constexpr int LUU_TILE = 64, LUU_T = 4, LUU_THREADS = 256;
-
-template <class T>   // FP32 complex (33 KB of static shared memory)
-__global__ void __launch_bounds__(LUU_THREADS)
-    lu_update_kernel(int rest, int nb, const T *__restrict__ L21, const T *__restrict__ U12, T *__restrict__ A22,
-                     int lda, long long sA)
-{
-    __shared__ T Ls[LU_NB][LUU_TILE + 1];
-    __shared__ T Us[LU_NB][LUU_TILE + 1];
-    const int f = blockIdx.z;
-    L21 += f * sA;
-    U12 += f * sA;
-    A22 += f * sA;
-    const int m0 = blockIdx.y * LUU_TILE, n0 = blockIdx.x * LUU_TILE;
-    const int tid = threadIdx.x;
-    const T zero = ctraits<T>::make(0, 0);
-    // L21 tile: rows m0.., columns 0..nb-1 (column-major, coalesced down rows)
-    for (int e = tid; e < LU_NB * LUU_TILE; e += LUU_THREADS) {
-        const int r = e % LUU_TILE, k = e / LUU_TILE;
-        Ls[k][r] = (k < nb && m0 + r < rest) ? L21[m0 + r + (size_t)k * lda] : zero;
-    }
-    // U12 tile: rows 0..nb-1, columns n0..
-    for (int e = tid; e < LU_NB * LUU_TILE; e += LUU_THREADS) {
-        const int k = e % LU_NB, c = e / LU_NB;
-        Us[k][c] = (k < nb && n0 + c < rest) ? U12[k + (size_t)(n0 + c) * lda] : zero;
-    }
-    __syncthreads();
-    constexpr int NT = LUU_TILE / LUU_T;   // 16 x 16 threads
-    const int tx = tid % NT, ty = tid / NT;
-    T acc[LUU_T][LUU_T];
-#pragma unroll
-    for (int i = 0; i < LUU_T; ++i)
-#pragma unroll
-        for (int j = 0; j < LUU_T; ++j) acc[i][j] = zero;
-    for (int k = 0; k < nb; ++k) {
-        T a[LUU_T], b[LUU_T];
-#pragma unroll
-        for (int i = 0; i < LUU_T; ++i) a[i] = Ls[k][ty + NT * i];
-#pragma unroll
-        for (int j = 0; j < LUU_T; ++j) b[j] = Us[k][tx + NT * j];
-#pragma unroll
-        for (int i = 0; i < LUU_T; ++i)
-#pragma unroll
-            for (int j = 0; j < LUU_T; ++j) zfma(acc[i][j], a[i], b[j]);
-    }
-#pragma unroll
-    for (int i = 0; i < LUU_T; ++i) {
-        const int r = m0 + ty + NT * i;
-        if (r >= rest) continue;
-#pragma unroll
-        for (int j = 0; j < LUU_T; ++j) {
-            const int c = n0 + tx + NT * j;
-            if (c >= rest) continue;
-            T *p = A22 + r + (size_t)c * lda;
-            const T old = *p;
-            // (-acc) + old: gemm_kernel's alpha (-1) acc + beta (1) C, the same roundings
-            T v = ctraits<T>::make(-acc[i][j].x, -acc[i][j].y);
-            v = zadd(v, old);
-            *p = v;
-        }
-    }
-}
-
 template <class T>
 int getrf_batched(ia_context *ctx, int n, T *A, int lda, long long sA, int *ipiv, int *info, int batch)
 {
@@ -511,20 +442,10 @@ int getrf_batched(ia_context *ctx, int n, T *A, int lda, long long sA, int *ipiv
         trsm_block_kernel<T, false><<<g, 128, 0, ctx->stream>>>(nb, A + k0 + (size_t)k0 * lda, lda, sA,
                                                                  A + k0 + (size_t)kend * lda, lda, sA, rest);
         IA_LAUNCH_CHECK(ctx);
-        if constexpr (std::is_same<T, float2>::value) {
-            dim3 gu((rest + LUU_TILE - 1) / LUU_TILE, (rest + LUU_TILE - 1) / LUU_TILE, batch);
-            lu_update_kernel<T><<<gu, LUU_THREADS, 0, ctx->stream>>>(rest, nb, A + kend + (size_t)k0 * lda,
-                                                                     A + k0 + (size_t)kend * lda,
-                                                                     A + kend + (size_t)kend * lda, lda, sA);
-            IA_LAUNCH_CHECK(ctx);
-        } else {
-            // FP64: the generic GEMM (its tiles fit the 48 KB of static shared
-            // memory; the FP64 pipe bounds it either way)
-            int r = gemm_batched<T>(ctx, OP_N, OP_N, rest, rest, nb, mone, A + kend + (size_t)k0 * lda, lda, sA,
-                                    A + k0 + (size_t)kend * lda, lda, sA, one, A + kend + (size_t)kend * lda, lda,
-                                    sA, batch);
-            if (r) return r;
-        }
+        int r = gemm_batched<T>(ctx, OP_N, OP_N, rest, rest, nb, mone, A + kend + (size_t)k0 * lda, lda, sA,
+                                A + k0 + (size_t)kend * lda, lda, sA, one, A + kend + (size_t)kend * lda, lda, sA,
+                                batch);
+        if (r) return r;
     }
     return IA_OK;
 }
