@@ -1,6 +1,8 @@
 """GPU suite: the kernel-variant autotuner.  Tuned and untuned runs of the
 mixed IBEM pipeline must agree bit for bit (variants differ only in the
-thread mapping), the table must fill, and a tuning file must round-trip."""
+thread mapping), the table must fill, and a tuning file must round-trip.
+The mixed pipeline's tuned GEMMs are its FP32 LU trailing updates (its
+FP64-level products run on the tensor-core GEMM, which is not tuned)."""
 import os
 
 import numpy as np
@@ -35,8 +37,7 @@ def test_tuned_equals_untuned(cuda, ctx, tmp_path, monkeypatch):
     tuned = api.ibem_solve_batch(ctx, mesh, *args, cfg)
     torch.cuda.synchronize()
     n = L.ia_tune_table_size()
-    # one entry per GEMM shape of the 162-node LU's trailing updates (the
-    # FP64-level products run on the tensor-core GEMM, which is not tuned)
+    # one entry per GEMM shape of the 162-node LU's trailing updates
     assert n >= 4
     lines = tune_file.read_text().split("\n")
     assert len([x for x in lines if x.strip()]) == n
