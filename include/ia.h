@@ -59,8 +59,11 @@ typedef enum {
 #define IA_INFO_SINGULAR  2  /* zero pivot */
 #define IA_INFO_NONFINITE 4  /* NaN/Inf met */
 #define IA_INFO_TIMEOUT   8  /* a bounded device-side wait ran out (the entry's output is not written) */
-#define IA_INFO_PRECISION 16 /* mixed path: the bin's result failed the precision guard (see mixed_guard) and
-                                was not recomputed in FP64 (fallback off, or the stream was capturing) */
+#define IA_INFO_PRECISION 16 /* mixed path: the bin's regularisation level is below the mixed floor
+                                (mixed_guard) and the bin was not recomputed in FP64 (fallback off, or
+                                the stream was capturing) */
+#define IA_INFO_UNRESOLVED 32 /* mixed path: the bin's eigen-decomposition failed the trace check
+                                 (sum s^2 against ||H||_F^2) and was not solved again */
 
 enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
 enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };
@@ -104,15 +107,17 @@ typedef struct {
                               operand (default 7); 0 = double-float CUDA-core GEMM */
     double mixed_guard;    /* mixed solves: the smallest lambda / s_1 (TSVD: s_k / s_1) the mixed path
                               answers (default 1e-3).  Below it the Gram-based mixed eigensolver does not
-                              resolve the singular values that decide the solution, so the bin fails the
-                              precision guard, as does a bin with any info flag or whose sum of s_i^2
-                              misses ||H||_F^2 by more than 1e-10 relative. */
+                              resolve the singular values that decide the solution (IA_INFO_PRECISION);
+                              a bin whose sum of s_i^2 misses ||H||_F^2 by more than 1e-9 relative fails
+                              too (IA_INFO_UNRESOLVED), as does a bin with any solver flag. */
     int pipeline_parts;    /* IBEM batches: staggered parts, one stream each (0 = automatic: 4 when F is a
                               multiple of 16 and >= 32, 2 when a multiple of 8 and >= 16, else 1;
                               explicit: 1..8 dividing F into parts of a multiple of 4 bins) */
-    int mixed_fallback;    /* 1 (default): bins that fail the guard are solved again by the FP64 path
-                              before the call returns (one host synchronisation per call; skipped while
-                              the stream is capturing, where such bins keep IA_INFO_PRECISION); 0: never */
+    int mixed_fallback;    /* 1 (default): bins that fail the guard are solved again before the call
+                              returns -- IA_INFO_UNRESOLVED alone by the mixed path with 3 eigen-
+                              refinement steps first, everything else (and what fails again) by the
+                              FP64 path (one host synchronisation per call; skipped while the stream
+                              is capturing, where such bins keep their flags); 0: never */
 } ia_config;
 
 /* quadrature rules for IBEM: barycentric (xi1, xi2, w) structure-of-arrays,

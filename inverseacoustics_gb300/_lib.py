@@ -16,7 +16,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "allocatio
           4: "Jacobi iteration did not converge", 5: "singular matrix", 6: "non-finite value",
           7: "invalid quadrature rule", 8: "size above the entry point's limit",
           9: "workspace would grow during stream capture"}
-IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE, IA_INFO_TIMEOUT, IA_INFO_PRECISION = 1, 2, 4, 8, 16
+IA_INFO_NOCONV, IA_INFO_SINGULAR, IA_INFO_NONFINITE, IA_INFO_TIMEOUT = 1, 2, 4, 8
+IA_INFO_PRECISION, IA_INFO_UNRESOLVED = 16, 32
 IA_GCV_STANDARD, IA_GCV_REFERENCE = 0, 1
 IA_PREC_FP64, IA_PREC_MIXED = 0, 1
 IA_METHOD_TIKHONOV_GCV, IA_METHOD_TSVD, IA_METHOD_TIKHONOV_FIXED = 0, 1, 2

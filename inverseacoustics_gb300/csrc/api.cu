@@ -838,32 +838,16 @@ static int move_bins(ia_context *ctx, const void *src, void *dst, size_t bytes, 
     return IA_OK;
 }
 
-// redo(Fb, in, out, info): the entry point in FP64 on Fb compact bins
-using RedoFn = std::function<int(int, void *const *, void *const *, int *)>;
+// redo(Fb, in, out, info, cfg): the entry point with cfg on Fb compact bins
+using RedoFn = std::function<int(int, void *const *, void *const *, int *, const ia_config *)>;
 
-// After a batched solve issued on ctx->stream: with the mixed path and
-// cfg->mixed_fallback, the bins whose info word is set (the precision guard's
-// IA_INFO_PRECISION or any solver flag) are solved again by the FP64 path on
-// compact copies of their per-bin inputs, and the FP64 outputs and info words
-// replace the mixed ones.  One host synchronisation (the info words); nothing
-// happens while the stream is capturing, where the flags stay for the caller.
-// The index list and compact copies live in one stream-ordered allocation
-// that is released before the call returns.
-static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_info, std::initializer_list<BinSpan> ins,
-                         std::initializer_list<BinSpan> outs, const RedoFn &redo)
+// The bins idx of a finished batched call, solved again with rc on compact
+// copies of their per-bin inputs; the outputs and info words replace the
+// first attempt's.  The index list and compact copies live in one
+// stream-ordered allocation released before the function returns.
+static int redo_bins(ia_context *ctx, const std::vector<int> &idx, int *d_info, std::initializer_list<BinSpan> ins,
+                     std::initializer_list<BinSpan> outs, const RedoFn &redo, const ia_config *rc)
 {
-    ctx->last_fallback = 0;
-    if (cfg->precision != IA_PREC_MIXED || !cfg->mixed_fallback) return IA_OK;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    IA_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
-    if (cs != cudaStreamCaptureStatusNone || ctx->capturing) return IA_OK;
-    std::vector<int> h((size_t)F);
-    IA_CUDA_TRY(cudaMemcpyAsync(h.data(), d_info, sizeof(int) * (size_t)F, cudaMemcpyDeviceToHost, ctx->stream));
-    IA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    std::vector<int> idx;
-    for (int f = 0; f < F; ++f)
-        if (h[f]) idx.push_back(f);
-    if (idx.empty()) return IA_OK;
     const int Fb = (int)idx.size();
     size_t bytes = 2 * ws_round(sizeof(int) * (size_t)Fb);
     for (const BinSpan &a : ins) bytes += ws_round(a.bytes * Fb);
@@ -883,7 +867,7 @@ static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_in
         if (!st) st = move_bins(ctx, a.base, c, a.bytes, d_idx, Fb, false);
     }
     for (const BinSpan &a : outs) cout.push_back(a.base ? (void *)cur.take<char>(a.bytes * Fb) : nullptr);
-    if (!st) st = redo(Fb, cin.data(), cout.data(), c_info);
+    if (!st) st = redo(Fb, cin.data(), cout.data(), c_info, rc);
     size_t i = 0;
     for (const BinSpan &a : outs) {
         if (!st && a.base) st = move_bins(ctx, cout[i], const_cast<void *>(a.base), a.bytes, d_idx, Fb, true);
@@ -895,7 +879,6 @@ static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_in
     // the index list's host copy must outlive its transfer
     e = cudaStreamSynchronize(ctx->stream);
     if (!st && e != cudaSuccess) st = cuda_status(e);
-    if (!st) ctx->last_fallback = Fb;
     return st;
 }
 
@@ -907,6 +890,52 @@ static ia_config fp64_config(const ia_config *cfg)
     c.precision = IA_PREC_FP64;
     c.pipeline_parts = 0;
     return c;
+}
+
+// eigen-refinement steps of the mixed retry
+constexpr int MIXED_RETRY_STEPS = 3;
+
+// After a batched solve issued on ctx->stream: with the mixed path and
+// cfg->mixed_fallback, the bins whose info word is set are solved again.
+// A bin flagged only IA_INFO_UNRESOLVED (its eigen-decomposition failed the
+// trace check: Ogita-Aishima steps that did not settle, as on the symmetric
+// plate array's near-degenerate pairs) first gets the mixed path once more
+// with MIXED_RETRY_STEPS refinement steps (that call's own fallback takes
+// what still fails to FP64); every other flagged bin (lambda below the mixed
+// floor, solver flags) goes to the FP64 path directly.  One host
+// synchronisation when nothing is flagged; nothing happens while the stream
+// is capturing, where the flags stay for the caller.
+static int fp64_fallback(ia_context *ctx, const ia_config *cfg, int F, int *d_info, std::initializer_list<BinSpan> ins,
+                         std::initializer_list<BinSpan> outs, const RedoFn &redo)
+{
+    ctx->last_fallback = 0;
+    if (cfg->precision != IA_PREC_MIXED || !cfg->mixed_fallback) return IA_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    IA_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone || ctx->capturing) return IA_OK;
+    std::vector<int> h((size_t)F);
+    IA_CUDA_TRY(cudaMemcpyAsync(h.data(), d_info, sizeof(int) * (size_t)F, cudaMemcpyDeviceToHost, ctx->stream));
+    IA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    const bool can_retry = cfg->refine_steps < MIXED_RETRY_STEPS;
+    std::vector<int> retry, fp64;
+    for (int f = 0; f < F; ++f) {
+        if (!h[f]) continue;
+        if (can_retry && h[f] == IA_INFO_UNRESOLVED) retry.push_back(f);
+        else fp64.push_back(f);
+    }
+    int st = IA_OK;
+    if (!retry.empty()) {
+        ia_config rc = *cfg;
+        rc.refine_steps = MIXED_RETRY_STEPS;
+        rc.pipeline_parts = 0;
+        st = redo_bins(ctx, retry, d_info, ins, outs, redo, &rc);
+    }
+    if (!st && !fp64.empty()) {
+        const ia_config rc = fp64_config(cfg);
+        st = redo_bins(ctx, fp64, d_info, ins, outs, redo, &rc);
+    }
+    if (!st) ctx->last_fallback = (int)(retry.size() + fp64.size());
+    return st;
 }
 
 static size_t solve_ws_bytes(int m, int n, int F, int nrhs, const ia_config *cfg)
@@ -935,9 +964,8 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
     return fp64_fallback(
         ctx, cfg, F, d_info, {{d_H, 16 * (size_t)m * n}, {d_b, 16 * (size_t)nrhs * m}},
         {{d_x, 16 * (size_t)nrhs * n}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
-        [&](int Fb, void *const *in, void *const *out, int *info) {
-            const ia_config c64 = fp64_config(cfg);
-            return ia_solve_batch(ctx, m, n, Fb, (const ia_complex *)in[0], nrhs, (const ia_complex *)in[1], &c64,
+        [&](int Fb, void *const *in, void *const *out, int *info, const ia_config *rc) {
+            return ia_solve_batch(ctx, m, n, Fb, (const ia_complex *)in[0], nrhs, (const ia_complex *)in[1], rc,
                                   (ia_complex *)out[0], (double *)out[1], (double *)out[2], info);
         });
 }
@@ -1002,10 +1030,9 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         return fp64_fallback(
             ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
             {{d_x, 16 * (size_t)nrhs * m}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
-            [&](int Fb, void *const *in, void *const *out, int *info) {
-                const ia_config c64 = fp64_config(cfg);
+            [&](int Fb, void *const *in, void *const *out, int *info, const ia_config *rc) {
                 return ia_ibem_solve_batch(ctx, mesh, l, d_mics, Fb, (const double *)in[0], nrhs,
-                                           (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                           (const ia_complex *)in[1], rc, (ia_complex *)out[0], (double *)out[1],
                                            (double *)out[2], info);
             });
     };
@@ -1066,10 +1093,9 @@ int ia_esm_solve_batch(ia_context *ctx, int l, int m, const double *d_mics, cons
     return fp64_fallback(
         ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
         {{d_x, 16 * (size_t)nrhs * m}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
-        [&](int Fb, void *const *in, void *const *out, int *info) {
-            const ia_config c64 = fp64_config(cfg);
+        [&](int Fb, void *const *in, void *const *out, int *info, const ia_config *rc) {
             return ia_esm_solve_batch(ctx, l, m, d_mics, d_src, Fb, (const double *)in[0], nrhs,
-                                      (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                      (const ia_complex *)in[1], rc, (ia_complex *)out[0], (double *)out[1],
                                       (double *)out[2], info);
         });
 }
@@ -1096,10 +1122,9 @@ int ia_hels_solve_batch(ia_context *ctx, int l, const double *d_pts, int n_sh, i
     return fp64_fallback(
         ctx, cfg, F, d_info, {{d_k, sizeof(double)}, {d_p, 16 * (size_t)nrhs * l}},
         {{d_x, 16 * (size_t)nrhs * nt}, {d_lambda, 8 * (size_t)nrhs}, {d_s, 8 * (size_t)p}},
-        [&](int Fb, void *const *in, void *const *out, int *info) {
-            const ia_config c64 = fp64_config(cfg);
+        [&](int Fb, void *const *in, void *const *out, int *info, const ia_config *rc) {
             return ia_hels_solve_batch(ctx, l, d_pts, n_sh, Fb, (const double *)in[0], nrhs,
-                                       (const ia_complex *)in[1], &c64, (ia_complex *)out[0], (double *)out[1],
+                                       (const ia_complex *)in[1], rc, (ia_complex *)out[0], (double *)out[1],
                                        (double *)out[2], info);
         });
 }

@@ -229,8 +229,9 @@ int wide_solve_batched(ia_context *ctx, int m, int n, int batch, const double2 *
 // one-sided Jacobi start, double-float Ogita-Aishima steps, Newton-Schulz and
 // an FP64 two-sided Jacobi on X^H (H H^H) X; then s, U^H b, GCV, the
 // back-projection and the precision guard (IA_INFO_PRECISION in info[f] for
-// a bin whose lambda (TSVD: s_k) is below cfg->mixed_guard s_1, whose sum of
-// s^2 misses ||H_f||_F^2 by more than 1e-10 relative)
+// a bin whose lambda (TSVD: s_k) is below cfg->mixed_guard s_1,
+// IA_INFO_UNRESOLVED for one whose sum of s^2 misses ||H_f||_F^2 by more than
+// 1e-9 relative)
 size_t wide_solve_mixed_ws_bytes(int m, int n, int nrhs, int batch);
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
                              const double2 *b, const ia_config *cfg, double2 *x, double *lambda, double *s_out,
