@@ -63,7 +63,9 @@ typedef enum {
                                 (mixed_guard) and the bin was not recomputed in FP64 (fallback off, or
                                 the stream was capturing) */
 #define IA_INFO_UNRESOLVED 32 /* mixed path: the bin's eigen-decomposition failed the trace check
-                                 (sum s^2 against ||H||_F^2) and was not solved again */
+                                 (sum s^2 against ||H||_F^2) and was not solved again; with
+                                 IA_INFO_PRECISION too when its spectrum reaches the Gram floor
+                                 sqrt(N eps) s_1 */
 
 enum { IA_GCV_STANDARD = 0, IA_GCV_REFERENCE = 1 };
 enum { IA_PREC_FP64 = 0, IA_PREC_MIXED = 1 };

@@ -1155,7 +1155,16 @@ __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, i
     // a successful decomposition meets the trace to ~1e-10 (X orthonormal to
     // that level after Newton-Schulz); a lost or doubled eigenpair shows at
     // 1e-8 and above
-    if (!(a2 > 0.0 && a2 < INFINITY && fabs(s2 - a2) <= 1e-9 * a2)) info[f] |= IA_INFO_UNRESOLVED;
+    if (!(a2 > 0.0 && a2 < INFINITY && fabs(s2 - a2) <= 1e-9 * a2)) {
+        info[f] |= IA_INFO_UNRESOLVED;
+        // a spectrum that reaches the Gram matrix's floor (eig_beta_kernel
+        // reports values below sqrt(N eps) s_1 there) is beyond the mixed
+        // path: more refinement steps can settle the eigenpairs but not
+        // resolve those values, on which GCV's choice may then hinge
+        double smin = s1;
+        for (int i = 0; i < p; ++i) smin = fmin(smin, sf[i]);
+        if (smin <= 10.0 * sqrt((double)p * 2.220446049250313e-16) * s1) info[f] |= IA_INFO_PRECISION;
+    }
     if (!(level >= ratio * s1)) info[f] |= IA_INFO_PRECISION;
 }
 
