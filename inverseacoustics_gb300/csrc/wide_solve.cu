@@ -1133,17 +1133,22 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
 // for the FP64 path.  A broken eigen-decomposition (an eigenvalue lost or
 // doubled) shows in the trace.
 __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, int p, const double *__restrict__ s,
-                                       int nrhs, const double *__restrict__ lam, int method, int tsvd_k,
-                                       double ratio, int *__restrict__ info)
+                                       int nrhs, const double *__restrict__ lam, const double2 *__restrict__ beta,
+                                       int method, int tsvd_k, double ratio, int *__restrict__ info)
 {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     const double *sf = s + (size_t)f * p;
-    double s2 = 0.0, s1 = 0.0;
+    double s2 = 0.0, s1 = 0.0, smin = INFINITY;
     for (int i = 0; i < p; ++i) {
         s2 += sf[i] * sf[i];
         s1 = fmax(s1, sf[i]);
+        smin = fmin(smin, sf[i]);
     }
+    // eig_beta_kernel reports the values a Gram matrix cannot resolve at
+    // sqrt(N eps) s_1; "unresolved" here: at most twice that
+    const double floor_s = sqrt((double)p * 2.220446049250313e-16) * s1;
+    const bool reaches_floor = smin <= 10.0 * floor_s;
     double level;
     if (method == IA_METHOD_TSVD) {
         level = sf[tsvd_k - 1];
@@ -1157,15 +1162,39 @@ __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, i
     // 1e-8 and above
     if (!(a2 > 0.0 && a2 < INFINITY && fabs(s2 - a2) <= 1e-9 * a2)) {
         info[f] |= IA_INFO_UNRESOLVED;
-        // a spectrum that reaches the Gram matrix's floor (eig_beta_kernel
-        // reports values below sqrt(N eps) s_1 there) is beyond the mixed
-        // path: more refinement steps can settle the eigenpairs but not
-        // resolve those values, on which GCV's choice may then hinge
-        double smin = s1;
-        for (int i = 0; i < p; ++i) smin = fmin(smin, sf[i]);
-        if (smin <= 10.0 * sqrt((double)p * 2.220446049250313e-16) * s1) info[f] |= IA_INFO_PRECISION;
+        // more refinement steps can settle the eigenpairs of a spectrum that
+        // reaches the floor, but not resolve the values below it
+        if (reaches_floor) info[f] |= IA_INFO_PRECISION;
     }
     if (!(level >= ratio * s1)) info[f] |= IA_INFO_PRECISION;
+    // GCV and the unresolved subspace: the data's energy per unresolved
+    // component (their sum |beta|^2 is exact as a subspace quantity) against
+    // the mean energy of the components the chosen lambda filters out.  Where
+    // the unresolved components carry ten times that, they hold signal, and
+    // the true GCV minimum may lie among the values the mixed path cannot
+    // resolve (an order-15 spherical-harmonic operator at low kr: the mixed
+    // GCV settles on a large-lambda local minimum, FP64's is 1e-11 s_1); where
+    // they hold the noise level (the IBEM sphere at 30 dB) the choice stands.
+    if (method != IA_METHOD_TSVD && reaches_floor) {
+        for (int r = 0; r < nrhs; ++r) {
+            const double lm = lam[(size_t)f * nrhs + r], l2 = lm * lm;
+            const double2 *bt = beta + ((size_t)f * nrhs + r) * p;
+            double bu = 0.0, num = 0.0, den = 0.0;
+            int nu = 0;
+            for (int i = 0; i < p; ++i) {
+                const double b2 = bt[i].x * bt[i].x + bt[i].y * bt[i].y;
+                if (sf[i] <= 2.0 * floor_s) {
+                    bu += b2;
+                    ++nu;
+                } else {
+                    const double fi = l2 / (sf[i] * sf[i] + l2);
+                    num += fi * fi * b2;
+                    den += fi;
+                }
+            }
+            if (nu > 0 && den > 0.0 && bu / nu > 10.0 * (num / den)) info[f] |= IA_INFO_PRECISION;
+        }
+    }
 }
 
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
@@ -1193,8 +1222,9 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
                                                                          transposed ? 1 : 0, rank, s, z, nrhs, x);
     IA_LAUNCH_CHECK(ctx);
     // 6. precision guard (IA_INFO_PRECISION for the FP64 fallback)
-    precision_guard_kernel<<<(batch + 127) / 128, 128, 0, ctx->stream>>>(batch, fro2, N, s, nrhs, lam, cfg->method,
-                                                                         cfg->tsvd_k, cfg->mixed_guard, info);
+    precision_guard_kernel<<<(batch + 127) / 128, 128, 0, ctx->stream>>>(batch, fro2, N, s, nrhs, lam, beta,
+                                                                         cfg->method, cfg->tsvd_k, cfg->mixed_guard,
+                                                                         info);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
