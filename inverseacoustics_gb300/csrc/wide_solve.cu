@@ -1175,9 +1175,15 @@ __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, i
     // resolve (an order-15 spherical-harmonic operator at low kr: the mixed
     // GCV settles on a large-lambda local minimum, FP64's is 1e-11 s_1); where
     // they hold the noise level (the IBEM sphere at 30 dB) the choice stands.
+    // A choice at the top of the grid (lambda ~ s_1: everything filtered)
+    // over such a spectrum says only that no resolved level beats filtering
+    // all; the comparison below is then empty, and the true minimum may lie
+    // among the unresolved values (the order-15 HELS operator at kr 3.6:
+    // mixed lambda = s_1, FP64's 3e-8 s_1), so that too goes to FP64.
     if (method != IA_METHOD_TSVD && reaches_floor) {
         for (int r = 0; r < nrhs; ++r) {
             const double lm = lam[(size_t)f * nrhs + r], l2 = lm * lm;
+            if (lm >= 0.5 * s1) info[f] |= IA_INFO_PRECISION;
             const double2 *bt = beta + ((size_t)f * nrhs + r) * p;
             double bu = 0.0, num = 0.0, den = 0.0;
             int nu = 0;
