@@ -163,7 +163,7 @@ def _bench_radiation(ctx, dev, stream, flush, reps=2):
     import numpy as np
     import torch
 
-    from inverseacoustics_gb300 import api
+    from inverseacoustics_gb300 import _lib, api
     from inverseacoustics_gb300 import geometry as g
     w = g.radiation_plate(n_freq=256)
     x, area, mics = w.arrays["centres"], w.params["area"], w.arrays["mics"]
@@ -177,6 +177,7 @@ def _bench_radiation(ctx, dev, stream, flush, reps=2):
     cfgs = {prec: (api.default_config(precision=prec), api.default_config(method=1, tsvd_k=36, precision=prec))
             for prec in (0, 1)}
     outs = {}
+    retried = {}
 
     def stage_times(prec, r):
         cm, cs = cfgs[prec]
@@ -188,6 +189,7 @@ def _bench_radiation(ctx, dev, stream, flush, reps=2):
         lam, modes, info = api.radiation_modes_batch(ctx, R, nm, cm)
         ev[2].record(stream)
         q, _, _, info2 = api.esm_solve_batch(ctx, md, xd, kd, pd, cs)
+        retried[prec] = _lib.lib().ia_last_fallback_bins(ctx.handle)
         ev[3].record(stream)
         W = api.sound_power_batch(ctx, R, q)
         ev[4].record(stream)
@@ -212,6 +214,9 @@ def _bench_radiation(ctx, dev, stream, flush, reps=2):
             "fp64_stages_ms": dict(zip(["sinc_R", "modes", "esm_tsvd", "sound_power"], fp64)),
             "accuracy": {"modes_lambda_vs_fp64_rel_lambda1": err_lam, "tsvd_x_vs_fp64": err_q,
                          "sound_power_vs_fp64": err_w},
+            "tsvd_bins_solved_again": retried.get(1, 0),
+            "note": "mixed TSVD: bins whose eigen-decomposition fails the trace check are solved again "
+                    "(mixed, three refinement steps) inside the timed call",
             "info_clean": int(i1.abs().sum() + j1.abs().sum() + i0.abs().sum() + j0.abs().sum()) == 0}
 
 

@@ -210,3 +210,45 @@ def test_hels_full_size_mixed_matches_oracle(cuda, ctx, hels_case):
     x, lam, s, info, fb = _hels_run(ctx, cuda, w, pts, p, 1)
     assert fb == int((~passed).sum())
     _hels_check(w, pts, p, ref, x, lam, s, info, f"mixed ({fb} bins solved again)", passed)
+
+
+# --------------------------------------------------------------------------
+# Plate workload (config 4): the ESM velocity reconstruction by TSVD (k = 36)
+# from 192 microphones at 0.05 m, 1280 sources, 256 bins 20-2000 Hz.  The
+# symmetric array gives near-degenerate singular pairs; at a few bins the
+# mixed eigensolver's two Ogita-Aishima steps leave a pair unsettled (s_1 off
+# by up to 7e-6 s_1), which its trace check catches (IA_INFO_UNRESOLVED); the
+# fallback solves those bins again on the mixed path with three steps.
+def test_plate_tsvd_mixed_guard_and_retry(cuda, ctx):
+    import torch
+    from inverseacoustics_gb300 import _lib, api
+    from oracle import ia_oracle as O
+    w = g.radiation_plate(n_freq=256)
+    x, area, mics = w.arrays["centres"], w.params["area"], w.arrays["mics"]
+    rng = np.random.default_rng(3)
+    p = np.stack([g.add_noise(rng, g.rayleigh_pressure(mics, x, area, k, w.params["vel"][f]), 30.0)[None, :]
+                  for f, k in enumerate(w.k)])
+    args = (T(mics, cuda), T(x, cuda), T(w.k, cuda), T(p, cuda))
+    so = np.array([np.linalg.svd(O.monopole_matrix(mics, x, k), compute_uv=False)[:36] for k in w.k])
+
+    def run(prec, fallback):
+        q, lam, s, info = api.esm_solve_batch(ctx, *args, api.default_config(method=1, tsvd_k=36, precision=prec,
+                                                                             mixed_fallback=fallback))
+        torch.cuda.synchronize()
+        return q.cpu().numpy(), s.cpu().numpy()[:, :36], info.cpu().numpy(), _lib.lib().ia_last_fallback_bins(ctx.handle)
+
+    q0, s0, info0, _ = run(1, 0)
+    flagged = np.nonzero(info0)[0]
+    es0 = np.abs(s0 - so).max(axis=1) / so[:, 0]
+    q, s, info, fb = run(1, 1)
+    q64, _, info64, _ = run(0, 1)
+    es = np.abs(s - so).max(axis=1) / so[:, 0]
+    eq = np.array([relerr(q[f], q64[f]) for f in range(len(w.k))])
+    print(f"\nplate TSVD, 256 bins: {len(flagged)} bins flagged {sorted(set(info0[flagged].tolist()))} (s_1..36 "
+          f"error there {es0[flagged].max() if len(flagged) else 0:.1e} s_1, elsewhere {np.delete(es0, flagged).max():.1e}); "
+          f"after the retry: s_1..36 {es.max():.1e} s_1, x vs FP64 {eq.max():.1e}")
+    assert (info0[flagged] == _lib.IA_INFO_UNRESOLVED).all()
+    assert np.delete(es0, flagged).max() < 1e-7
+    assert fb == len(flagged)
+    assert int(np.abs(info).sum()) == 0 and int(np.abs(info64).sum()) == 0
+    assert es.max() < 1e-7 and eq.max() < 1e-6
