@@ -507,8 +507,8 @@ __device__ __forceinline__ float2 shfl_c(float2 v, int src)
     return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-template <int GETRS_RB>
-__global__ void __launch_bounds__(32 * GETRS_RB) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
+template <int GETRS_RB, int NT>
+__global__ void __launch_bounds__(NT) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
                                                                      int lda, long long sA,
                                                                      const int *__restrict__ ipiv, float2 *B, int ldb,
                                                                      long long sB)
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(32 * GETRS_RB) getrs_fused_kernel(int n, int n
             D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
         }
         __syncthreads();
-        {
+        if (wid < GETRS_RB) {
             float2 *x = X + (size_t)wid * n + k0;
             float2 v = lane < nb ? x[lane] : zero;
             for (int r = 0; r < nb; ++r) {
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(32 * GETRS_RB) getrs_fused_kernel(int n, int n
             D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
         }
         __syncthreads();
-        {
+        if (wid < GETRS_RB) {
             float2 *x = X + (size_t)wid * n + k0;
             float2 v = lane < nb ? x[lane] : zero;
             for (int r = nb - 1; r >= 0; --r) {
@@ -640,12 +640,15 @@ int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long l
         // 64-bin pass 28.4 against 28.0 ms)
         constexpr int rb = 8;
         const size_t smem = getrs_fused_smem(n, rb);
+        // a warp per right-hand side (512 threads, the rows split further,
+        // measured slower: 29.1 vs 28.2 ms per 64-bin pass)
+        constexpr int nt = 32 * rb;
         if (smem <= 200 * 1024) {
-            auto kern = getrs_fused_kernel<rb>;
+            auto kern = getrs_fused_kernel<rb, nt>;
             if (smem > 48 * 1024)
                 IA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
             dim3 gf((nrhs + rb - 1) / rb, batch);
-            kern<<<gf, 32 * rb, smem, ctx->stream>>>(n, nrhs, LU, lda, sA, ipiv, B, ldb, sB);
+            kern<<<gf, nt, smem, ctx->stream>>>(n, nrhs, LU, lda, sA, ipiv, B, ldb, sB);
             IA_LAUNCH_CHECK(ctx);
             return IA_OK;
         }
