@@ -187,6 +187,10 @@ int tc_slice(ia_context *ctx, bool role_b, Op op, const double2 *X, int ld, long
              int batch, TcPlanes &out, WsCursor &cur);
 int tc_slice(ia_context *ctx, bool role_b, Op op, const float4 *X, int ld, long long sX, int R, int K, int S,
              int batch, TcPlanes &out, WsCursor &cur);
+// both operands of one product (A role: op(A) M x K, B role: op(B) K x N) in
+// one launch
+int tc_slice_pair(ia_context *ctx, Op opa, const double2 *A, int lda, long long sA, int M, Op opb, const double2 *B,
+                  int ldb, long long sB, int N, int K, int S, int batch, TcPlanes &pa, TcPlanes &pb, WsCursor &cur);
 // C (M x N complex FP64) = alpha A B + beta C; info (per batch entry, may be
 // null) gets IA_INFO_TIMEOUT when a pipeline wait ran out
 int tc_gemm(ia_context *ctx, const TcPlanes &A, const TcPlanes &B, int M, int N, double alpha, double beta,

@@ -139,14 +139,29 @@ __device__ __forceinline__ __nv_bfloat162 bf2(int a, int b)
 // maxima, then the digits (the second pass reads from L2).
 constexpr int SL_ROWS = 32, SL_K = 64;
 
-template <class Src, bool RCONTIG, int S>
-__global__ void __launch_bounds__(256) tc_slice_kernel(int R, int K, const Src *__restrict__ X, int ld, long long sX,
-                                                         int conj, int role_b, int Kp, __nv_bfloat16 *__restrict__ planes,
-                                                         int *__restrict__ exps)
+// One operand to slice (a launch can carry two, blockIdx.z picking one)
+template <class Src>
+struct SliceOp {
+    const Src *X;
+    int ld;
+    long long sX;
+    int R, conj, role_b, rcontig;
+    __nv_bfloat16 *planes;
+    int *exps;
+};
+
+template <class Src, int S>
+__global__ void __launch_bounds__(256) tc_slice_kernel(SliceOp<Src> op0, SliceOp<Src> op1, int K, int Kp)
 {
     __shared__ Src tile[SL_ROWS][SL_K + 1];
+    const SliceOp<Src> &op = blockIdx.z ? op1 : op0;
     const int f = blockIdx.y, r0 = blockIdx.x * SL_ROWS, t = threadIdx.x;
-    X += f * sX;
+    const int R = op.R, ld = op.ld, conj = op.conj, role_b = op.role_b;
+    const bool RCONTIG = op.rcontig != 0;
+    if (r0 >= R) return;   // the other operand's taller grid
+    const Src *__restrict__ X = op.X + f * op.sX;
+    __nv_bfloat16 *__restrict__ planes = op.planes;
+    int *__restrict__ exps = op.exps;
     const int rows = role_b ? 2 * R : R;
     const size_t pstride = (size_t)rows * Kp;
     planes += (size_t)f * S * pstride;
@@ -416,21 +431,19 @@ int gemm_launch(ia_context *ctx, const CUtensorMap &ta, const CUtensorMap &tb, c
 }
 
 template <class Src, int S>
-int slice_launch(ia_context *ctx, bool rcontig, bool conj, bool role_b, const Src *X, int ld, long long sX, int R,
-                 int K, int Kp, int batch, __nv_bfloat16 *planes, int *exps)
+int slice_launch(ia_context *ctx, const SliceOp<Src> &a, const SliceOp<Src> *b, int K, int Kp, int batch)
 {
-    dim3 grid((R + SL_ROWS - 1) / SL_ROWS, batch);
-    if (rcontig)
-        tc_slice_kernel<Src, true, S><<<grid, 256, 0, ctx->stream>>>(R, K, X, ld, sX, conj, role_b, Kp, planes, exps);
-    else
-        tc_slice_kernel<Src, false, S><<<grid, 256, 0, ctx->stream>>>(R, K, X, ld, sX, conj, role_b, Kp, planes, exps);
+    const int rmax = b && b->R > a.R ? b->R : a.R;
+    dim3 grid((rmax + SL_ROWS - 1) / SL_ROWS, batch, b ? 2 : 1);
+    tc_slice_kernel<Src, S><<<grid, 256, 0, ctx->stream>>>(a, b ? *b : a, K, Kp);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
 
+// the operand descriptor and plane allocation of one operand
 template <class Src>
-int slice_any(ia_context *ctx, bool role_b, Op op, const Src *X, int ld, long long sX, int R, int K, int S, int batch,
-              TcPlanes &out, WsCursor &cur)
+int slice_prepare(bool role_b, Op op, const Src *X, int ld, long long sX, int R, int K, int S, int batch,
+                  TcPlanes &out, WsCursor &cur, SliceOp<Src> &d)
 {
     if (R < 1 || K < 1 || batch < 1 || S < TC_SLICES_MIN || S > TC_SLICES_MAX) return IA_ERR_ARG;
     const int Kp = (2 * K + 7) & ~7;
@@ -444,13 +457,29 @@ int slice_any(ia_context *ctx, bool role_b, Op op, const Src *X, int ld, long lo
     out.e = cur.take<int>((size_t)batch * R);
     if (cur.off > cur.cap) return IA_ERR_ALLOC;
     // view V(r, k): the A role reads rows of op(A), the B role columns of op(B)
-    const bool rcontig = role_b ? op != OP_N : op == OP_N;
-    const bool conj = op == OP_C;
+    d = SliceOp<Src>{X, ld, sX, R, op == OP_C ? 1 : 0, role_b ? 1 : 0, (role_b ? op != OP_N : op == OP_N) ? 1 : 0,
+                     out.p, out.e};
+    return IA_OK;
+}
+
+template <class Src>
+int slice_dispatch(ia_context *ctx, int S, const SliceOp<Src> &a, const SliceOp<Src> *b, int K, int Kp, int batch)
+{
     switch (S) {
-    case 6: return slice_launch<Src, 6>(ctx, rcontig, conj, role_b, X, ld, sX, R, K, Kp, batch, out.p, out.e);
-    case 7: return slice_launch<Src, 7>(ctx, rcontig, conj, role_b, X, ld, sX, R, K, Kp, batch, out.p, out.e);
-    default: return slice_launch<Src, 8>(ctx, rcontig, conj, role_b, X, ld, sX, R, K, Kp, batch, out.p, out.e);
+    case 6: return slice_launch<Src, 6>(ctx, a, b, K, Kp, batch);
+    case 7: return slice_launch<Src, 7>(ctx, a, b, K, Kp, batch);
+    default: return slice_launch<Src, 8>(ctx, a, b, K, Kp, batch);
     }
+}
+
+template <class Src>
+int slice_any(ia_context *ctx, bool role_b, Op op, const Src *X, int ld, long long sX, int R, int K, int S, int batch,
+              TcPlanes &out, WsCursor &cur)
+{
+    SliceOp<Src> d;
+    const int st = slice_prepare<Src>(role_b, op, X, ld, sX, R, K, S, batch, out, cur, d);
+    if (st) return st;
+    return slice_dispatch<Src>(ctx, S, d, nullptr, K, out.Kp, batch);
 }
 
 }  // namespace
@@ -471,6 +500,16 @@ int tc_slice(ia_context *ctx, bool role_b, Op op, const float4 *X, int ld, long 
              int batch, TcPlanes &out, WsCursor &cur)
 {
     return slice_any<float4>(ctx, role_b, op, X, ld, sX, R, K, S, batch, out, cur);
+}
+
+int tc_slice_pair(ia_context *ctx, Op opa, const double2 *A, int lda, long long sA, int M, Op opb, const double2 *B,
+                  int ldb, long long sB, int N, int K, int S, int batch, TcPlanes &pa, TcPlanes &pb, WsCursor &cur)
+{
+    SliceOp<double2> da, db;
+    int st = slice_prepare<double2>(false, opa, A, lda, sA, M, K, S, batch, pa, cur, da);
+    if (!st) st = slice_prepare<double2>(true, opb, B, ldb, sB, N, K, S, batch, pb, cur, db);
+    if (st) return st;
+    return slice_dispatch<double2>(ctx, S, da, &db, K, pa.Kp, batch);
 }
 
 int tc_gemm(ia_context *ctx, const TcPlanes &A, const TcPlanes &B, int M, int N, double alpha, double beta,

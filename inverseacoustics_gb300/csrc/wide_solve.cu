@@ -868,8 +868,7 @@ struct EigGemm {
             return dfgemm_batched(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
         WsCursor cur{ws, 0, bytes};
         TcPlanes Pa{}, Pb{};
-        int st = tc_slice(ctx, false, opa, A, lda, sA, M, K, EIG_SLICES, batch, Pa, cur);
-        if (!st) st = tc_slice(ctx, true, opb, B, ldb, sB, N, K, EIG_SLICES, batch, Pb, cur);
+        int st = tc_slice_pair(ctx, opa, A, lda, sA, M, opb, B, ldb, sB, N, K, EIG_SLICES, batch, Pa, Pb, cur);
         if (!st) st = tc_gemm(ctx, Pa, Pb, M, N, alpha, beta, C, ldc, sC, batch, info);
         return st;
     }
