@@ -22,10 +22,13 @@
 //
 // Both replace the reference's csvd + gcvG + tikhonovG / tsvd chain
 // (CUDA/tsvd.cuh:10-172, MATLAB/regtools) for the batched path.
+#include <cooperative_groups.h>
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
 namespace ia {
+
+namespace cg = cooperative_groups;
 
 constexpr int QR_THREADS = 512;
 
@@ -217,12 +220,276 @@ constexpr int QR_KPL = 24;
 
 // perm (batch x cols, may be null): column pivoting, perm[k] = the input
 // column that ends in position k
+// ---- column-pivoted QR of one FP32 matrix over a cluster of QRC_CS CTAs ---
+// The single-CTA kernel above is a chain of `cols` latency-bound reflector
+// steps on one SM.  Here CTA r of a bin's cluster owns columns [r cw, (r+1) cw)
+// in its shared memory; per step the owner of column j forms the reflector
+// and every CTA applies it to its own columns, so four SMs share the trailing
+// updates.  Per step, through distributed shared memory: each CTA's pivot
+// candidate (largest remaining norm, first on ties) is read by all, which
+// take the same decision; a pivot in another CTA is swapped in by copying the
+// two columns across; the reflector is copied from its owner.  Three cluster
+// barriers per step (two without a swap).  The arithmetic per column is the
+// single-CTA kernel's (warp per column, the same reductions), except the
+// reflector's norm, a reduction over the owner's threads.  Mixed path only
+// (FP32, pivoted, no right-hand sides); tau may be null.
+constexpr int QRC_CS = 4;
+constexpr int QRC_THREADS = 512;
+
+__global__ void __launch_bounds__(QRC_THREADS) qr_cluster_kernel(int rows, int cols, float2 *A, int lda, long long sA,
+                                                                 float2 *tau, int *perm)
+{
+    typedef float R;
+    constexpr int KPL = QR_KPL;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int f = blockIdx.x / QRC_CS;
+    const int cw = (cols + QRC_CS - 1) / QRC_CS;
+    const int c0 = rank * cw, c1 = c0 + cw < cols ? c0 + cw : cols, nown = c1 > c0 ? c1 - c0 : 0;
+    extern __shared__ __align__(16) unsigned char qrc_smem[];
+    float2 *colbuf = reinterpret_cast<float2 *>(qrc_smem);      // nown columns of `rows`
+    float2 *xs = colbuf + (size_t)cw * rows;                      // the current reflector (rows)
+    float2 *tmp = xs + rows;                                      // a column arriving by a swap (rows)
+    R *cn = reinterpret_cast<R *>(tmp + rows);                    // norms^2 of the owned columns' remaining rows
+    int *idx = reinterpret_cast<int *>(cn + cw);                  // original index of each owned column
+    __shared__ R red[QRC_THREADS / 32];
+    __shared__ R cand_v;
+    __shared__ int cand_i;
+    __shared__ float2 s_tau;
+    __shared__ float2 s_scale;
+    __shared__ R s_swap_cn;
+    __shared__ int s_swap_idx;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = QRC_THREADS / 32;
+    const float2 zero = make_float2(0.f, 0.f);
+    A += f * sA;
+    for (int e = tid; e < nown * rows; e += QRC_THREADS) {
+        const int c = e / rows, i = e % rows;
+        colbuf[e] = A[i + (size_t)(c0 + c) * lda];
+    }
+    __syncthreads();
+    for (int c = wid; c < nown; c += nw) {
+        R a = 0;
+        for (int i = lane; i < rows; i += 32) a += zabs2(colbuf[i + (size_t)c * rows]);
+        a = warp_sum(a);
+        if (lane == 0) {
+            cn[c] = a;
+            idx[c] = c0 + c;
+        }
+    }
+    __syncthreads();
+    const int steps = cols < rows ? cols : rows;
+    for (int j = 0; j < steps; ++j) {
+        // pivot: this CTA's candidate among its columns >= j, then the cluster's
+        if (wid == 0) {
+            R best = -1;
+            int bi = cols;
+            for (int c = lane; c < nown; c += 32)
+                if (c0 + c >= j && cn[c] > best) {
+                    best = cn[c];
+                    bi = c0 + c;
+                }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > best || (ov == best && oi < bi)) {
+                    best = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                cand_v = best;
+                cand_i = bi;
+            }
+        }
+        cluster.sync();
+        R pv = -1;
+        int p = cols;
+        for (int q = 0; q < QRC_CS; ++q) {
+            const R v = *cluster.map_shared_rank(&cand_v, q);
+            const int i = *cluster.map_shared_rank(&cand_i, q);
+            if (v > pv || (v == pv && i < p)) {
+                pv = v;
+                p = i;
+            }
+        }
+        const int oj = j / cw, op = p / cw;
+        if (p != j) {
+            if (oj == op) {
+                if (rank == oj) {
+                    float2 *a = colbuf + (size_t)(j - c0) * rows, *b = colbuf + (size_t)(p - c0) * rows;
+                    for (int i = tid; i < rows; i += QRC_THREADS) {
+                        const float2 t = a[i];
+                        a[i] = b[i];
+                        b[i] = t;
+                    }
+                    if (tid == 0) {
+                        const R tn = cn[j - c0];
+                        cn[j - c0] = cn[p - c0];
+                        cn[p - c0] = tn;
+                        const int ti = idx[j - c0];
+                        idx[j - c0] = idx[p - c0];
+                        idx[p - c0] = ti;
+                    }
+                }
+            } else {
+                // each of the two owners copies the other's column in, then
+                // (after the barrier) over its own
+                if (rank == oj || rank == op) {
+                    const int mine = rank == oj ? j : p, other = rank == oj ? p : j;
+                    const int orank = rank == oj ? op : oj;
+                    const float2 *src = cluster.map_shared_rank(colbuf, orank) + (size_t)(other - orank * cw) * rows;
+                    for (int i = tid; i < rows; i += QRC_THREADS) tmp[i] = src[i];
+                    if (tid == 0) {
+                        s_swap_cn = *cluster.map_shared_rank(cn + (other - orank * cw), orank);
+                        s_swap_idx = *cluster.map_shared_rank(idx + (other - orank * cw), orank);
+                    }
+                    (void)mine;
+                }
+                cluster.sync();
+                if (rank == oj || rank == op) {
+                    const int mine = rank == oj ? j : p;
+                    float2 *dst = colbuf + (size_t)(mine - c0) * rows;
+                    for (int i = tid; i < rows; i += QRC_THREADS) dst[i] = tmp[i];
+                    if (tid == 0) {
+                        cn[mine - c0] = s_swap_cn;
+                        idx[mine - c0] = s_swap_idx;
+                    }
+                }
+            }
+        }
+        // the reflector of column j, by its owner
+        if (rank == oj) {
+            __syncthreads();
+            float2 *x = colbuf + (size_t)(j - c0) * rows + j;
+            const int len = rows - j;
+            R sg = 0;
+            for (int i = 1 + tid; i < len; i += QRC_THREADS) sg += zabs2(x[i]);
+            sg = warp_sum(sg);
+            if (lane == 0) red[wid] = sg;
+            __syncthreads();
+            if (tid == 0) {
+                R sigma = 0;
+                for (int w = 0; w < nw; ++w) sigma += red[w];
+                const float2 alpha = x[0];
+                if (sigma == 0 && alpha.y == 0) {
+                    s_tau = zero;
+                    s_scale = zero;
+                } else {
+                    const R nrm = sqrtf(zabs2(alpha) + sigma);
+                    const R beta = alpha.x >= 0 ? -nrm : nrm;
+                    s_tau = make_float2((beta - alpha.x) / beta, -alpha.y / beta);
+                    s_scale = zdiv(make_float2(1.f, 0.f), make_float2(alpha.x - beta, alpha.y));
+                    x[0] = make_float2(beta, 0.f);
+                }
+                if (tau) tau[(size_t)f * cols + j] = s_tau;
+            }
+            __syncthreads();
+            const float2 sc = s_scale;
+            const bool none = s_tau.x == 0 && s_tau.y == 0;
+            for (int i = 1 + tid; i < len; i += QRC_THREADS) {
+                const float2 v = none ? x[i] : zmul(x[i], sc);
+                if (!none) x[i] = v;
+                xs[j + i] = v;
+            }
+        }
+        cluster.sync();
+        // every CTA: the reflector (and tau) from the owner, then its columns > j
+        float2 tv;
+        {
+            const float2 *oxs = cluster.map_shared_rank(xs, oj);
+            if (rank != oj)
+                for (int i = j + 1 + tid; i < rows; i += QRC_THREADS) xs[i] = oxs[i];
+            tv = *cluster.map_shared_rank(&s_tau, oj);
+        }
+        __syncthreads();
+        const int len = rows - j;
+        const bool none = tv.x == 0 && tv.y == 0;
+        const float2 ctau = zconj(tv);
+        for (int c = wid; c < nown; c += nw) {
+            if (c0 + c <= j) continue;
+            float2 *col = colbuf + (size_t)c * rows + j;
+            if (none) {
+                // no reflector: the norm loses its row j
+                if (lane == 0) {
+                    const R v = cn[c] - zabs2(col[0]);
+                    cn[c] = v > 0 ? v : 0;
+                }
+                continue;
+            }
+            float2 w = lane == 0 ? col[0] : zero;
+            float2 v[KPL];
+#pragma unroll
+            for (int t = 0; t < KPL; ++t) {
+                const int i = 1 + lane + 32 * t;
+                v[t] = i < len ? col[i] : zero;
+            }
+#pragma unroll
+            for (int t = 0; t < KPL; ++t) {
+                const int i = 1 + lane + 32 * t;
+                if (i < len) zcfma(w, xs[j + i], v[t]);
+            }
+            w = warp_sum2(w);
+            w = zmul(ctau, w);
+            if (lane == 0) col[0] = zsub(col[0], w);
+            R nr = 0;
+#pragma unroll
+            for (int t = 0; t < KPL; ++t) {
+                const int i = 1 + lane + 32 * t;
+                if (i < len) {
+                    zfms(v[t], xs[j + i], w);
+                    col[i] = v[t];
+                    nr += zabs2(v[t]);
+                }
+            }
+            nr = warp_sum(nr);
+            if (lane == 0) cn[c] = nr;
+        }
+        __syncthreads();
+    }
+    cluster.sync();   // no CTA leaves while another may still read its shared memory
+    for (int e = tid; e < nown * rows; e += QRC_THREADS) {
+        const int c = e / rows, i = e % rows;
+        A[i + (size_t)(c0 + c) * lda] = colbuf[e];
+    }
+    if (perm)
+        for (int c = tid; c < nown; c += QRC_THREADS) perm[(size_t)f * cols + c0 + c] = idx[c];
+}
+
+static size_t qr_cluster_smem(int rows, int cols)
+{
+    const int cw = (cols + QRC_CS - 1) / QRC_CS;
+    return sizeof(float2) * ((size_t)cw * rows + 2 * (size_t)rows) + (sizeof(float) + sizeof(int)) * (size_t)cw;
+}
+
 template <class T, bool PIV>
 static int qr_launch_t(ia_context *ctx, int rows, int cols, T *A, int lda, long long sA, T *tau, int nrhs, T *B,
                        int ldb, long long sB, int batch, int *perm)
 {
     typedef typename ctraits<T>::R R;
     const size_t piv = PIV ? (sizeof(R) + sizeof(int)) * (size_t)cols : 0;
+    if constexpr (std::is_same<T, float2>::value && PIV) {
+        const size_t csm = qr_cluster_smem(rows, cols);
+        if (!B && rows <= 1 + 32 * QR_KPL && cols >= 2 * QRC_CS && csm <= 227 * 1024) {
+            IA_CUDA_TRY(cudaFuncSetAttribute(qr_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3((unsigned)(QRC_CS * batch));
+            lc.blockDim = dim3(QRC_THREADS);
+            lc.dynamicSmemBytes = csm;
+            lc.stream = ctx->stream;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = QRC_CS;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            lc.attrs = at;
+            lc.numAttrs = 1;
+            IA_CUDA_TRY(cudaLaunchKernelEx(&lc, qr_cluster_kernel, rows, cols, (float2 *)A, lda, sA, (float2 *)tau,
+                                           perm));
+            IA_LAUNCH_CHECK(ctx);
+            return IA_OK;
+        }
+    }
     if (rows <= 1 + 32 * QR_KPL) {
         const size_t smem = sizeof(T) * (size_t)rows + piv;
         if (smem > 48 * 1024) {
