@@ -493,30 +493,72 @@ int backsolve_upper_batched(ia_context *ctx, int n, int nrhs, const T *LU, int l
 
 // Fused LU solve (FP32 complex): the row interchanges, the unit-lower L solve
 // and the upper U solve for GETRS_RB right-hand-side columns of one matrix per
-// CTA, in one launch, the n x GETRS_RB block of B in shared memory.  Block
-// steps of LU_NB rows: the diagonal block is staged in shared memory and
-// solved warp per column (lane per row, each solved entry broadcast by
-// shuffle); the rows below (forward) or above (backward) are then updated
-// thread per row, the block's LU_NB columns of L or U read coalesced from
-// global memory (L2).  Replaces 2 n / LU_NB dependent small launches (a
+// CTA, in one launch, the n x GETRS_RB block of B in shared memory (columns of
+// even stride, so two consecutive entries load as one 16-byte word).  Block
+// steps of LU_NB rows: the diagonal block is staged in shared memory, zero
+// outside the block (a partial last block needs no masks), with the
+// reciprocals of U's diagonal computed in parallel; it is solved warp per
+// column, lane per row, each solved entry broadcast by shuffle, branch-free
+// (a select per step in place of the lane tests and the division).  The rows
+// below (forward) or above (backward) are then updated thread per row, the
+// block's LU_NB entries of the row of L or U loaded together from global
+// memory (L2), the solved entries read in pairs.  Full blocks run without
+// per-entry predicates.  Replaces 2 n / LU_NB dependent small launches (a
 // diagonal-block solve and a GEMM update per step) by one.
-// right-hand sides per CTA: a warp per column in the diagonal solves
 
 __device__ __forceinline__ float2 shfl_c(float2 v, int src)
 {
     return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
+// X rows [lo, hi) -= T(:, 0:nb) X(k0:k0+nb, :), thread per row (T: the L or
+// U block column, leading dimension lda, starting at row 0 of the matrix)
+template <int RB, int NT, bool FULL>
+__device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int lda, float2 *X, int xs, int k0,
+                                             int nb, int lo, int hi)
+{
+    constexpr int TH = LU_NB / 2;   // the row's entries in two halves (register budget: two CTAs per SM)
+    for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
+        const float2 *tp = T + i;
+        float2 acc[RB];
+#pragma unroll
+        for (int c = 0; c < RB; ++c) acc[c] = X[i + (size_t)c * xs];
+#pragma unroll
+        for (int h = 0; h < LU_NB; h += TH) {
+            float2 trow[TH];
+#pragma unroll
+            for (int t = 0; t < TH; ++t)
+                trow[t] = (FULL || h + t < nb) ? tp[(size_t)(h + t) * lda] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < TH; t += 2) {
+                if (FULL || h + t < nb) {
+#pragma unroll
+                    for (int c = 0; c < RB; ++c) {
+                        // X(k0 + h + t, c) and the entry below: k0, h, t and xs even
+                        const float4 x2 = *reinterpret_cast<const float4 *>(X + k0 + h + t + (size_t)c * xs);
+                        zfms(acc[c], trow[t], make_float2(x2.x, x2.y));
+                        zfms(acc[c], trow[t + 1], make_float2(x2.z, x2.w));
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < RB; ++c) X[i + (size_t)c * xs] = acc[c];
+    }
+}
+
 template <int GETRS_RB, int NT>
-__global__ void __launch_bounds__(NT) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
+__global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, const float2 *__restrict__ LU,
                                                                      int lda, long long sA,
                                                                      const int *__restrict__ ipiv, float2 *B, int ldb,
                                                                      long long sB)
 {
     extern __shared__ __align__(16) unsigned char gf_smem[];
-    float2 *X = reinterpret_cast<float2 *>(gf_smem);                                  // n x GETRS_RB
-    float2(*D)[LU_NB + 1] = reinterpret_cast<float2(*)[LU_NB + 1]>(X + (size_t)n * GETRS_RB);
-    int *piv = reinterpret_cast<int *>(D + LU_NB);                                    // n
+    const int xs = (n + 1) & ~1;
+    float2 *X = reinterpret_cast<float2 *>(gf_smem);                                  // xs x GETRS_RB
+    float2(*D)[LU_NB + 1] = reinterpret_cast<float2(*)[LU_NB + 1]>(X + (size_t)xs * GETRS_RB);
+    float2 *Dinv = reinterpret_cast<float2 *>(D + LU_NB);                              // LU_NB
+    int *piv = reinterpret_cast<int *>(Dinv + LU_NB);                                  // n
     const int f = blockIdx.y, c0 = blockIdx.x * GETRS_RB;
     const int nc = nrhs - c0 < GETRS_RB ? nrhs - c0 : GETRS_RB;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -524,14 +566,14 @@ __global__ void __launch_bounds__(NT) getrs_fused_kernel(int n, int nrhs, const 
     ipiv += (size_t)f * n;
     B += f * sB + (size_t)c0 * ldb;
     const float2 zero = make_float2(0.f, 0.f);
-    for (int e = tid; e < n * GETRS_RB; e += blockDim.x) {
-        const int i = e % n, c = e / n;
-        X[e] = c < nc ? B[i + (size_t)c * ldb] : zero;
+    for (int e = tid; e < xs * GETRS_RB; e += NT) {
+        const int i = e % xs, c = e / xs;
+        X[e] = c < nc && i < n ? B[i + (size_t)c * ldb] : zero;
     }
-    for (int j = tid; j < n; j += blockDim.x) piv[j] = ipiv[j];
+    for (int j = tid; j < n; j += NT) piv[j] = ipiv[j];
     __syncthreads();
     if (tid < GETRS_RB) {
-        float2 *x = X + (size_t)tid * n;
+        float2 *x = X + (size_t)tid * xs;
         for (int j = 0; j < n; ++j) {
             const int p = piv[j];
             if (p != j) {
@@ -545,89 +587,68 @@ __global__ void __launch_bounds__(NT) getrs_fused_kernel(int n, int nrhs, const 
     // forward: L Y = P B
     for (int k0 = 0; k0 < n; k0 += LU_NB) {
         const int nb = n - k0 < LU_NB ? n - k0 : LU_NB, kend = k0 + nb;
-        for (int e = tid; e < nb * nb; e += blockDim.x) {
-            const int r = e % nb, cc = e / nb;
-            D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
+        for (int e = tid; e < LU_NB * LU_NB; e += NT) {
+            const int r = e % LU_NB, cc = e / LU_NB;
+            D[r][cc] = r < nb && cc < nb ? LU[k0 + r + (size_t)(k0 + cc) * lda] : zero;
         }
         __syncthreads();
         if (wid < GETRS_RB) {
-            float2 *x = X + (size_t)wid * n + k0;
+            // lanes >= nb hold zero and, with D zero there, stay zero
+            float2 *x = X + (size_t)wid * xs + k0;
             float2 v = lane < nb ? x[lane] : zero;
-            for (int r = 0; r < nb; ++r) {
+#pragma unroll
+            for (int r = 0; r < LU_NB; ++r) {
                 const float2 xr = shfl_c(v, r);
-                if (lane > r && lane < nb) zfms(v, D[lane][r], xr);
+                const float2 d = lane > r ? D[lane][r] : zero;
+                zfms(v, d, xr);
             }
             if (lane < nb) x[lane] = v;
         }
         __syncthreads();
-        for (int i = kend + tid; i < n; i += blockDim.x) {
-            // the row's LU_NB entries of L first, all loads in flight at once
-            // (one L2 round trip per row instead of one per entry)
-            float2 lrow[LU_NB];
-#pragma unroll
-            for (int t = 0; t < LU_NB; ++t) lrow[t] = t < nb ? LU[i + (size_t)(k0 + t) * lda] : zero;
-            float2 acc[GETRS_RB];
-#pragma unroll
-            for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
-#pragma unroll
-            for (int t = 0; t < LU_NB; ++t) {
-                if (t < nb) {
-#pragma unroll
-                    for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], lrow[t], X[k0 + t + (size_t)c * n]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];
-        }
+        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, kend, n);
+        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, kend, n);
         __syncthreads();
     }
     // backward: U X = Y
     for (int k0 = ((n - 1) / LU_NB) * LU_NB; k0 >= 0; k0 -= LU_NB) {
         const int nb = n - k0 < LU_NB ? n - k0 : LU_NB;
-        for (int e = tid; e < nb * nb; e += blockDim.x) {
-            const int r = e % nb, cc = e / nb;
-            D[r][cc] = LU[k0 + r + (size_t)(k0 + cc) * lda];
+        for (int e = tid; e < LU_NB * LU_NB; e += NT) {
+            const int r = e % LU_NB, cc = e / LU_NB;
+            D[r][cc] = r < nb && cc < nb ? LU[k0 + r + (size_t)(k0 + cc) * lda] : zero;
+        }
+        if (tid < LU_NB) {
+            const float2 d = tid < nb ? LU[k0 + tid + (size_t)(k0 + tid) * lda] : zero;
+            Dinv[tid] = tid < nb ? zdiv(make_float2(1.f, 0.f), d) : zero;
         }
         __syncthreads();
         if (wid < GETRS_RB) {
-            float2 *x = X + (size_t)wid * n + k0;
+            float2 *x = X + (size_t)wid * xs + k0;
             float2 v = lane < nb ? x[lane] : zero;
-            for (int r = nb - 1; r >= 0; --r) {
-                if (lane == r) v = zdiv(v, D[r][r]);
+#pragma unroll
+            for (int r = LU_NB - 1; r >= 0; --r) {
+                const float2 sv = zmul(v, Dinv[r]);
+                v = lane == r ? sv : v;
                 const float2 xr = shfl_c(v, r);
-                if (lane < r) zfms(v, D[lane][r], xr);
+                const float2 d = lane < r ? D[lane][r] : zero;
+                zfms(v, d, xr);
             }
             if (lane < nb) x[lane] = v;
         }
         __syncthreads();
-        for (int i = tid; i < k0; i += blockDim.x) {
-            float2 urow[LU_NB];
-#pragma unroll
-            for (int t = 0; t < LU_NB; ++t) urow[t] = t < nb ? LU[i + (size_t)(k0 + t) * lda] : zero;
-            float2 acc[GETRS_RB];
-#pragma unroll
-            for (int c = 0; c < GETRS_RB; ++c) acc[c] = X[i + (size_t)c * n];
-#pragma unroll
-            for (int t = 0; t < LU_NB; ++t) {
-                if (t < nb) {
-#pragma unroll
-                    for (int c = 0; c < GETRS_RB; ++c) zfms(acc[c], urow[t], X[k0 + t + (size_t)c * n]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < GETRS_RB; ++c) X[i + (size_t)c * n] = acc[c];
-        }
+        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, 0, k0);
+        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, 0, k0);
         __syncthreads();
     }
-    for (int e = tid; e < n * nc; e += blockDim.x) {
+    for (int e = tid; e < n * nc; e += NT) {
         const int i = e % n, c = e / n;
-        B[i + (size_t)c * ldb] = X[e];
+        B[i + (size_t)c * ldb] = X[i + (size_t)c * xs];
     }
 }
 
 static size_t getrs_fused_smem(int n, int GETRS_RB)
 {
-    return sizeof(float2) * ((size_t)n * GETRS_RB + (size_t)LU_NB * (LU_NB + 1)) + sizeof(int) * (size_t)n;
+    const size_t xs = (size_t)((n + 1) & ~1);
+    return sizeof(float2) * (xs * GETRS_RB + (size_t)LU_NB * (LU_NB + 1) + LU_NB) + sizeof(int) * (size_t)n;
 }
 
 template <class T>

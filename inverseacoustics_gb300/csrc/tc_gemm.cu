@@ -235,6 +235,131 @@ __global__ void __launch_bounds__(256) tc_slice_kernel(SliceOp<Src> op0, SliceOp
     }
 }
 
+// Single-pass form: SL1_RB rows of the view per CTA, their K values read from
+// global memory once into a shared-memory strip; warp w then takes row w: the
+// row maximum from the strip, then the digits of two complex values per lane
+// (8-byte plane stores, 256 bytes per warp and plane).  The same digits and
+// exponents as the two-pass kernel above, which re-reads the operand for the
+// digits (from DRAM once the operand outgrows L2); that kernel remains for
+// rows longer than the strip allows.
+constexpr int SL1_RB = 8, SL1_THREADS = 256, SL1_UNROLL = 4;
+
+__host__ __device__ constexpr int sl1_stride(int Kh) { return Kh + 1; }   // odd in 16-byte units: no bank conflicts
+
+__device__ __forceinline__ unsigned bf2_bits(__nv_bfloat162 v)
+{
+    return (unsigned)__bfloat16_as_ushort(v.x) | ((unsigned)__bfloat16_as_ushort(v.y) << 16);
+}
+
+template <class Src, int S>
+__global__ void __launch_bounds__(SL1_THREADS, 2) tc_slice1_kernel(SliceOp<Src> op0, SliceOp<Src> op1, int K, int Kp)
+{
+    extern __shared__ __align__(16) unsigned char sl1_smem[];
+    Src *strip = reinterpret_cast<Src *>(sl1_smem);   // SL1_RB rows x sl1_stride(Kh)
+    const SliceOp<Src> &op = blockIdx.z ? op1 : op0;
+    const int f = blockIdx.y, r0 = blockIdx.x * SL1_RB, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int R = op.R;
+    if (r0 >= R) return;   // the other operand's taller grid
+    const int Kh = Kp >> 1, ks = sl1_stride(Kh);
+    const int nr = R - r0 < SL1_RB ? R - r0 : SL1_RB;
+    const Src *__restrict__ X = op.X + f * op.sX;
+    const bool conj = op.conj != 0;
+    if (op.rcontig) {
+        // V(r, k) = X[r + k ld]: the CTA's rows of one k are 8 contiguous
+        // values; a warp covers 4 values of k per step
+        const int r = lane & (SL1_RB - 1), kq = lane >> 3;
+        for (int kb = 4 * w; kb < Kh; kb += 4 * (SL1_THREADS / 32) * SL1_UNROLL) {
+            Src v[SL1_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SL1_UNROLL; ++u) {
+                const int k = kb + kq + 4 * (SL1_THREADS / 32) * u;
+                v[u] = Src{};
+                if (r < nr && k < K) v[u] = load_conj(X, (size_t)(r0 + r) + (size_t)k * op.ld, conj);
+            }
+#pragma unroll
+            for (int u = 0; u < SL1_UNROLL; ++u) {
+                const int k = kb + kq + 4 * (SL1_THREADS / 32) * u;
+                if (k < Kh) strip[(size_t)r * ks + k] = v[u];
+            }
+        }
+    } else {
+        // V(r, k) = X[k + r ld]: a row is contiguous; warp w loads row w
+        const Src *xr = X + (size_t)(r0 + w) * op.ld;
+        for (int kb = lane; kb < Kh; kb += 32 * SL1_UNROLL) {
+            Src v[SL1_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SL1_UNROLL; ++u) {
+                const int k = kb + 32 * u;
+                v[u] = Src{};
+                if (w < nr && k < K) v[u] = load_conj(xr, (size_t)k, conj);
+            }
+#pragma unroll
+            for (int u = 0; u < SL1_UNROLL; ++u) {
+                const int k = kb + 32 * u;
+                if (k < Kh) strip[(size_t)w * ks + k] = v[u];
+            }
+        }
+    }
+    __syncthreads();
+    if (w >= nr) return;
+    const Src *srow = strip + (size_t)w * ks;
+    unsigned long long key = 0;
+    for (int k = lane; k < K; k += 32) {
+        const unsigned long long kk = abs_key(srow[k]);
+        key = kk > key ? kk : key;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+        key = ok > key ? ok : key;
+    }
+    const int e = key_exponent(key, (const Src *)nullptr);
+    const int row = r0 + w;
+    if (lane == 0) op.exps[(size_t)f * R + row] = e;
+    const int q = 5 - e + 6 * (S - 1);
+    const int rows = op.role_b ? 2 * R : R;
+    const size_t pstride = (size_t)rows * Kp;
+    __nv_bfloat16 *__restrict__ planes = op.planes + (size_t)f * S * pstride;
+    for (int k = 2 * lane; k < Kh; k += 64) {
+        // two complex values (k, k + 1); Kh is a multiple of 4
+        long long x[4];
+        to_fixed(srow[k], q, x[0], x[1]);
+        to_fixed(srow[k + 1], q, x[2], x[3]);
+        // digits least significant first (digits64's order), each plane
+        // written as soon as its four digits exist
+#pragma unroll
+        for (int s = S - 1; s >= 0; --s) {
+            int d[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (s > 0) {
+                    int r = (int)(x[j] & 63);
+                    if (r > 32) r -= 64;
+                    d[j] = r;
+                    x[j] = (x[j] - r) >> 6;
+                } else {
+                    d[j] = (int)x[j];
+                }
+            }
+            __nv_bfloat16 *P = planes + (size_t)s * pstride + 2 * (size_t)k;
+            if (!op.role_b) {
+                uint2 u;
+                u.x = bf2_bits(bf2(d[0], d[1]));
+                u.y = bf2_bits(bf2(d[2], d[3]));
+                *reinterpret_cast<uint2 *>(P + (size_t)row * Kp) = u;
+            } else {
+                uint2 u0, u1;
+                u0.x = bf2_bits(bf2(d[0], -d[1]));
+                u0.y = bf2_bits(bf2(d[2], -d[3]));
+                u1.x = bf2_bits(bf2(d[1], d[0]));
+                u1.y = bf2_bits(bf2(d[3], d[2]));
+                *reinterpret_cast<uint2 *>(P + (size_t)(2 * row) * Kp) = u0;
+                *reinterpret_cast<uint2 *>(P + (size_t)(2 * row + 1) * Kp) = u1;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the tensor-core GEMM on slice planes
 // ---------------------------------------------------------------------------
@@ -434,6 +559,16 @@ template <class Src, int S>
 int slice_launch(ia_context *ctx, const SliceOp<Src> &a, const SliceOp<Src> *b, int K, int Kp, int batch)
 {
     const int rmax = b && b->R > a.R ? b->R : a.R;
+    const size_t smem1 = sizeof(Src) * SL1_RB * (size_t)sl1_stride(Kp >> 1);
+    if (smem1 <= 200 * 1024) {
+        if (smem1 > 48 * 1024)
+            IA_CUDA_TRY(cudaFuncSetAttribute(tc_slice1_kernel<Src, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem1));
+        dim3 grid((rmax + SL1_RB - 1) / SL1_RB, batch, b ? 2 : 1);
+        tc_slice1_kernel<Src, S><<<grid, SL1_THREADS, smem1, ctx->stream>>>(a, b ? *b : a, K, Kp);
+        IA_LAUNCH_CHECK(ctx);
+        return IA_OK;
+    }
     dim3 grid((rmax + SL_ROWS - 1) / SL_ROWS, batch, b ? 2 : 1);
     tc_slice_kernel<Src, S><<<grid, 256, 0, ctx->stream>>>(a, b ? *b : a, K, Kp);
     IA_LAUNCH_CHECK(ctx);

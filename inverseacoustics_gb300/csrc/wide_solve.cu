@@ -469,8 +469,14 @@ static int qr_launch_t(ia_context *ctx, int rows, int cols, T *A, int lda, long 
     typedef typename ctraits<T>::R R;
     const size_t piv = PIV ? (sizeof(R) + sizeof(int)) * (size_t)cols : 0;
     if constexpr (std::is_same<T, float2>::value && PIV) {
+        // the cluster form shortens one bin's chain but holds four SMs for
+        // ~60 % of the one-CTA form's time (2.3x its SM time): only for
+        // batches that leave most of the GPU idle (at most a quarter of the
+        // SMs in clusters; a 16-bin part of the 64-bin pass takes the one-CTA
+        // form)
         const size_t csm = qr_cluster_smem(rows, cols);
-        if (!B && rows <= 1 + 32 * QR_KPL && cols >= 2 * QRC_CS && csm <= 227 * 1024) {
+        if (!B && rows <= 1 + 32 * QR_KPL && cols >= 2 * QRC_CS && csm <= 227 * 1024 &&
+            4 * QRC_CS * batch <= ctx->sm_count) {
             IA_CUDA_TRY(cudaFuncSetAttribute(qr_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
             cudaLaunchConfig_t lc = {};
             lc.gridDim = dim3((unsigned)(QRC_CS * batch));
