@@ -551,9 +551,20 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
         up((void **)&M->d_gptr, gptr.data(), sizeof(int) * gptr.size());
         up((void **)&M->d_gidx, gidx.data(), sizeof(int) * gidx.size());
     }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&M->d_creg, sizeof(double) * (size_t)m);
     if (e != cudaSuccess) {
         ia_mesh_destroy(M);
         return cuda_status(e);
+    }
+    // complete before any stream of the context reads it
+    int st = mesh_creg(ctx, M);
+    if (!st) {
+        const cudaError_t ce = cudaStreamSynchronize(ctx->stream);
+        if (ce != cudaSuccess) st = cuda_status(ce);
+    }
+    if (st) {
+        ia_mesh_destroy(M);
+        return st;
     }
     *out = M;
     return IA_OK;
@@ -577,6 +588,7 @@ int ia_mesh_destroy(ia_mesh *M)
     cudaFree(M->d_qdat_f);
     cudaFree(M->d_qnrm_f);
     cudaFree(M->d_dftab);
+    cudaFree(M->d_creg);
     free(M);
     return IA_OK;
 }

@@ -55,6 +55,7 @@ struct ia_mesh {
     float *d_qdat_f;       // d_qdat as double-float (hi, lo) pairs
     float *d_qnrm_f;       // d_qnrm as double-float (hi, lo) pairs
     float4 *d_dftab;       // 1024 x (sin hi, sin lo, cos hi, cos lo)(j pi / 512) for the double-float assembly
+    double *d_creg;        // m: the regular elements' C term per node (FP64), for the double-float assembly
     int *d_gptr, *d_gidx;  // node-node pattern, CSR (m + 1, gnnz): nodes sharing an element
     int gnnz;
 };
@@ -259,6 +260,7 @@ int esm_system(ia_context *ctx, int m, int l, const double *src, const double *m
                double rho, double2 *DT, double2 *RHS);
 // df32: regular-element arithmetic in double-float (mixed path) instead of FP64;
 // split_ab (with df32): At and Bt are written as float4 (re hi, im hi, re lo, im lo)
+int mesh_creg(ia_context *ctx, ia_mesh *mesh);
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
               bool df32 = false, bool split_ab = false);

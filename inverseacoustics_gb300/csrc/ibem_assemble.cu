@@ -110,7 +110,7 @@ struct FreqBlock {
 // Regular-rule integral of one element against x_o for the block's
 // frequencies.  qd: precomputed (x, y, z, wa0..2, wb0..2) for each point,
 // structure of arrays with stride n (elements) and 9 * n per point.
-template <class R, int FB>
+template <class R, int FB, bool CT>
 __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
                                                 R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[FB], R dkf,
                                                 const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C,
@@ -126,7 +126,7 @@ __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n,
         const R r = r_mul(r2, invr);
         const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
         const R ft = r_mul(nd, r_mul(invr, invr));
-        r_mac(ct, r_mul(cw[q], ft), r_sub(r_zero(R()), invr));   // C term: w_q / 4pi (-ft / r)
+        if (CT) r_mac(ct, r_mul(cw[q], ft), r_sub(r_zero(R()), invr));   // C term: w_q / 4pi (-ft / r)
         cx<R> ph, step;
         r_sincos(r_mul(kf[0], r), tab, P, C, ph.im, ph.re);
         if (fb.uniform && fb.nf > 1) r_sincos(r_mul(dkf, r), tab, P, C, step.im, step.re);
@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     const double *__restrict__ reg,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
     const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, const float4 *__restrict__ dftab,
-    int split_ab, double2 *__restrict__ At, double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t,
-    double2 *__restrict__ Bhs_t)
+    int split_ab, const double *__restrict__ creg, double2 *__restrict__ At, double2 *__restrict__ Bt,
+    double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
 {
     constexpr int FB = AsmBlock<R>::FB;
     extern __shared__ __align__(16) unsigned char ibem_smem[];
@@ -289,9 +289,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             for (int f = 0; f < FB; ++f)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
-            regular_element<R>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb, kf, dkf,
-                               tab, P, C, cw, a, b, ctr);
-            ctr = r_norm(ctr);
+            regular_element<R, FB, !DF>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb,
+                                        kf, dkf, tab, P, C, cw, a, b, ctr);
+            if (!DF) ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
             for (int f = 0; f < FB; ++f) {
@@ -358,7 +358,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         if (lane == 0) ct_red[wid] = cs;
         __syncthreads();
         if (tid == 0) {
-            double tot = 0.0;
+            // the regular elements' part: evaluated above (FP64 kernel) or
+            // once per mesh (creg, double-float kernel)
+            double tot = DF ? creg[self] : 0.0;
             for (int w = 0; w < IBEM_THREADS / 32; ++w) tot += ct_red[w];
             const R diag = r_of_double<R>(-(1.0 + tot));
             for (int f = 0; f < fb.nf; ++f) {
@@ -396,6 +398,53 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     }
 }
 
+// The regular elements' C term per surface node, FP64: the frequency-
+// independent part of the collocation diagonal, sum over the elements not
+// incident to the node and the regular rule's points of w_q / 4pi (-(n.d) / r^3)
+// (the same terms the FP64 assembly kernel sums per row).  The double-float
+// assembly reads it rather than evaluating it for every (row, frequency).
+__global__ void __launch_bounds__(IBEM_THREADS) creg_kernel(int m, int n, int nq, const double *__restrict__ nodes,
+                                                            const double *__restrict__ qdat,
+                                                            const double *__restrict__ qnrm,
+                                                            const int *__restrict__ evert,
+                                                            const double *__restrict__ reg, double *__restrict__ creg)
+{
+    __shared__ double red[IBEM_THREADS / 32];
+    const int row = blockIdx.x, tid = threadIdx.x;
+    const double xo = nodes[row], yo = nodes[row + m], zo = nodes[row + 2 * (size_t)m];
+    double ct = 0.0;
+    for (int e = tid; e < n; e += IBEM_THREADS) {
+        const int4 vv = reinterpret_cast<const int4 *>(evert)[e];
+        if (vv.x == row || vv.y == row || vv.z == row) continue;
+        const double nx = qnrm[e], ny = qnrm[e + n], nz = qnrm[e + 2 * (size_t)n];
+        for (int q = 0; q < nq; ++q) {
+            const double *p = qdat + (size_t)q * 9 * n + e;
+            const double dx = p[0] - xo, dy = p[(size_t)n] - yo, dz = p[2 * (size_t)n] - zo;
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double invr = rsqrt(r2);
+            const double ft = (nx * dx + ny * dy + nz * dz) * (invr * invr);
+            ct = fma(reg[q + 2 * nq] * IA_INV4PI * ft, -invr, ct);
+        }
+    }
+    ct = warp_sum(ct);
+    if ((tid & 31) == 0) red[tid >> 5] = ct;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < IBEM_THREADS / 32; ++w) tot += red[w];
+        creg[row] = tot;
+    }
+}
+
+int mesh_creg(ia_context *ctx, ia_mesh *mesh)
+{
+    if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
+    creg_kernel<<<mesh->m, IBEM_THREADS, 0, ctx->stream>>>(mesh->m, mesh->n, mesh->nq, mesh->d_nodes, mesh->d_qdat,
+                                                         mesh->d_qnrm, mesh->d_evert, mesh->d_reg, mesh->d_creg);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
               bool df32, bool split_ab)
@@ -414,15 +463,15 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
         ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
-            mesh->d_reg, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0, At,
-            Bt, Ahs_t, Bhs_t);
+            mesh->d_reg, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0,
+            mesh->d_creg, At, Bt, Ahs_t, Bhs_t);
     } else {
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
             mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_reg, mesh->d_sing,
-            mesh->nqs, mics, cp, k, c, rho, coef, red, nullptr, 0, At, Bt, Ahs_t, Bhs_t);
+            mesh->nqs, mics, cp, k, c, rho, coef, red, nullptr, 0, nullptr, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
