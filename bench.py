@@ -636,17 +636,18 @@ def run_ours(args):
         del a64
     except Exception:
         pass
-    # The dominant kernel of the pass (16 % of the serialised launch list,
-    # profiles/ibem_pipeline_mixed_launches_F64.txt) is the mixed-path
-    # assembly, ibem_rows_kernel<dfl>.  Its bound is FP32 instruction issue,
-    # not HBM: warp instructions per 64-frequency launch scaled from the ncu
-    # capture of the same kernel in profiles/ibem_rows_kernel_dfl_F16.txt
-    # (smsp__inst_executed.sum 1.2536e9 for an 8-frequency launch; the work
+    # The dominant kernel of the pass (44 % of its SM time, 20 % of the
+    # serialised launch list, profiles/ibem_pipeline_mixed_launches_F64.txt)
+    # is the mixed-path assembly, ibem_rows_kernel<dfl>.  Its bound is FP32
+    # instruction issue, not HBM: warp instructions per 64-frequency launch
+    # scaled from the ncu capture of the same kernel in
+    # profiles/ibem_rows_kernel_dfl_F16.txt
+    # (smsp__inst_executed.sum 1.1914e9 for an 8-frequency launch; the work
     # per (row, frequency) CTA is fixed, so 64 frequencies issue 8x that),
     # against one warp instruction per SM sub-partition per clock at the
     # sampled SM clock; its DRAM bytes (read + write, 767.9 MB per 64
     # frequencies) come from the launch list's capture.
-    asm_warp_instr = 8 * 1.25363e9
+    asm_warp_instr = 8 * 1.19142e9
     asm_traffic = 767.9e6
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
@@ -666,7 +667,7 @@ def run_ours(args):
                 "hbm": {"achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                         "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "peak_kind": peak_kind,
                         "algorithmic_bytes": asm_bytes},
-                "note": "FP32-issue bound (ncu: issue 75 %, FMA pipe 66 %, 734 FP32 lane instructions per "
+                "note": "FP32-issue bound (ncu: issue 73 %, FMA pipe 64 %, 698 FP32 lane instructions per "
                         "quadrature-point evaluation); HBM is not its bound"}
     roofline_tensor = {"kernel": "tc_slice_kernel x2 + tc_gemm_kernel<7> (the transfer's FP64-level products, "
                                  "642 x 120 x 642 complex, 64 bins)",
