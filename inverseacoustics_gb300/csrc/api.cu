@@ -1065,12 +1065,14 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         cudaStream_t sq = ctx->side[q];
         if ((e = cudaStreamWaitEvent(sq, q == 0 ? ctx->ev_fork : ctx->ev_rows[q - 1], 0)) != cudaSuccess) break;
         ctx->stream = sq;
+        ctx->tail_part = q + 1 == parts;
         WsCursor cur{(char *)ctx->ws + need * q, 0, need};
         st = ibem_solve_part(ctx, mesh, l, d_mics, Fp, d_k + f0, nrhs, (const double2 *)d_p + (size_t)f0 * nrhs * l,
                              cfg, (double2 *)d_x + (size_t)f0 * nrhs * m,
                              d_lambda ? d_lambda + (size_t)f0 * nrhs : nullptr, d_s ? d_s + (size_t)f0 * p : nullptr,
                              d_info + f0, cur, q + 1 < parts ? ctx->ev_rows[q] : nullptr);
         ctx->stream = main;
+        ctx->tail_part = 0;
         if (!st && cur.off > need) st = IA_ERR_ALLOC;   // workspace accounting broken: the parts would overlap
     }
     // join every started part's stream back into the caller's stream

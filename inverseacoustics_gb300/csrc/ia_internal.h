@@ -21,6 +21,8 @@ struct ia_context {
     int capturing;         // between ia_capture_begin and ia_capture_end
     int no_tune;           // the autotuner may not time variants (allocation-free calls)
     int last_fallback;     // bins the last batched solve recomputed in FP64 (mixed_fallback)
+    int tail_part;         // the last part of a staggered pipeline is running (its chain ends the pass:
+                           // latency-bound stages may take more SMs per bin)
     int *dcount;           // small device counters (the GPU-wide Jacobi's per-bin flags), lazily allocated
     size_t dcount_n;
     // streams and events of the staggered IBEM pipeline (one stream per part;

@@ -470,13 +470,15 @@ static int qr_launch_t(ia_context *ctx, int rows, int cols, T *A, int lda, long 
     const size_t piv = PIV ? (sizeof(R) + sizeof(int)) * (size_t)cols : 0;
     if constexpr (std::is_same<T, float2>::value && PIV) {
         // the cluster form shortens one bin's chain but holds four SMs for
-        // ~60 % of the one-CTA form's time (2.3x its SM time): only for
-        // batches that leave most of the GPU idle (at most a quarter of the
-        // SMs in clusters; a 16-bin part of the 64-bin pass takes the one-CTA
-        // form)
+        // ~60 % of the one-CTA form's time (2.3x its SM time): for batches
+        // that leave most of the GPU idle (at most a quarter of the SMs in
+        // clusters) and for the last part of a staggered pipeline, whose
+        // chain ends the pass; the other 16-bin parts of the 64-bin pass take
+        // the one-CTA form.  Both forms give bitwise the same factors (the
+        // same reductions in the same order, the same pivot rule).
         const size_t csm = qr_cluster_smem(rows, cols);
         if (!B && rows <= 1 + 32 * QR_KPL && cols >= 2 * QRC_CS && csm <= 227 * 1024 &&
-            4 * QRC_CS * batch <= ctx->sm_count) {
+            (4 * QRC_CS * batch <= ctx->sm_count || ctx->tail_part)) {
             IA_CUDA_TRY(cudaFuncSetAttribute(qr_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
             cudaLaunchConfig_t lc = {};
             lc.gridDim = dim3((unsigned)(QRC_CS * batch));
