@@ -14,10 +14,13 @@
 // Only the first Mdot rows enter the dot products; rows Mdot..M-1 are rotated
 // along (the pipeline keeps conj(b)^T there, so U^H b falls out of the
 // rotations without forming U).
+#include <cooperative_groups.h>
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
 namespace ia {
+
+namespace cg = cooperative_groups;
 
 constexpr int SVD_MAX_WARPS = 16;
 
@@ -353,6 +356,193 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
 }
 
+// The same iteration over a cluster of JC_CS CTAs per bin (FP32, no
+// accumulator), for latency: small batches and the last part of a staggered
+// pipeline, whose chain ends the pass.  CTA q owns the pair slots
+// [q P, (q + 1) P) of the circle ordering (P = N2 / 2 / JC_CS).  From one
+// round to the next the ordering moves every "upper" column (slot k holds
+// columns (r + k) and (r - k) mod (N2 - 1), column N2 - 1 fixed in slot 0)
+// one slot down and every "lower" column one slot up; so a CTA keeps its
+// columns in two rings of P + 1 entries indexed by slot +/- round, and per
+// round only two columns cross to a neighbour CTA, written straight into its
+// ring's free entry through distributed shared memory (slot 0's upper column
+// turns into slot 1's lower one in CTA 0, the top slot's lower into its upper
+// one in the last CTA).  One cluster barrier per round.  Per pair the
+// arithmetic is jacobi_half_kernel's (a half-warp per pair, the same
+// reductions, rotation and stopping rule; the sweep's rotation count and
+// largest coupling are combined over the cluster), so the factors are
+// bitwise the same.
+constexpr int JC_CS = 4;
+
+template <class T>
+__global__ void __launch_bounds__(512)
+    jacobi_cluster_kernel(int M, int Mdot, int N, T *Yg, long long sY, int max_sweeps, typename ctraits<T>::R tol,
+                          int *info)
+{
+    typedef typename ctraits<T>::R R;
+    constexpr int KPL = 8;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int f = blockIdx.x / JC_CS;
+    const int N2 = N + (N & 1), NR = N2 - 1, P = N2 / 2 / JC_CS, RING = P + 1, k0 = rank * P;
+    extern __shared__ __align__(16) unsigned char jc_raw[];
+    T *up = reinterpret_cast<T *>(jc_raw);   // RING x M: upper columns, entry (slot + t) mod RING
+    T *lo = up + (size_t)RING * M;           // RING x M: lower columns, entry (slot - t) mod RING
+    T *fixc = lo + (size_t)RING * M;         // M: column N2 - 1 (CTA 0)
+    __shared__ int s_rot[2];
+    __shared__ unsigned s_rel[2];
+    Yg += f * sY;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int half = lane >> 4, hl = lane & 15, hw = 2 * wid + half;
+    const unsigned mask = half ? 0xffff0000u : 0x0000ffffu;
+    const T zero = ctraits<T>::make(0, 0);
+    // columns of slot k at round r (k0 = 0 .. NP - 1)
+    auto col_up = [&](int k, int r) { int c = r + k; return c >= NR ? c - NR : c; };
+    auto col_lo = [&](int k, int r) { if (k == 0) return N2 - 1; int c = r - k; return c < 0 ? c + NR : c; };
+    auto load_col = [&](T *dst, int c) {
+        for (int i = threadIdx.x; i < M; i += blockDim.x) dst[i] = c < N ? Yg[(size_t)c * M + i] : zero;
+    };
+    // round 0: slot k holds columns k and N2 - 1 - k (N2 - 1 in slot 0)
+    for (int s = 0; s < P; ++s) {
+        const int k = k0 + s;
+        load_col(up + (size_t)s * M, col_up(k, 0));
+        if (k == 0) load_col(fixc, N2 - 1);
+        else load_col(lo + (size_t)s * M, col_lo(k, 0));
+    }
+    if (threadIdx.x == 0) {
+        s_rot[0] = s_rot[1] = 0;
+        s_rel[0] = s_rel[1] = 0u;
+    }
+    cluster.sync();
+    int r = 0, t = 0, par = 0, sweep = 0;   // round mod NR, round mod RING
+    for (; sweep < max_sweeps; ++sweep) {
+        int rot_local = 0;
+        float relmax = 0.f;
+        for (int round = 0; round < NR; ++round) {
+            const int tn = t + 1 == RING ? 0 : t + 1;
+            for (int s = hw; s < P; s += 2 * nw) {
+                const int k = k0 + s;
+                const int cu = col_up(k, r), cl = col_lo(k, r);
+                int eu = s + t;
+                if (eu >= RING) eu -= RING;
+                int el = s - t;
+                if (el < 0) el += RING;
+                T *pu = up + (size_t)eu * M, *pl = k == 0 ? fixc : lo + (size_t)el * M;
+                const bool uf = cu < cl;   // the upper column is y_i
+                T *yi = uf ? pu : pl, *yj = uf ? pl : pu;
+                const int j = uf ? cl : cu;
+                T ui[KPL], uj[KPL];
+#pragma unroll
+                for (int q = 0; q < KPL; ++q) {
+                    const int rr = hl + 16 * q;
+                    ui[q] = rr < M ? yi[rr] : zero;
+                    uj[q] = rr < M ? yj[rr] : zero;
+                }
+                if (j < N) {
+                    R a = 0, b = 0, c;
+                    T g = zero, sp;
+#pragma unroll
+                    for (int q = 0; q < KPL; ++q) {
+                        if (hl + 16 * q < Mdot) {
+                            a += zabs2(ui[q]);
+                            b += zabs2(uj[q]);
+                            zcfma(g, ui[q], uj[q]);
+                        }
+                    }
+                    a = half_sum<T>(a, mask);
+                    b = half_sum<T>(b, mask);
+                    g.x = half_sum<T>(g.x, mask);
+                    g.y = half_sum<T>(g.y, mask);
+                    R rel = 0;
+                    if (jacobi_rotation(a, b, g, tol, c, sp, sizeof(R) == 4 ? &rel : nullptr)) {
+                        relmax = fmaxf(relmax, (float)rel);
+#pragma unroll
+                        for (int q = 0; q < KPL; ++q) {
+                            const int rr = hl + 16 * q;
+                            if (rr < M) {
+                                rotate_pair(ui[q], uj[q], c, sp);
+                                yi[rr] = ui[q];
+                                yj[rr] = uj[q];
+                            }
+                        }
+                        rot_local++;
+                    }
+                }
+                // the columns that leave this CTA's rings for the next round
+                const T *vu = uf ? ui : uj, *vl = uf ? uj : ui;   // registers of the upper / lower column
+                if (s == 0) {
+                    T *dst;
+                    if (rank > 0) {
+                        int e = P - 1 + tn;
+                        if (e >= RING) e -= RING;
+                        dst = cluster.map_shared_rank(up, rank - 1) + (size_t)e * M;
+                    } else {
+                        int e = 1 - tn;
+                        if (e < 0) e += RING;
+                        dst = lo + (size_t)e * M;
+                    }
+#pragma unroll
+                    for (int q = 0; q < KPL; ++q)
+                        if (hl + 16 * q < M) dst[hl + 16 * q] = vu[q];
+                }
+                if (s == P - 1) {
+                    T *dst;
+                    if (rank < JC_CS - 1) {
+                        int e = -tn;
+                        if (e < 0) e += RING;
+                        dst = cluster.map_shared_rank(lo, rank + 1) + (size_t)e * M;
+                    } else {
+                        int e = P - 1 + tn;
+                        if (e >= RING) e -= RING;
+                        dst = up + (size_t)e * M;
+                    }
+#pragma unroll
+                    for (int q = 0; q < KPL; ++q)
+                        if (hl + 16 * q < M) dst[hl + 16 * q] = vl[q];
+                }
+            }
+            cluster.sync();
+            t = tn;
+            r = r + 1 == NR ? 0 : r + 1;
+        }
+        if (hl == 0 && rot_local) {
+            atomicAdd(&s_rot[par], rot_local);
+            if (sizeof(R) == 4) atomicMax(&s_rel[par], __float_as_uint(relmax));
+        }
+        cluster.sync();
+        int total = 0;
+        unsigned mr = 0u;
+        for (int q = 0; q < JC_CS; ++q) {
+            total += *cluster.map_shared_rank(&s_rot[par], q);
+            const unsigned v = *cluster.map_shared_rank(&s_rel[par], q);
+            mr = v > mr ? v : mr;
+        }
+        if (threadIdx.x == 0) {
+            s_rot[par ^ 1] = 0;
+            s_rel[par ^ 1] = 0u;
+        }
+        par ^= 1;
+        if (total == 0) break;
+        if (sizeof(R) == 4 && __uint_as_float(mr) < 0.5f * sqrtf((float)tol)) break;
+    }
+    cluster.sync();   // every CTA has read the others' counters
+    // r is back at 0 after whole sweeps: the round-0 layout, entries shifted by t
+    for (int s = 0; s < P; ++s) {
+        const int k = k0 + s;
+        int eu = s + t;
+        if (eu >= RING) eu -= RING;
+        int el = s - t;
+        if (el < 0) el += RING;
+        const int cu = col_up(k, r), cl = col_lo(k, r);
+        const T *pu = up + (size_t)eu * M, *pl = k == 0 ? fixc : lo + (size_t)el * M;
+        for (int i = threadIdx.x; i < M; i += blockDim.x) {
+            if (cu < N) Yg[(size_t)cu * M + i] = pu[i];
+            if (cl < N) Yg[(size_t)cl * M + i] = pl[i];
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
+}
+
 template <class T>
 __global__ void identity_kernel(int N, T *V, long long sV)
 {
@@ -544,6 +734,36 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     // once in 32 warps; FP64: 16 warps, the 128-register budget), Y in shared
     // memory up to the per-CTA limit (an FP64 121 x 120 system fits)
     const size_t half_smem_max = sizeof(T) <= 8 ? 200 * 1024 : 227 * 1024 - 64;   // 16 B static besides
+    if constexpr (sizeof(T) == 8) {
+        // FP32 over a cluster per bin: for batches that leave most of the GPU
+        // idle and for the last part of a staggered pipeline (4x the SMs for
+        // ~1/3 of the time per bin; bitwise the one-CTA result)
+        const int np = (N + (N & 1)) / 2;
+        if (!V && M <= 128 && N <= 128 && np % JC_CS == 0 && np / JC_CS >= 2 &&
+            (4 * JC_CS * batch <= ctx->sm_count || ctx->tail_part)) {
+            const int P = np / JC_CS;
+            const size_t csm = sizeof(T) * ((size_t)2 * (P + 1) * M + M);
+            const int nwc = (P + 1) / 2;
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3((unsigned)(JC_CS * batch));
+            lc.blockDim = dim3((unsigned)(32 * nwc));
+            lc.dynamicSmemBytes = csm;
+            lc.stream = ctx->stream;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = JC_CS;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            lc.attrs = at;
+            lc.numAttrs = 1;
+            if (csm > 48 * 1024)
+                IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)csm));
+            IA_CUDA_TRY(cudaLaunchKernelEx(&lc, jacobi_cluster_kernel<T>, M, Mdot, N, Y, sY, max_sweeps, tol, info));
+            IA_LAUNCH_CHECK(ctx);
+            return IA_OK;
+        }
+    }
     if (!V && M <= 128 && N <= 128 && smem <= half_smem_max) {
         const int pairs = (N + (N & 1)) / 2;
         const int wcap = sizeof(T) <= 8 ? 32 : 16;
