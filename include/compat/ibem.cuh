@@ -5,10 +5,15 @@
 //   ibemgpu <- CUDA/ibem.cuh:263  (r_msg, e_ng, r_lhg device pointers; cp host)
 // Quadrature: like the reference, IPF.txt (regular rule) and IPFs.txt
 // (singular rule, one $PAGE per vertex) are read from the current directory
-// (format of CUDA/ibem.cuh:265-312); when they are absent, ia_ibem's built-in
-// rules are used instead of exiting.
+// (format of CUDA/ibem.cuh:265-312); when both are absent, ia_ibem's built-in
+// rules are used instead of exiting; when either is present but does not
+// parse (a missing partner file, a truncated table, a bad count), the call
+// throws instead of using rules the caller did not ask for.
 #pragma once
+#include <cstdio>
 #include <cstring>
+#include <stdexcept>
+#include <string>
 #include <vector>
 #include "ia_compat_common.cuh"
 
@@ -60,20 +65,33 @@ inline bool ia_compat_read_ipf(std::vector<double> &reg, int &nq, std::vector<do
     return count == 3 * nqs;
 }
 
+// The quadrature rules for a call: null when neither file exists (built-in
+// rules), the parsed tables otherwise; throws when a file exists but the pair
+// does not parse.
+inline const ia_rules *ia_compat_rules(std::vector<double> &reg, std::vector<double> &sing, ia_rules &rules,
+                                       const char *who)
+{
+    FILE *a = std::fopen("IPF.txt", "r"), *b = std::fopen("IPFs.txt", "r");
+    const bool any = a || b;
+    if (a) std::fclose(a);
+    if (b) std::fclose(b);
+    if (!any) return nullptr;
+    int nq = 0, nqs = 0;
+    if (!ia_compat_read_ipf(reg, nq, sing, nqs))
+        throw std::runtime_error(std::string(who) + ": IPF.txt / IPFs.txt present but malformed");
+    rules.nq = nq;
+    rules.regular = reg.data();
+    rules.nqs = nqs;
+    rules.singular = sing.data();
+    return &rules;
+}
+
 extern "C" inline void ibem(int m, int l, int n, double *r_ms, int *e_n, double *r_lh, cuDoubleComplex **m_e,
                             cuDoubleComplex **h, double k, int n_ch, double *cp)
 {
     std::vector<double> reg, sing;
-    int nq = 0, nqs = 0;
     ia_rules rules;
-    const ia_rules *rp = nullptr;
-    if (ia_compat_read_ipf(reg, nq, sing, nqs)) {
-        rules.nq = nq;
-        rules.regular = reg.data();
-        rules.nqs = nqs;
-        rules.singular = sing.data();
-        rp = &rules;
-    }
+    const ia_rules *rp = ia_compat_rules(reg, sing, rules, "ibem");
     ia_config cfg = ia_compat_config();
     ia_compat_check(ia_ibem(m, l, n, r_ms, e_n, r_lh, (ia_complex **)m_e, (ia_complex **)h, k, n_ch, cp, rp, &cfg),
                     "ibem");

@@ -15,16 +15,8 @@ extern "C" inline void invr(int m, int l, int n, double *r_ms, int *e_n, double 
                             cuDoubleComplex **h, cuDoubleComplex **q_e, double k, int n_ch, double *cp, int n_am)
 {
     std::vector<double> reg, sing;
-    int nq = 0, nqs = 0;
     ia_rules rules;
-    const ia_rules *rp = nullptr;
-    if (ia_compat_read_ipf(reg, nq, sing, nqs)) {
-        rules.nq = nq;
-        rules.regular = reg.data();
-        rules.nqs = nqs;
-        rules.singular = sing.data();
-        rp = &rules;
-    }
+    const ia_rules *rp = ia_compat_rules(reg, sing, rules, "invr");
     ia_config cfg = ia_compat_config();
     ia_compat_check(ia_invr(m, l, n, r_ms, e_n, r_lh, (ia_complex **)m_e, (ia_complex **)h, (ia_complex **)q_e, k,
                             n_ch, cp, n_am, rp, &cfg),

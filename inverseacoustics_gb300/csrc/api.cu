@@ -8,6 +8,7 @@
 #include <functional>
 #include <initializer_list>
 #include <mutex>
+#include <tuple>
 #include <vector>
 #include "ia_common.cuh"
 #include "df32.cuh"
@@ -343,6 +344,16 @@ int ia_mesh_create(ia_context *ctx, int m, int n, const double *nodes, const int
         int a = elems[i], b = elems[i + n], c = elems[i + 2 * n];
         if (a < 0 || b < 0 || c < 0 || a >= m || b >= m || c >= m) return IA_ERR_ARG;
         if (a == b || b == c || a == c) return IA_ERR_ARG;
+    }
+    {
+        // two nodes at the same point give two equal collocation rows (a
+        // singular system): refused, like a degenerate element
+        std::vector<int> ord(m);
+        for (int i = 0; i < m; ++i) ord[i] = i;
+        auto key = [&](int i) { return std::make_tuple(nodes[i], nodes[i + m], nodes[i + 2 * m]); };
+        std::sort(ord.begin(), ord.end(), [&](int x, int y) { return key(x) < key(y); });
+        for (int i = 1; i < m; ++i)
+            if (key(ord[i]) == key(ord[i - 1])) return IA_ERR_ARG;
     }
     std::vector<double> reg, sing;
     int nq, nqs;

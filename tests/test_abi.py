@@ -70,3 +70,12 @@ def test_bad_arguments_rejected_before_device_work():
         with pytest.raises(_lib.IAError) as e:
             api.invr(nodes, elems, np.ones((3, 2)), 1.0, n_am)
         assert e.value.code == 1
+    # wavenumber k <= 0 or not a number (the reference has no check: k = 0
+    # zeroes i rho c k B and gives a singular transfer)
+    for k in (0.0, -2.0, float("nan")):
+        with pytest.raises(_lib.IAError) as e:
+            api.ibem(nodes, elems, np.ones((3, 2)), k)
+        assert e.value.code == 1
+        with pytest.raises(_lib.IAError) as e:
+            api.hels(np.ones((3, 4)), np.ones((3, 4)), k, 2)
+        assert e.value.code == 1

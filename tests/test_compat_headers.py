@@ -32,6 +32,59 @@ def test_compat_program_compiles_and_links(tmp_path):
     assert os.path.exists(exe)
 
 
+def _write_ipf(d, reg, sing, truncate_reg=False, bad_count=False, pages=3):
+    nq = reg.shape[0]
+    lines = [str(nq + 1 if bad_count else nq)] + [f"{a!r} {b!r} {w!r}" for a, b, w in reg]
+    if truncate_reg:
+        lines = lines[:-2]
+    (d / "IPF.txt").write_text("\n".join(lines) + "\n")
+    nqs = sing.shape[1]
+    out = [str(nqs)]
+    for p in range(pages):
+        out.append(f"$PAGE {p + 1}")
+        out += [f"{a!r} {b!r} {w!r}" for a, b, w in sing[p]]
+    (d / "IPFs.txt").write_text("\n".join(out) + "\n")
+
+
+def test_compat_quadrature_files(tmp_path):
+    """Like the reference, the drop-in ibem()/invr() read IPF.txt and IPFs.txt
+    from the current directory; with neither present the built-in rules are
+    used; a file that is present but does not parse (partner file missing,
+    truncated table, wrong count, a missing page) makes the call throw rather
+    than fall back to rules the caller did not ask for (the reference exits on
+    a missing file, CUDA/ibem.cuh:270-273, and reads past a short one)."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "compat_ipf")
+    src = os.path.join(ROOT, "tests", "compat", "compat_ipf.cu")
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", f"-I{ROOT}/include/compat", f"-I{ROOT}/include", src, "-o", exe,
+                        f"-L{LIBDIR}", "-lia", "-Xlinker", f"-rpath={LIBDIR}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    reg, sing = Q.builtin()      # (nq, 3) and (3 pages, nqs, 3) rows of xi1, xi2, w
+
+    def run(setup):
+        d = tmp_path / setup
+        d.mkdir()
+        if setup == "valid":
+            _write_ipf(d, reg, sing)
+        elif setup == "only_regular":
+            _write_ipf(d, reg, sing)
+            (d / "IPFs.txt").unlink()
+        elif setup == "truncated":
+            _write_ipf(d, reg, sing, truncate_reg=True)
+        elif setup == "bad_count":
+            _write_ipf(d, reg, sing, bad_count=True)
+        elif setup == "missing_page":
+            _write_ipf(d, reg, sing, pages=2)
+        out = subprocess.run([exe], capture_output=True, text=True, cwd=d)
+        assert out.returncode == 0, out.stderr
+        return out.stdout.strip()
+
+    assert run("none") == "builtin"
+    assert run("valid") == f"rules {reg.shape[0]} {sing.shape[1]}"
+    for bad in ("only_regular", "truncated", "bad_count", "missing_page"):
+        assert run(bad).startswith("error ibem: IPF.txt / IPFs.txt present but malformed"), bad
+
+
 @pytest.mark.gpu
 def test_compat_program_matches_oracle(tmp_path, cuda):
     exe = _build(tmp_path)

@@ -101,10 +101,8 @@ def test_design_full_size_finite_differences(cuda, ctx):
     assert np.max(np.abs(gl2.cpu().numpy() - glo)) <= 1e-9 * np.max(np.abs(glo))
 
 
-def test_design_adam_on_device(cuda, ctx):
-    """200 Adam steps of the full design problem (128 frequencies) with the
-    adjoint behind a torch.autograd.Function; no host round trip inside the
-    loop.  The loss must fall."""
+def _design_fn(ctx):
+    """The test harness's torch.autograd.Function around ia_esm_design_batch."""
     from inverseacoustics_gb300 import api
     import torch
 
@@ -122,6 +120,12 @@ def test_design_adam_on_device(cuda, ctx):
             gm, gd, gl = fctx.saved_tensors
             return gout * gm, gout * gd, gout * gl, None, None, None, None
 
+    return EsmDesign
+
+
+def _design_problem(cuda):
+    """The full design problem: 128 frequencies, 128 mics, 642 sources, 16
+    fields; (initial mics, initial log lambda, device tensors S, K, Q, N)."""
     w = g.esm_design(n_freq=128)
     rng = np.random.default_rng(40)
     mics0, surf = w.arrays["mics"], w.arrays["surface"]
@@ -134,20 +138,78 @@ def test_design_adam_on_device(cuda, ctx):
         p = G @ q[f]
         noise[f] = 10 ** (-30 / 20) * np.linalg.norm(p) / math.sqrt(p.size) * g.complex_normal(rng, (128, 16))
         ll0[f] = math.log(0.05 * np.linalg.norm(G) / math.sqrt(128))
-    mics = T(mics0, cuda).requires_grad_(True)
-    retreat = T(np.array([0.04]), cuda).requires_grad_(True)
-    loglam = T(ll0, cuda).requires_grad_(True)
-    S, K = T(surf, cuda), T(w.k, cuda)
-    Q, N = T(np.transpose(q, (0, 2, 1)), cuda), T(np.transpose(noise, (0, 2, 1)), cuda)
-    opt = torch.optim.Adam([{"params": [mics, retreat], "lr": 2e-4}, {"params": [loglam], "lr": 2e-2}])
-    losses = []
-    for step in range(200):
-        opt.zero_grad()
-        L = EsmDesign.apply(mics, retreat, loglam, S, K, Q, N)
-        L.backward()
-        opt.step()
-        if step in (0, 199):
-            losses.append(L.detach())
+    return (mics0, ll0, T(surf, cuda), T(w.k, cuda), T(np.transpose(q, (0, 2, 1)), cuda),
+            T(np.transpose(noise, (0, 2, 1)), cuda))
+
+
+def _adam(params):
+    import torch
+    mics, retreat, loglam = params
+    return torch.optim.Adam([{"params": [mics, retreat], "lr": 2e-4}, {"params": [loglam], "lr": 2e-2}])
+
+
+def save_checkpoint(path, params, opt):
+    """Parameters and Adam state of the design loop as one .npz."""
+    d = {}
+    for i, p in enumerate(params):
+        st = opt.state[p]
+        d[f"param{i}"] = p.detach().cpu().numpy()
+        d[f"exp_avg{i}"] = st["exp_avg"].cpu().numpy()
+        d[f"exp_avg_sq{i}"] = st["exp_avg_sq"].cpu().numpy()
+        d[f"step{i}"] = st["step"].cpu().numpy()
+    np.savez(path, **d)
+
+
+def load_checkpoint(path, params, opt):
+    import torch
+    z = np.load(path)
+    with torch.no_grad():
+        for i, p in enumerate(params):
+            p.copy_(torch.as_tensor(z[f"param{i}"], device=p.device))
+    for i, p in enumerate(params):
+        opt.state[p] = {"step": torch.as_tensor(z[f"step{i}"]),
+                        "exp_avg": torch.as_tensor(z[f"exp_avg{i}"], device=p.device),
+                        "exp_avg_sq": torch.as_tensor(z[f"exp_avg_sq{i}"], device=p.device)}
+
+
+def test_design_adam_on_device(cuda, ctx, tmp_path):
+    """200 Adam steps of the full design problem (128 frequencies) with the
+    adjoint behind a torch.autograd.Function; no host round trip inside the
+    loop.  The loss must fall.  A checkpoint (parameters and Adam state, .npz)
+    written at step 100 and resumed in a fresh optimizer ends bitwise where the
+    uninterrupted run ends (the adjoint's reductions are deterministic)."""
+    import torch
+    EsmDesign = _design_fn(ctx)
+    mics0, ll0, S, K, Q, N = _design_problem(cuda)
+
+    def fresh():
+        return [T(mics0, cuda).requires_grad_(True), T(np.array([0.04]), cuda).requires_grad_(True),
+                T(ll0, cuda).requires_grad_(True)]
+
+    def run(params, opt, steps, ckpt_at=None):
+        losses = []
+        for step in steps:
+            if step == ckpt_at:
+                save_checkpoint(tmp_path / "design.npz", params, opt)
+            opt.zero_grad()
+            L = EsmDesign.apply(params[0], params[1], params[2], S, K, Q, N)
+            L.backward()
+            opt.step()
+            if step in (0, 199):
+                losses.append(L.detach())
+        return losses
+
+    params = fresh()
+    opt = _adam(params)
+    losses = run(params, opt, range(200), ckpt_at=100)
     torch.cuda.synchronize()
     l0, l1 = (float(x.item()) for x in losses)
     assert math.isfinite(l1) and l1 < 0.95 * l0, (l0, l1)
+    # resume from step 100
+    params2 = fresh()
+    opt2 = _adam(params2)
+    load_checkpoint(tmp_path / "design.npz", params2, opt2)
+    run(params2, opt2, range(100, 200))
+    torch.cuda.synchronize()
+    for p, p2 in zip(params, params2):
+        assert torch.equal(p.detach(), p2.detach())

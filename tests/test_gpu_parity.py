@@ -351,3 +351,9 @@ def test_bad_rule_and_mesh_rejected(cuda, ctx):
     with pytest.raises(api.IAError) as e:
         api.Mesh(ctx, nodes, el)
     assert e.value.code == 1
+    # two nodes at one point: equal collocation rows, a singular system
+    nd = nodes.copy()
+    nd[:, 5] = nd[:, 3]
+    with pytest.raises(api.IAError) as e:
+        api.Mesh(ctx, nd, elems)
+    assert e.value.code == 1
