@@ -159,6 +159,18 @@ const char *ia_version(void);
 int ia_last_cuda_error(void);
 void ia_free(void *p);
 
+/* Debug aid with no counterpart in the reference (which has no checks of its
+ * own): in the debug build of the library (libia_debug.so, compiled with
+ * IA_DEBUG_BOUNDS) the main kernels test their global-memory indexes against
+ * the buffers' extents, skip an access that fails and record it.  This call
+ * reports the records since the previous call and clears them: *enabled = 1
+ * when the library was built with the checks (0: release build, nothing
+ * checked), *count = the number of failed tests, and for the first failure its
+ * source file name (static string, or NULL), line, index and extent.  It
+ * copies from the device and so waits for the device's queued work. */
+int ia_bounds_report(int *enabled, unsigned long long *count, const char **file, int *line, long long *index,
+                     long long *extent);
+
 /* gmsh v2.2 ASCII mesh reader; replaces geometry() (CUDA/utils.cuh:291).
  * Nodes r_ms (3 x m SoA), triangles e_n (element type 2 with three distinct
  * vertices, 0-based, 3 x n SoA, file order) and field points

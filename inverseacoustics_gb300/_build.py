@@ -3,6 +3,8 @@
 Each translation unit compiles in parallel to an object file under
 ``inverseacoustics_gb300/_build/``; the objects link into
 ``inverseacoustics_gb300/libia.so`` (static CUDA runtime, C ABI only).
+``build(debug_bounds=True)`` makes the bounds-checked debug library
+``libia_debug.so`` (IA_DEBUG_BOUNDS; objects under ``_build_debug/``).
 """
 from __future__ import annotations
 
@@ -44,15 +46,17 @@ def _stale(out, ins):
     return any(os.path.getmtime(i) > t for i in ins)
 
 
-def build(verbose: bool = False, force: bool = False, extra_flags=None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, extra_flags=None, debug_bounds: bool = False) -> str:
+    bdir = BUILD + "_debug" if debug_bounds else BUILD
+    lib = os.path.join(HERE, "libia_debug.so") if debug_bounds else LIB
+    os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
     deps = _deps()
-    flags = NVCC_FLAGS + list(extra_flags or [])
+    flags = NVCC_FLAGS + list(extra_flags or []) + (["-DIA_DEBUG_BOUNDS"] if debug_bounds else [])
     jobs = []
     objs = []
     for src in sources():
-        obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
+        obj = os.path.join(bdir, os.path.basename(src).replace(".cu", ".o"))
         objs.append(obj)
         if force or _stale(obj, [src] + deps):
             jobs.append([nvcc, *ARCH, *flags, "-c", src, "-o", obj])
@@ -66,15 +70,15 @@ def build(verbose: bool = False, force: bool = False, extra_flags=None) -> str:
                     print(r.stdout + r.stderr)
                 if r.returncode != 0:
                     raise RuntimeError(f"nvcc failed for {j[-3]}")
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static"]
+    if force or jobs or _stale(lib, objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", lib, *objs, "-cudart", "static"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode != 0:
             print(" ".join(cmd))
             print(r.stdout + r.stderr)
         if r.returncode != 0:
-            raise RuntimeError("link of libia.so failed")
-    return LIB
+            raise RuntimeError(f"link of {os.path.basename(lib)} failed")
+    return lib
 
 
 if __name__ == "__main__":

@@ -9,7 +9,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libia.so")
+# IA_LIBRARY selects another in-tree build, e.g. the bounds-checked
+# libia_debug.so (inverseacoustics_gb300._build.build(debug_bounds=True))
+LIB_PATH = os.environ.get("IA_LIBRARY") or os.path.join(HERE, "libia.so")
 
 IA_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "allocation failed",
@@ -67,6 +69,8 @@ _SIGS = {
     "ia_status_string": (C.c_char_p, [_I]),
     "ia_version": (C.c_char_p, []),
     "ia_last_cuda_error": (_I, []),
+    "ia_bounds_report": (_I, [C.POINTER(C.c_int), C.POINTER(C.c_ulonglong), C.POINTER(C.c_char_p),
+                              C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "ia_free": (None, [_P]),
     "ia_read_msh": (_I, [C.c_char_p, _D, _D, _PP, _PP, _PP, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "ia_esm": (_I, [_I, _I, _P, _P, _PP, _PP, _D, _D, _P]),
@@ -120,11 +124,11 @@ def declared_symbols():
 
 
 def lib():
-    """Load libia.so.  Raises OSError if it has not been built."""
+    """Load libia.so (or IA_LIBRARY).  Raises OSError if it has not been built."""
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise OSError(f"libia.so not built at {LIB_PATH}; run inverseacoustics_gb300._build.build()")
+            raise OSError(f"library not built at {LIB_PATH}; run inverseacoustics_gb300._build.build()")
         L = C.CDLL(LIB_PATH)
         for name, (res, args) in _SIGS.items():
             fn = getattr(L, name)

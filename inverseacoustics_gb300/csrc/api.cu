@@ -265,6 +265,42 @@ const char *ia_status_string(int status)
 const char *ia_version(void) { return "ia-gb300 0.1 (sm_103a)"; }
 int ia_config_size(void) { return (int)sizeof(ia_config); }
 int ia_last_cuda_error(void) { return g_last_cuda_error; }
+
+int ia_bounds_report(int *enabled, unsigned long long *count, const char **file, int *line, long long *index,
+                     long long *extent)
+{
+    if (!enabled || !count || !file || !line || !index || !extent) return IA_ERR_ARG;
+    *count = 0;
+    *file = nullptr;
+    *line = 0;
+    *index = *extent = 0;
+#ifndef IA_DEBUG_BOUNDS
+    *enabled = 0;   // release build: nothing is checked, no device access
+    return IA_OK;
+#else
+    *enabled = 1;
+    const struct {
+        const char *name;
+        int (*read)(ia::IaBoundsSite *);
+    } units[] = {{"dense.cu", ia::bounds_read_dense}, {"tc_gemm.cu", ia::bounds_read_tc},
+                 {"svd.cu", ia::bounds_read_svd},     {"wide_solve.cu", ia::bounds_read_wide},
+                 {"ibem_assemble.cu", ia::bounds_read_asm}};
+    if (cudaDeviceSynchronize() != cudaSuccess) return IA_ERR_CUDA;
+    for (const auto &u : units) {
+        ia::IaBoundsSite site;
+        const int st = u.read(&site);
+        if (st) return st;
+        if (site.count && !*file) {
+            *file = u.name;
+            *line = site.line;
+            *index = site.index;
+            *extent = site.extent;
+        }
+        *count += site.count;
+    }
+    return IA_OK;
+#endif
+}
 void ia_free(void *p) { free(p); }
 
 int ia_create(ia_context **out, int device, void *stream)

@@ -514,8 +514,8 @@ __device__ __forceinline__ float2 shfl_c(float2 v, int src)
 // X rows [lo, hi) -= T(:, 0:nb) X(k0:k0+nb, :), thread per row (T: the L or
 // U block column, leading dimension lda, starting at row 0 of the matrix)
 template <int RB, int NT, bool FULL>
-__device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int lda, float2 *X, int xs, int k0,
-                                             int nb, int lo, int hi)
+__device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int lda, long long text, float2 *X, int xs,
+                                             int k0, int nb, int lo, int hi)
 {
     constexpr int TH = LU_NB / 2;   // the row's entries in two halves (register budget: two CTAs per SM)
     for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
@@ -528,7 +528,9 @@ __device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int l
             float2 trow[TH];
 #pragma unroll
             for (int t = 0; t < TH; ++t)
-                trow[t] = (FULL || h + t < nb) ? tp[(size_t)(h + t) * lda] : make_float2(0.f, 0.f);
+                trow[t] = (FULL || h + t < nb) && IA_IDX_OK(i + (long long)(h + t) * lda, text)
+                              ? tp[(size_t)(h + t) * lda]
+                              : make_float2(0.f, 0.f);
 #pragma unroll
             for (int t = 0; t < TH; t += 2) {
                 if (FULL || h + t < nb) {
@@ -566,9 +568,10 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
     ipiv += (size_t)f * n;
     B += f * sB + (size_t)c0 * ldb;
     const float2 zero = make_float2(0.f, 0.f);
+    const long long lext = (long long)n * lda, bext = (long long)nc * ldb;   // this matrix's LU, this CTA's B columns
     for (int e = tid; e < xs * GETRS_RB; e += NT) {
         const int i = e % xs, c = e / xs;
-        X[e] = c < nc && i < n ? B[i + (size_t)c * ldb] : zero;
+        X[e] = c < nc && i < n && IA_IDX_OK(i + (long long)c * ldb, bext) ? B[i + (size_t)c * ldb] : zero;
     }
     for (int j = tid; j < n; j += NT) piv[j] = ipiv[j];
     __syncthreads();
@@ -576,7 +579,7 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
         float2 *x = X + (size_t)tid * xs;
         for (int j = 0; j < n; ++j) {
             const int p = piv[j];
-            if (p != j) {
+            if (p != j && IA_IDX_OK(p, n)) {
                 const float2 t = x[j];
                 x[j] = x[p];
                 x[p] = t;
@@ -589,7 +592,9 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
         const int nb = n - k0 < LU_NB ? n - k0 : LU_NB, kend = k0 + nb;
         for (int e = tid; e < LU_NB * LU_NB; e += NT) {
             const int r = e % LU_NB, cc = e / LU_NB;
-            D[r][cc] = r < nb && cc < nb ? LU[k0 + r + (size_t)(k0 + cc) * lda] : zero;
+            D[r][cc] = r < nb && cc < nb && IA_IDX_OK(k0 + r + (long long)(k0 + cc) * lda, lext)
+                           ? LU[k0 + r + (size_t)(k0 + cc) * lda]
+                           : zero;
         }
         __syncthreads();
         if (wid < GETRS_RB) {
@@ -605,8 +610,9 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
             if (lane < nb) x[lane] = v;
         }
         __syncthreads();
-        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, kend, n);
-        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, kend, n);
+        const long long text = lext - (long long)k0 * lda;
+        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, text, X, xs, k0, nb, kend, n);
+        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, text, X, xs, k0, nb, kend, n);
         __syncthreads();
     }
     // backward: U X = Y
@@ -614,10 +620,14 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
         const int nb = n - k0 < LU_NB ? n - k0 : LU_NB;
         for (int e = tid; e < LU_NB * LU_NB; e += NT) {
             const int r = e % LU_NB, cc = e / LU_NB;
-            D[r][cc] = r < nb && cc < nb ? LU[k0 + r + (size_t)(k0 + cc) * lda] : zero;
+            D[r][cc] = r < nb && cc < nb && IA_IDX_OK(k0 + r + (long long)(k0 + cc) * lda, lext)
+                           ? LU[k0 + r + (size_t)(k0 + cc) * lda]
+                           : zero;
         }
         if (tid < LU_NB) {
-            const float2 d = tid < nb ? LU[k0 + tid + (size_t)(k0 + tid) * lda] : zero;
+            const float2 d = tid < nb && IA_IDX_OK(k0 + tid + (long long)(k0 + tid) * lda, lext)
+                                 ? LU[k0 + tid + (size_t)(k0 + tid) * lda]
+                                 : zero;
             Dinv[tid] = tid < nb ? zdiv(make_float2(1.f, 0.f), d) : zero;
         }
         __syncthreads();
@@ -635,13 +645,14 @@ __global__ void __launch_bounds__(NT, 2) getrs_fused_kernel(int n, int nrhs, con
             if (lane < nb) x[lane] = v;
         }
         __syncthreads();
-        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, 0, k0);
-        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, X, xs, k0, nb, 0, k0);
+        const long long text = lext - (long long)k0 * lda;
+        if (nb == LU_NB) getrs_update<GETRS_RB, NT, true>(LU + (size_t)k0 * lda, lda, text, X, xs, k0, nb, 0, k0);
+        else getrs_update<GETRS_RB, NT, false>(LU + (size_t)k0 * lda, lda, text, X, xs, k0, nb, 0, k0);
         __syncthreads();
     }
     for (int e = tid; e < n * nc; e += NT) {
         const int i = e % n, c = e / n;
-        B[i + (size_t)c * ldb] = X[i + (size_t)c * xs];
+        if (IA_IDX_OK(i + (long long)c * ldb, bext)) B[i + (size_t)c * ldb] = X[i + (size_t)c * xs];
     }
 }
 
@@ -812,5 +823,7 @@ template int copy2d_batched<double2, float2>(ia_context *, int, int, const doubl
                                              long long, bool, int);
 template int copy2d_batched<float2, double2>(ia_context *, int, int, const float2 *, int, long long, double2 *, int,
                                              long long, bool, int);
+
+IA_BOUNDS_READER(bounds_read_dense)
 
 }  // namespace ia

@@ -13,6 +13,53 @@
 
 namespace ia {
 
+// ---- debug builds: bounds checks on global-memory indexes ------------------
+// Compiled with -DIA_DEBUG_BOUNDS (libia_debug.so), IA_IDX_OK(i, n) tests a
+// global index against its buffer's extent before the access; the kernels
+// skip an access whose test fails (a load then gives zero), and the first
+// failing site of the translation unit (source line, index, extent) and the
+// number of failures are recorded for ia_bounds_report().  A wrong index thus
+// shows up as a report, not as a fault of a shared GPU.  In release builds
+// IA_IDX_OK is the constant true and costs nothing.
+struct IaBoundsSite {
+    unsigned long long count;
+    long long index, extent;
+    int line, pad;
+};
+#ifdef IA_DEBUG_BOUNDS
+static __device__ IaBoundsSite ia_tu_bounds;   // one per translation unit
+__device__ __forceinline__ bool ia_idx_check(long long i, long long n, int line)
+{
+    if (i >= 0 && i < n) return true;
+    if (atomicAdd(&ia_tu_bounds.count, 1ull) == 0ull) {
+        ia_tu_bounds.index = i;
+        ia_tu_bounds.extent = n;
+        ia_tu_bounds.line = line;
+    }
+    return false;
+}
+#define IA_IDX_OK(i, n) (::ia::ia_idx_check((long long)(i), (long long)(n), __LINE__))
+// reads (and clears) this translation unit's record
+#define IA_BOUNDS_READER(fn)                                                                  \
+    int fn(IaBoundsSite *out)                                                                 \
+    {                                                                                         \
+        IaBoundsSite z{};                                                                     \
+        if (cudaMemcpyFromSymbol(out, ia_tu_bounds, sizeof(IaBoundsSite)) != cudaSuccess)    \
+            return IA_ERR_CUDA;                                                               \
+        if (cudaMemcpyToSymbol(ia_tu_bounds, &z, sizeof(IaBoundsSite)) != cudaSuccess)       \
+            return IA_ERR_CUDA;                                                               \
+        return IA_OK;                                                                         \
+    }
+#else
+#define IA_IDX_OK(i, n) true
+#define IA_BOUNDS_READER(fn)                                                                  \
+    int fn(IaBoundsSite *out)                                                                 \
+    {                                                                                         \
+        *out = IaBoundsSite{};                                                                \
+        return IA_OK;                                                                         \
+    }
+#endif
+
 struct z64 { double re, im; };
 
 __host__ __device__ __forceinline__ double2 zmake(double r, double i) { return make_double2(r, i); }

@@ -263,6 +263,13 @@ int esm_system(ia_context *ctx, int m, int l, const double *src, const double *m
 // df32: regular-element arithmetic in double-float (mixed path) instead of FP64;
 // split_ab (with df32): At and Bt are written as float4 (re hi, im hi, re lo, im lo)
 int mesh_creg(ia_context *ctx, ia_mesh *mesh);
+// debug builds: each instrumented translation unit's bounds record (read and cleared)
+struct IaBoundsSite;
+int bounds_read_dense(IaBoundsSite *out);
+int bounds_read_tc(IaBoundsSite *out);
+int bounds_read_svd(IaBoundsSite *out);
+int bounds_read_wide(IaBoundsSite *out);
+int bounds_read_asm(IaBoundsSite *out);
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
               bool df32 = false, bool split_ab = false);

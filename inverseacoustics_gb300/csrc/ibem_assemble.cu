@@ -376,6 +376,10 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
         const double s = rho * c * fb.k[f];
         const cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
         double2 *arow, *brow;
+        // the row's offset in its output (F x mt x m surface rows or F x l x m field rows)
+        const long long roff = row < mt ? ((long long)fg * mt + row) * m : ((long long)fg * l + (row - mt)) * m;
+        const long long rext = row < mt ? (long long)F * mt * m : (long long)F * l * m;
+        if (!IA_IDX_OK(roff + m - 1, rext)) continue;
         if (row < mt) {
             arow = At ? At + ((size_t)fg * mt + row) * m : nullptr;
             brow = Bt ? Bt + ((size_t)fg * mt + row) * m : nullptr;
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(IBEM_THREADS) creg_kernel(int m, int n, int nq
     ct = warp_sum(ct);
     if ((tid & 31) == 0) red[tid >> 5] = ct;
     __syncthreads();
-    if (tid == 0) {
+    if (tid == 0 && IA_IDX_OK(row, m)) {
         double tot = 0.0;
         for (int w = 0; w < IBEM_THREADS / 32; ++w) tot += red[w];
         creg[row] = tot;
@@ -476,5 +480,7 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
+
+IA_BOUNDS_READER(bounds_read_asm)
 
 }  // namespace ia

@@ -399,8 +399,10 @@ __global__ void __launch_bounds__(512)
     // columns of slot k at round r (k0 = 0 .. NP - 1)
     auto col_up = [&](int k, int r) { int c = r + k; return c >= NR ? c - NR : c; };
     auto col_lo = [&](int k, int r) { if (k == 0) return N2 - 1; int c = r - k; return c < 0 ? c + NR : c; };
+    const long long yext = (long long)M * N;
     auto load_col = [&](T *dst, int c) {
-        for (int i = threadIdx.x; i < M; i += blockDim.x) dst[i] = c < N ? Yg[(size_t)c * M + i] : zero;
+        for (int i = threadIdx.x; i < M; i += blockDim.x)
+            dst[i] = c < N && IA_IDX_OK((long long)c * M + i, yext) ? Yg[(size_t)c * M + i] : zero;
     };
     // round 0: slot k holds columns k and N2 - 1 - k (N2 - 1 in slot 0)
     for (int s = 0; s < P; ++s) {
@@ -536,8 +538,8 @@ __global__ void __launch_bounds__(512)
         const int cu = col_up(k, r), cl = col_lo(k, r);
         const T *pu = up + (size_t)eu * M, *pl = k == 0 ? fixc : lo + (size_t)el * M;
         for (int i = threadIdx.x; i < M; i += blockDim.x) {
-            if (cu < N) Yg[(size_t)cu * M + i] = pu[i];
-            if (cl < N) Yg[(size_t)cl * M + i] = pl[i];
+            if (cu < N && IA_IDX_OK((long long)cu * M + i, yext)) Yg[(size_t)cu * M + i] = pu[i];
+            if (cl < N && IA_IDX_OK((long long)cl * M + i, yext)) Yg[(size_t)cl * M + i] = pl[i];
         }
     }
     if (rank == 0 && threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
@@ -896,5 +898,7 @@ int svd_batched(ia_context *ctx, int m, int n, const double2 *A, bool transposed
     if (tall) return svd_finalize_batched(ctx, M, N, Y, Vacc, s, U, V, batch, info);
     return svd_finalize_batched(ctx, M, N, Y, Vacc, s, V, U, batch, info);
 }
+
+IA_BOUNDS_READER(bounds_read_svd)
 
 }  // namespace ia

@@ -264,6 +264,8 @@ __global__ void __launch_bounds__(SL1_THREADS, 2) tc_slice1_kernel(SliceOp<Src> 
     const int nr = R - r0 < SL1_RB ? R - r0 : SL1_RB;
     const Src *__restrict__ X = op.X + f * op.sX;
     const bool conj = op.conj != 0;
+    // extent of this entry's operand: K columns of ld (r-contiguous) or R rows of ld
+    const long long xext = op.rcontig ? (long long)op.ld * K : (long long)op.ld * R;
     if (op.rcontig) {
         // V(r, k) = X[r + k ld]: the CTA's rows of one k are 8 contiguous
         // values; a warp covers 4 values of k per step
@@ -274,7 +276,8 @@ __global__ void __launch_bounds__(SL1_THREADS, 2) tc_slice1_kernel(SliceOp<Src> 
             for (int u = 0; u < SL1_UNROLL; ++u) {
                 const int k = kb + kq + 4 * (SL1_THREADS / 32) * u;
                 v[u] = Src{};
-                if (r < nr && k < K) v[u] = load_conj(X, (size_t)(r0 + r) + (size_t)k * op.ld, conj);
+                if (r < nr && k < K && IA_IDX_OK((r0 + r) + (long long)k * op.ld, xext))
+                    v[u] = load_conj(X, (size_t)(r0 + r) + (size_t)k * op.ld, conj);
             }
 #pragma unroll
             for (int u = 0; u < SL1_UNROLL; ++u) {
@@ -291,7 +294,8 @@ __global__ void __launch_bounds__(SL1_THREADS, 2) tc_slice1_kernel(SliceOp<Src> 
             for (int u = 0; u < SL1_UNROLL; ++u) {
                 const int k = kb + 32 * u;
                 v[u] = Src{};
-                if (w < nr && k < K) v[u] = load_conj(xr, (size_t)k, conj);
+                if (w < nr && k < K && IA_IDX_OK((long long)(r0 + w) * op.ld + k, xext))
+                    v[u] = load_conj(xr, (size_t)k, conj);
             }
 #pragma unroll
             for (int u = 0; u < SL1_UNROLL; ++u) {
@@ -342,12 +346,14 @@ __global__ void __launch_bounds__(SL1_THREADS, 2) tc_slice1_kernel(SliceOp<Src> 
                 }
             }
             __nv_bfloat16 *P = planes + (size_t)s * pstride + 2 * (size_t)k;
+            const long long pext = (long long)S * pstride;   // this entry's planes
             if (!op.role_b) {
                 uint2 u;
                 u.x = bf2_bits(bf2(d[0], d[1]));
                 u.y = bf2_bits(bf2(d[2], d[3]));
-                *reinterpret_cast<uint2 *>(P + (size_t)row * Kp) = u;
-            } else {
+                if (IA_IDX_OK((long long)s * pstride + (long long)row * Kp + 2 * k + 3, pext))
+                    *reinterpret_cast<uint2 *>(P + (size_t)row * Kp) = u;
+            } else if (IA_IDX_OK((long long)s * pstride + (long long)(2 * row + 1) * Kp + 2 * k + 3, pext)) {
                 uint2 u0, u1;
                 u0.x = bf2_bits(bf2(d[0], -d[1]));
                 u0.y = bf2_bits(bf2(d[2], -d[3]));
@@ -663,6 +669,8 @@ int tc_gemm(ia_context *ctx, const TcPlanes &A, const TcPlanes &B, int M, int N,
     default: return IA_ERR_ARG;
     }
 }
+
+IA_BOUNDS_READER(bounds_read_tc)
 
 }  // namespace ia
 

@@ -262,9 +262,10 @@ __global__ void __launch_bounds__(QRC_THREADS) qr_cluster_kernel(int rows, int c
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = QRC_THREADS / 32;
     const float2 zero = make_float2(0.f, 0.f);
     A += f * sA;
+    const long long aext = (long long)cols * lda;
     for (int e = tid; e < nown * rows; e += QRC_THREADS) {
         const int c = e / rows, i = e % rows;
-        colbuf[e] = A[i + (size_t)(c0 + c) * lda];
+        colbuf[e] = IA_IDX_OK(i + (long long)(c0 + c) * lda, aext) ? A[i + (size_t)(c0 + c) * lda] : zero;
     }
     __syncthreads();
     for (int c = wid; c < nown; c += nw) {
@@ -450,7 +451,7 @@ __global__ void __launch_bounds__(QRC_THREADS) qr_cluster_kernel(int rows, int c
     cluster.sync();   // no CTA leaves while another may still read its shared memory
     for (int e = tid; e < nown * rows; e += QRC_THREADS) {
         const int c = e / rows, i = e % rows;
-        A[i + (size_t)(c0 + c) * lda] = colbuf[e];
+        if (IA_IDX_OK(i + (long long)(c0 + c) * lda, aext)) A[i + (size_t)(c0 + c) * lda] = colbuf[e];
     }
     if (perm)
         for (int c = tid; c < nown; c += QRC_THREADS) perm[(size_t)f * cols + c0 + c] = idx[c];
@@ -1508,5 +1509,7 @@ int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const dou
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
+
+IA_BOUNDS_READER(bounds_read_wide)
 
 }  // namespace ia

@@ -79,3 +79,12 @@ def test_bad_arguments_rejected_before_device_work():
         with pytest.raises(_lib.IAError) as e:
             api.hels(np.ones((3, 4)), np.ones((3, 4)), k, 2)
         assert e.value.code == 1
+
+
+def test_release_build_reports_bounds_checks_off():
+    """libia.so is the release build: ia_bounds_report answers enabled = 0 and
+    touches no device (the checks exist only in libia_debug.so)."""
+    L = _lib.lib()
+    en, cnt, fil, line, idx, ext = C.c_int(7), C.c_ulonglong(9), C.c_char_p(), C.c_int(), C.c_longlong(), C.c_longlong()
+    assert L.ia_bounds_report(C.byref(en), C.byref(cnt), C.byref(fil), C.byref(line), C.byref(idx), C.byref(ext)) == 0
+    assert (en.value, cnt.value, fil.value) == (0, 0, None)
