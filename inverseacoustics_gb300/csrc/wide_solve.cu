@@ -868,6 +868,13 @@ __global__ void __launch_bounds__(OA_THREADS) oa_update_kernel(int N, const doub
 // of memory latency per phase.  (Applied warp per pair, with the global-memory
 // updates in sequence while the other warps waited at the barrier, the kernel
 // stalled on barriers: 68 cycles per issue.)
+// Pairs whose two diagonal entries both lie below the Gram floor N eps
+// max|S_ii| (half of tol) do not rotate: eigenvalues there are not resolved
+// by a Gram matrix and are reported at the floor (eig_beta_kernel), so all
+// such components get the same filter factor and enter the solution only as
+// a subspace, which rotations inside it leave unchanged.  On operators
+// spanning many decades (an order-15 spherical-harmonic expansion at low kr)
+// that noise-level block holds most of the coupled pairs.
 constexpr int HJ_THREADS = 512;
 
 __device__ __forceinline__ void hj_pair(int N2, int round, int k, int &i, int &j)
@@ -917,6 +924,9 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
     }
     __syncthreads();
     const double tol = 2.0 * (double)N * 2.220446049250313e-16 * red[0];
+    const double floor2 = 0.5 * tol;
+    // N: diag(S) at the sweep's start, after rflag's N2 ints (N2 even: 8-byte aligned)
+    double *dg = reinterpret_cast<double *>(rflag + N2);
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         // every pair of the sweep checked at once (independent loads): only
@@ -924,6 +934,7 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
         // this sweep raise in skipped rounds are met by the next sweep's check,
         // and a converged S costs one pass instead of N2 - 1 serial rounds
         for (int r = tid; r < N2 - 1; r += blockDim.x) rflag[r] = 0;
+        for (int i = tid; i < N; i += blockDim.x) dg[i] = S[i + (size_t)i * N].x;
         if (tid == 0) {
             s_rot = 0;
             s_nact = 0;
@@ -934,6 +945,7 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
             int i, j;
             hj_pair(N2, round, k, i, j);
             if (j >= N) continue;
+            if (dg[i] < floor2 && dg[j] < floor2) continue;
             const double2 s = S[i + (size_t)j * N];
             if (sqrt(s.x * s.x + s.y * s.y) > tol) rflag[round] = 1;
         }
@@ -949,6 +961,7 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
                 const double g = sqrt(s.x * s.x + s.y * s.y);
                 if (!(g > tol)) continue;
                 const double a = S[i + (size_t)i * N].x, b = S[j + (size_t)j * N].x;
+                if (a < floor2 && b < floor2) continue;
                 const double zeta = (b - a) / (2.0 * g);
                 const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                 const double c = 1.0 / sqrt(1.0 + t * t);
@@ -1387,7 +1400,7 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     {
         const int P = (N + (N & 1)) / 2;
         const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
-                            sizeof(int) * (size_t)(2 * P);
+                            sizeof(int) * (size_t)(2 * P) + sizeof(double) * (size_t)N;
         const int sweeps = cfg->svd_max_sweeps < 16 ? cfg->svd_max_sweeps : 16;
         herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
         IA_LAUNCH_CHECK(ctx);

@@ -2,7 +2,7 @@
 (ncu launch lists and kernel captures); prints nothing but a checksum.  Same
 workloads and code paths as bench.py's timed steps.
 
-    python -m inverseacoustics_gb300.profile_step [--workload ibem|radiation|design|bemmodes|admm]
+    python -m inverseacoustics_gb300.profile_step [--workload ibem|radiation|design|bemmodes|admm|hels]
         [--precision mixed|fp64] [--reps 2] [--freqs 64] [--subdiv 3] [--admm-iters 50]
         [--complex-modes]
 
@@ -14,6 +14,8 @@ bemmodes: BEM radiation modes of the IBEM sphere, 32 modes of Re(G Z), or
 with --complex-modes of G Z itself (the C++ invr()).
 admm: L1 ADMM on the sphere's monopole transfer matrices (120 mics, 642
 sources), epsilon = 0: all 14 continuation stages of --admm-iters iterations.
+hels: the order-15 spherical-harmonic expansion on the 16 x 16 plane (256
+mics), expansion matrices and Tikhonov-GCV.
 """
 from __future__ import annotations
 
@@ -117,6 +119,21 @@ def _admm(a, dev, api, g):
     return float(out[0].abs().sum()), int(out[1].sum())
 
 
+def _hels(a, dev, api, g):
+    import torch
+    w = g.hels_plane(n_freq=a.freqs)
+    p = torch.as_tensor(g.hels_plane_pressures(w), device=dev)
+    pts = torch.as_tensor(np.ascontiguousarray(g.cartesian_to_spherical(w.arrays["mics"])), device=dev)
+    k = torch.as_tensor(w.k, device=dev)
+    ctx = api.Context(0)
+    cfg = api.default_config(precision=1 if a.precision == "mixed" else 0)
+    out = None
+    for _ in range(a.reps):
+        out = api.hels_solve_batch(ctx, pts, w.params["order"], k, p, cfg)
+    torch.cuda.synchronize()
+    return float(out[0].abs().sum()), int(out[3].abs().sum())
+
+
 def main():
     import torch
 
@@ -124,7 +141,7 @@ def main():
     from . import geometry as g
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="ibem", choices=["ibem", "radiation", "design", "bemmodes", "admm"])
+    ap.add_argument("--workload", default="ibem", choices=["ibem", "radiation", "design", "bemmodes", "admm", "hels"])
     ap.add_argument("--admm-iters", type=int, default=50, help="ADMM: Nm (iterations per continuation stage)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--reps", type=int, default=2)
@@ -133,10 +150,10 @@ def main():
     ap.add_argument("--complex-modes", action="store_true", help="bemmodes: modes of G Z instead of Re(G Z)")
     a = ap.parse_args()
     if a.freqs is None:
-        a.freqs = {"ibem": 64, "radiation": 256, "design": 128, "bemmodes": 16, "admm": 64}[a.workload]
+        a.freqs = {"ibem": 64, "radiation": 256, "design": 128, "bemmodes": 16, "admm": 64, "hels": 512}[a.workload]
     dev = torch.device("cuda:0")
     fn = {"ibem": _ibem, "radiation": _radiation, "design": _design, "bemmodes": _bemmodes,
-          "admm": _admm}[a.workload]
+          "admm": _admm, "hels": _hels}[a.workload]
     chk, info = fn(a, dev, api, g)
     print("checksum", chk, "info", info)
 
