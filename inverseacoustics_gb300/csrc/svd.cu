@@ -356,9 +356,10 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
     if (threadIdx.x == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
 }
 
-// The same iteration over a cluster of JC_CS CTAs per bin (FP32, no
-// accumulator), for latency: small batches and the last part of a staggered
-// pipeline, whose chain ends the pass.  CTA q owns the pair slots
+// The same iteration over a cluster of CS CTAs per bin (no accumulator).
+// FP32: for latency, in small batches and the last part of a staggered
+// pipeline, whose chain ends the pass.  FP64 (bound by the FP64 pipe of its
+// SM): whenever the batch leaves SMs idle, CS = 2 or 4 CTAs per bin.  CTA q owns the pair slots
 // [q P, (q + 1) P) of the circle ordering (P = N2 / 2 / JC_CS).  From one
 // round to the next the ordering moves every "upper" column (slot k holds
 // columns (r + k) and (r - k) mod (N2 - 1), column N2 - 1 fixed in slot 0)
@@ -372,9 +373,7 @@ __global__ void __launch_bounds__(sizeof(T) <= 8 ? 1024 : 512)
 // reductions, rotation and stopping rule; the sweep's rotation count and
 // largest coupling are combined over the cluster), so the factors are
 // bitwise the same.
-constexpr int JC_CS = 4;
-
-template <class T>
+template <class T, int JC_CS>
 __global__ void __launch_bounds__(512)
     jacobi_cluster_kernel(int M, int Mdot, int N, T *Yg, long long sY, int max_sweeps, typename ctraits<T>::R tol,
                           int *info)
@@ -736,32 +735,42 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
     // once in 32 warps; FP64: 16 warps, the 128-register budget), Y in shared
     // memory up to the per-CTA limit (an FP64 121 x 120 system fits)
     const size_t half_smem_max = sizeof(T) <= 8 ? 200 * 1024 : 227 * 1024 - 64;   // 16 B static besides
-    if constexpr (sizeof(T) == 8) {
-        // FP32 over a cluster per bin: for batches that leave most of the GPU
+    {
+        // over a cluster per bin: FP32 for batches that leave most of the GPU
         // idle and for the last part of a staggered pipeline (4x the SMs for
-        // ~1/3 of the time per bin; bitwise the one-CTA result)
+        // ~0.7x the time per bin); FP64 whenever 2 or 4 CTAs per bin fit on
+        // the SMs (the FP64 pipe of more SMs per bin).  Bitwise the one-CTA
+        // result either way.
         const int np = (N + (N & 1)) / 2;
-        if (!V && M <= 128 && N <= 128 && np % JC_CS == 0 && np / JC_CS >= 2 &&
-            (4 * JC_CS * batch <= ctx->sm_count || ctx->tail_part)) {
-            const int P = np / JC_CS;
+        int cs = 0;
+        if (!V && M <= 128 && N <= 128) {
+            if (sizeof(T) == 8) {
+                if (np % 4 == 0 && np / 4 >= 2 && (16 * batch <= ctx->sm_count || ctx->tail_part)) cs = 4;
+            } else {
+                for (int c : {4, 2})
+                    if (!cs && np % c == 0 && np / c >= 2 && c * batch <= ctx->sm_count) cs = c;
+            }
+        }
+        if (cs) {
+            const int P = np / cs;
             const size_t csm = sizeof(T) * ((size_t)2 * (P + 1) * M + M);
             const int nwc = (P + 1) / 2;
             cudaLaunchConfig_t lc = {};
-            lc.gridDim = dim3((unsigned)(JC_CS * batch));
+            lc.gridDim = dim3((unsigned)(cs * batch));
             lc.blockDim = dim3((unsigned)(32 * nwc));
             lc.dynamicSmemBytes = csm;
             lc.stream = ctx->stream;
             cudaLaunchAttribute at[1];
             at[0].id = cudaLaunchAttributeClusterDimension;
-            at[0].val.clusterDim.x = JC_CS;
+            at[0].val.clusterDim.x = cs;
             at[0].val.clusterDim.y = 1;
             at[0].val.clusterDim.z = 1;
             lc.attrs = at;
             lc.numAttrs = 1;
+            auto kern = cs == 4 ? jacobi_cluster_kernel<T, 4> : jacobi_cluster_kernel<T, 2>;
             if (csm > 48 * 1024)
-                IA_CUDA_TRY(cudaFuncSetAttribute(jacobi_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)csm));
-            IA_CUDA_TRY(cudaLaunchKernelEx(&lc, jacobi_cluster_kernel<T>, M, Mdot, N, Y, sY, max_sweeps, tol, info));
+                IA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+            IA_CUDA_TRY(cudaLaunchKernelEx(&lc, kern, M, Mdot, N, Y, sY, max_sweeps, tol, info));
             IA_LAUNCH_CHECK(ctx);
             return IA_OK;
         }
