@@ -263,6 +263,12 @@ int esm_system(ia_context *ctx, int m, int l, const double *src, const double *m
 // df32: regular-element arithmetic in double-float (mixed path) instead of FP64;
 // split_ab (with df32): At and Bt are written as float4 (re hi, im hi, re lo, im lo)
 int mesh_creg(ia_context *ctx, ia_mesh *mesh);
+// two-sided FP64 Jacobi eigensolver of batch Hermitian N x N matrices S (in
+// place, diagonalised), rotations accumulated into X (start it at the
+// identity for the eigenvectors), LAM <- diag(S), unsorted; IA_INFO_NOCONV at
+// the sweep cap
+int herm_jacobi_batched(ia_context *ctx, int N, double2 *S, double2 *X, double *LAM, int max_sweeps, int batch,
+                        int *info);
 // debug builds: each instrumented translation unit's bounds record (read and cleared)
 struct IaBoundsSite;
 int bounds_read_dense(IaBoundsSite *out);

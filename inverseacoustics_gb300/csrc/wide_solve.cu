@@ -1397,14 +1397,9 @@ static int gram_eig_mixed(ia_context *ctx, int m, int n, int batch, const double
     }
     if ((st = eg(OP_N, OP_N, N, N, N, 1.0, E, N, sN, X, N, sN, 0.0, T1, N, sN, batch))) return st;
     if ((st = eg(OP_C, OP_N, N, N, N, 1.0, X, N, sN, T1, N, sN, 0.0, Sm, N, sN, batch))) return st;
-    {
-        const int P = (N + (N & 1)) / 2;
-        const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
-                            sizeof(int) * (size_t)(2 * P) + sizeof(double) * (size_t)N;
-        const int sweeps = cfg->svd_max_sweeps < 16 ? cfg->svd_max_sweeps : 16;
-        herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, Sm, X, lam_e, sweeps, info);
-        IA_LAUNCH_CHECK(ctx);
-    }
+    if ((st = herm_jacobi_batched(ctx, N, Sm, X, lam_e, cfg->svd_max_sweeps < 16 ? cfg->svd_max_sweeps : 16, batch,
+                                  info)))
+        return st;
     unscale_eig_kernel<<<batch, 128, 0, ctx->stream>>>(N, lam_e, ex);
     IA_LAUNCH_CHECK(ctx);
     *Xout = X;
@@ -1489,6 +1484,20 @@ __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, i
             if (nu > 0 && den > 0.0 && bu / nu > 10.0 * (num / den)) info[f] |= IA_INFO_PRECISION;
         }
     }
+}
+
+int herm_jacobi_batched(ia_context *ctx, int N, double2 *S, double2 *X, double *LAM, int max_sweeps, int batch,
+                        int *info)
+{
+    const int P = (N + (N & 1)) / 2;
+    const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
+                        sizeof(int) * (size_t)(2 * P) + sizeof(double) * (size_t)N;
+    if (smem > 227 * 1024 - 512) return IA_ERR_TOO_LARGE;
+    if (smem > 48 * 1024)
+        IA_CUDA_TRY(cudaFuncSetAttribute(herm_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, S, X, LAM, max_sweeps, info);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
 }
 
 int wide_solve_mixed_batched(ia_context *ctx, int m, int n, int batch, const double2 *A, bool transposed, int nrhs,
