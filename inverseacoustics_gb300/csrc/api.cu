@@ -692,11 +692,7 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
 }
 
 // the FP64-level products of the mixed transfer run on the tensor cores
-static bool tc_products(const ia_config *cfg, int m)
-{
-    const int S = cfg->gemm_slices;
-    return S >= TC_SLICES_MIN && S <= TC_SLICES_MAX && (long long)S * 1024 * ((2 * m + 7) & ~7) <= (1ll << 24);
-}
+static bool tc_products(const ia_config *cfg, int m) { return tc_products_ok(cfg->gemm_slices, m); }
 
 static size_t transfer_mixed_ws_bytes(int m, int l, int F, const ia_config *cfg)
 {

@@ -328,6 +328,13 @@ static bool complex_mode_subspace(const ia_config *cfg, int m, int nm)
     return 2 * (long long)(nm + p) <= m;
 }
 
+// slices of the mixed Z solve's tensor-core products (0: double-float GEMMs)
+static int bem_slices(const ia_config *cfg)
+{
+    if (cfg->gemm_slices < TC_SLICES_MIN) return 0;
+    return cfg->gemm_slices < TC_SLICES_MAX ? cfg->gemm_slices + 1 : TC_SLICES_MAX;
+}
+
 size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, const ia_config *cfg, bool cplx)
 {
     const size_t M = mesh->m, MT = M + n_ch, L = l, FF = F;
@@ -342,14 +349,23 @@ size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, c
                  radiation_modes_ws_bytes(2 * mesh->m, F, c.nr, &c.cfg, true);
         }
     } else b += ws_round(8 * M * M * FF) + ws_round(8 * nm * FF) + radiation_modes_ws_bytes(mesh->m, F, nm, cfg, true);
-    if (bem_mixed_solve(cfg, n_ch)) b += 2 * ws_round(8 * M * M * FF) + ws_round(16 * M * M * FF);
+    if (bem_mixed_solve(cfg, n_ch)) {
+        b += 2 * ws_round(8 * M * M * FF) + ws_round(16 * M * M * FF);
+        if (tc_products_ok(bem_slices(cfg), mesh->m))
+            b += tc_planes_bytes(mesh->m > l ? mesh->m : l, mesh->m, bem_slices(cfg), false, F) +
+                 tc_planes_bytes(mesh->m, mesh->m, bem_slices(cfg), true, F) + 1024;
+    }
     return b + 4096;
 }
 
 // Mixed Z = A^-1 B and H = A_hs Z - B_hs: A and B arrive as double-float row
 // blocks (A^T, B^T as float4); FP32 LU of A and FP32 solves for Z, refined
-// with double-float residuals B - A Z (max(1, refine_steps) times); H by the
-// double-float GEMM.  On exit Z (FP64, m x m) is in At's storage.
+// with FP64-level residuals B - A Z (max(1, refine_steps) times); H =
+// A_hs Z - B_hs.  Both FP64-level products run on the tensor cores (BF16
+// slices, one more than cfg->gemm_slices: Z's error reaches the modes through
+// A's conditioning, which low kR makes large; A sliced once) or, with
+// gemm_slices 0, as double-float CUDA-core GEMMs.  On exit Z (FP64, m x m) is
+// in At's storage.
 static int bem_mixed_z(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int F, const double *k,
                        const ia_config *cfg, double2 *At, double2 *Bt, double2 *A, double2 *B, double2 *Ahs_t,
                        double2 *Bhs_t, double2 *Ahs, double2 *H, int *ipiv, int *info, WsCursor &cur)
@@ -376,16 +392,43 @@ static int bem_mixed_z(ia_context *ctx, const ia_mesh *mesh, int l, const double
     if ((st = copy2d_batched<float2, double2>(ctx, m, m, Z32, m, mm, Z, m, mm, false, F))) return st;
     const int steps = cfg->refine_steps > 1 ? cfg->refine_steps : 1;
     const size_t n4 = (size_t)mm * F;
+    const int S = bem_slices(cfg);
+    const bool tcg = tc_products_ok(S, m);
+    TcPlanes Pa{}, Pz{};
+    WsCursor ca{nullptr, 0, 0}, cz{nullptr, 0, 0};
+    if (tcg) {
+        // A's planes once (rows of A, then of A_hs in the same region), Z's per product
+        const size_t ba = tc_planes_bytes(m > l ? m : l, m, S, false, F), bz = tc_planes_bytes(m, m, S, true, F);
+        ca = WsCursor{(char *)cur.take<unsigned char>(ba), 0, ba};
+        cz = WsCursor{(char *)cur.take<unsigned char>(bz), 0, bz};
+        if (cur.off > cur.cap) return IA_ERR_ALLOC;
+        if ((st = tc_slice(ctx, false, OP_N, A4, m, mm, m, m, S, F, Pa, ca))) return st;
+    }
     for (int it = 0; it < steps; ++it) {
         df_join_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(n4, B4, R);
         IA_LAUNCH_CHECK(ctx);
-        if ((st = split_df_batched(ctx, n4, Z, Z4))) return st;
-        if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, m, m, -1.0, A4, m, mm, Z4, m, mm, 1.0, R, m, mm, F))) return st;
+        if (tcg) {
+            cz.off = 0;
+            if ((st = tc_slice(ctx, true, OP_N, Z, m, mm, m, m, S, F, Pz, cz))) return st;
+            if ((st = tc_gemm(ctx, Pa, Pz, m, m, -1.0, 1.0, R, m, mm, F, info))) return st;
+        } else {
+            if ((st = split_df_batched(ctx, n4, Z, Z4))) return st;
+            if ((st = dfgemm4_batched(ctx, OP_N, OP_N, m, m, m, -1.0, A4, m, mm, Z4, m, mm, 1.0, R, m, mm, F)))
+                return st;
+        }
         if ((st = copy2d_batched<double2, float2>(ctx, m, m, R, m, mm, Z32, m, mm, false, F))) return st;
         if ((st = getrs_batched<float2>(ctx, m, m, A32, m, mm, ipiv, Z32, m, mm, F))) return st;
         if ((st = add2d_batched<float2>(ctx, m, m, Z32, m, mm, Z, m, mm, F))) return st;
     }
-    // H = A_hs Z - B_hs (A_hs split into A_hs^T's storage)
+    // H = A_hs Z - B_hs
+    if (tcg) {
+        ca.off = 0;
+        cz.off = 0;
+        if ((st = tc_slice(ctx, false, OP_N, Ahs, l, ml, l, m, S, F, Pa, ca))) return st;
+        if ((st = tc_slice(ctx, true, OP_N, Z, m, mm, m, m, S, F, Pz, cz))) return st;
+        return tc_gemm(ctx, Pa, Pz, l, m, 1.0, -1.0, H, l, ml, F, info);
+    }
+    // (A_hs split into A_hs^T's storage)
     float4 *Ahs4 = reinterpret_cast<float4 *>(Ahs_t);
     if ((st = split_df_batched(ctx, n4, Z, Z4))) return st;
     if ((st = split_df_batched(ctx, (size_t)ml * F, Ahs, Ahs4))) return st;

@@ -185,6 +185,12 @@ struct TcPlanes {
     int R, rows, Kp, S; // R rows of op(A) (rows = R) or columns of op(B) (rows = 2 R)
 };
 size_t tc_planes_bytes(int R, int K, int S, bool role_b, int batch);
+// cfg->gemm_slices selects the sliced GEMM for an inner dimension K (a slice
+// count in range and exact FP32 level sums: S 1024 Kp <= 2^24)
+inline bool tc_products_ok(int S, int K)
+{
+    return S >= TC_SLICES_MIN && S <= TC_SLICES_MAX && (long long)S * 1024 * ((2 * K + 7) & ~7) <= (1ll << 24);
+}
 // role_b false: A (M x K) = op(X); true: B (K x N) = op(X); R = M or N
 int tc_slice(ia_context *ctx, bool role_b, Op op, const double2 *X, int ld, long long sX, int R, int K, int S,
              int batch, TcPlanes &out, WsCursor &cur);
