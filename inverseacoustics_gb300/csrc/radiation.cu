@@ -373,13 +373,64 @@ __global__ void __launch_bounds__(512) rform_q_kernel(int rows, int cols, const 
     }
 }
 
+// The same explicit factor over column groups: CTA (g, f) forms columns
+// [FQ_COLS g, FQ_COLS (g + 1)) of bin f's Q, a warp per column held in shared
+// memory; each reflector j (from the group's last column down to 0) is staged
+// in shared memory once and applied by every warp whose column c >= j.  The
+// operations per column are rform_q_kernel's, in the same order (bitwise the
+// same Q); a bin's columns spread over cols / FQ_COLS CTAs instead of one,
+// and a reflector is read from L2 once per CTA instead of once per warp.
+constexpr int FQ_COLS = 16;
+
+template <class T>
+__global__ void __launch_bounds__(32 * FQ_COLS) rform_q_group_kernel(int rows, int cols, const T *__restrict__ Y,
+                                                                     const T *__restrict__ tau, T *__restrict__ Q)
+{
+    extern __shared__ __align__(16) unsigned char fq_raw[];
+    T *qs = reinterpret_cast<T *>(fq_raw);   // FQ_COLS x rows: the group's columns
+    T *vs = qs + (size_t)FQ_COLS * rows;     // rows: the current reflector
+    const int f = blockIdx.y, c0 = blockIdx.x * FQ_COLS;
+    Y += (size_t)f * rows * cols;
+    tau += (size_t)f * cols;
+    Q += (size_t)f * rows * cols;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int c = c0 + wid;
+    T *q = qs + (size_t)wid * rows;
+    for (int i = lane; i < rows; i += 32) q[i] = i == c ? T(1) : T(0);
+    const int ctop = (c0 + FQ_COLS < cols ? c0 + FQ_COLS : cols) - 1;
+    for (int j = ctop < rows - 1 ? ctop : rows - 1; j >= 0; --j) {
+        __syncthreads();   // every warp is done with the previous reflector
+        for (int i = j + 1 + (int)threadIdx.x; i < rows; i += blockDim.x) vs[i] = Y[i + (size_t)j * rows];
+        __syncthreads();
+        const T t = tau[j];
+        if (t == 0 || c >= cols || j > c) continue;   // H_j leaves e_c alone for j > c
+        T acc = lane == 0 ? q[j] : T(0);
+        for (int i = j + 1 + lane; i < rows; i += 32) acc = fma(vs[i], q[i], acc);
+        acc = warp_sum(acc) * t;
+        if (lane == 0) q[j] -= acc;
+        for (int i = j + 1 + lane; i < rows; i += 32) q[i] = fma(-vs[i], acc, q[i]);
+    }
+    __syncwarp();
+    if (c < cols)
+        for (int i = lane; i < rows; i += 32) Q[i + (size_t)c * rows] = q[i];
+}
+
 // Q = orth(Y): QR of Y in place, then the explicit thin factor into Q
 template <class T>
 static int orthonormalise(ia_context *ctx, int rows, int cols, T *Y, T *tau, T *Q, int batch)
 {
     rqr_kernel<T><<<batch, RQR_THREADS, 0, ctx->stream>>>(rows, cols, Y, tau);
     IA_LAUNCH_CHECK(ctx);
-    rform_q_kernel<T><<<batch, 512, 0, ctx->stream>>>(rows, cols, Y, tau, Q);
+    const size_t fsm = sizeof(T) * (size_t)(FQ_COLS + 1) * rows;
+    if (fsm <= 200 * 1024) {
+        if (fsm > 48 * 1024)
+            IA_CUDA_TRY(cudaFuncSetAttribute(rform_q_group_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fsm));
+        dim3 g((cols + FQ_COLS - 1) / FQ_COLS, batch);
+        rform_q_group_kernel<T><<<g, 32 * FQ_COLS, fsm, ctx->stream>>>(rows, cols, Y, tau, Q);
+    } else {
+        rform_q_kernel<T><<<batch, 512, 0, ctx->stream>>>(rows, cols, Y, tau, Q);
+    }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
