@@ -19,6 +19,7 @@
 // mixed path the iterations run in FP32 and are followed by FP64 power steps
 // whose products use double-float arithmetic on the FP32 pipe.
 #include "df32.cuh"
+#include <cooperative_groups.h>
 #include "ia_common.cuh"
 #include "ia_internal.h"
 
@@ -373,6 +374,124 @@ __global__ void __launch_bounds__(512) rform_q_kernel(int rows, int cols, const 
     }
 }
 
+// The same QR over a cluster of CS CTAs per bin: CTA r owns columns
+// [r cw, (r + 1) cw) in shared memory; per step the owner of column j forms the
+// reflector and publishes it with tau (double-buffered by step parity), and
+// after one cluster barrier every CTA copies it and updates its own columns
+// > j.  rqr_kernel's arithmetic in the same order (512 threads, the same
+// reductions): bitwise the same factors, with the trailing updates of a bin
+// on CS SMs and in shared memory instead of on one SM from L2.
+template <class T, int CS>
+__global__ void __launch_bounds__(RQR_THREADS) rqr_cluster_kernel(int rows, int cols, T *A, T *tau)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int f = blockIdx.x / CS;
+    const int cw = (cols + CS - 1) / CS, c0 = rank * cw;
+    const int nown = cols - c0 < cw ? (cols - c0 > 0 ? cols - c0 : 0) : cw;
+    extern __shared__ __align__(16) unsigned char rqc_raw[];
+    T *colbuf = reinterpret_cast<T *>(rqc_raw);   // cw x rows: this CTA's columns
+    T *xs = colbuf + (size_t)cw * rows;           // 2 x rows: the reflector, by step parity
+    __shared__ T red[RQR_THREADS / 32];
+    __shared__ T s_tau[2];
+    __shared__ T s_scale;
+    A += (size_t)f * rows * cols;
+    tau += (size_t)f * cols;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = RQR_THREADS / 32;
+    for (int e = tid; e < nown * rows; e += RQR_THREADS) colbuf[e] = A[(size_t)c0 * rows + e];
+    __syncthreads();
+    const int steps = cols < rows ? cols : rows;
+    for (int j = 0; j < steps; ++j) {
+        const int oj = j / cw, par = j & 1, len = rows - j;
+        T *xb = xs + (size_t)par * rows;
+        if (rank == oj) {
+            T *x = colbuf + (size_t)(j - c0) * rows + j;
+            T sg = 0;
+            for (int i = 1 + tid; i < len; i += RQR_THREADS) sg = fma(x[i], x[i], sg);
+            sg = warp_sum(sg);
+            if (lane == 0) red[wid] = sg;
+            __syncthreads();
+            if (tid == 0) {
+                T sigma = 0;
+                for (int w = 0; w < nw; ++w) sigma += red[w];
+                const T alpha = x[0];
+                if (sigma == 0) {
+                    s_tau[par] = 0;
+                    s_scale = 0;
+                } else {
+                    const T nrm = sqrt(alpha * alpha + sigma);
+                    const T beta = alpha >= 0 ? -nrm : nrm;
+                    s_tau[par] = (beta - alpha) / beta;
+                    s_scale = T(1) / (alpha - beta);
+                    x[0] = beta;
+                }
+                tau[j] = s_tau[par];
+            }
+            __syncthreads();
+            if (s_tau[par] != 0) {
+                const T sc = s_scale;
+                for (int i = 1 + tid; i < len; i += RQR_THREADS) {
+                    const T v = x[i] * sc;
+                    x[i] = v;
+                    xb[j + i] = v;
+                }
+            }
+        }
+        cluster.sync();
+        const T tv = *cluster.map_shared_rank(&s_tau[par], oj);
+        if (tv != 0) {
+            if (rank != oj) {
+                const T *ox = cluster.map_shared_rank(xb, oj);
+                for (int i = j + 1 + tid; i < rows; i += RQR_THREADS) xb[i] = ox[i];
+            }
+            __syncthreads();
+            const T *x = xb + j;   // x[0] = 1 implicitly
+            for (int cl = wid; cl < nown; cl += nw) {
+                if (c0 + cl <= j) continue;
+                T *col = colbuf + (size_t)cl * rows + j;
+                T w = lane == 0 ? col[0] : T(0);
+                for (int i = 1 + lane; i < len; i += 32) w = fma(x[i], col[i], w);
+                w = warp_sum(w) * tv;
+                if (lane == 0) col[0] -= w;
+                for (int i = 1 + lane; i < len; i += 32) col[i] = fma(-x[i], w, col[i]);
+            }
+        }
+        __syncthreads();
+    }
+    cluster.sync();   // no CTA leaves while another may read its reflector or tau
+    for (int e = tid; e < nown * rows; e += RQR_THREADS) A[(size_t)c0 * rows + e] = colbuf[e];
+}
+
+template <class T, int CS>
+static bool rqr_cluster_launch(ia_context *ctx, int rows, int cols, T *Y, T *tau, int batch, int &st)
+{
+    const int cw = (cols + CS - 1) / CS;
+    const size_t smem = sizeof(T) * ((size_t)cw * rows + 2 * (size_t)rows);
+    if (cw < 1 || smem > 200 * 1024 || CS * batch > ctx->sm_count) return false;
+    st = IA_OK;
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024)
+        e = cudaFuncSetAttribute(rqr_cluster_kernel<T, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3((unsigned)(CS * batch));
+        lc.blockDim = dim3(RQR_THREADS);
+        lc.dynamicSmemBytes = smem;
+        lc.stream = ctx->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = CS;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        e = cudaLaunchKernelEx(&lc, rqr_cluster_kernel<T, CS>, rows, cols, Y, tau);
+    }
+    if (e != cudaSuccess) st = cuda_status(e);
+    return true;
+}
+
 // The same explicit factor over column groups: CTA (g, f) forms columns
 // [FQ_COLS g, FQ_COLS (g + 1)) of bin f's Q, a warp per column held in shared
 // memory; each reflector j (from the group's last column down to 0) is staged
@@ -419,7 +538,15 @@ __global__ void __launch_bounds__(32 * FQ_COLS) rform_q_group_kernel(int rows, i
 template <class T>
 static int orthonormalise(ia_context *ctx, int rows, int cols, T *Y, T *tau, T *Q, int batch)
 {
-    rqr_kernel<T><<<batch, RQR_THREADS, 0, ctx->stream>>>(rows, cols, Y, tau);
+    // the QR: over a cluster of 8, 4 or 2 CTAs per bin (the largest that
+    // fits on the SMs with its column share in shared memory), else one CTA
+    // per bin
+    int st = IA_OK;
+    if (!(rqr_cluster_launch<T, 8>(ctx, rows, cols, Y, tau, batch, st) ||
+          rqr_cluster_launch<T, 4>(ctx, rows, cols, Y, tau, batch, st) ||
+          rqr_cluster_launch<T, 2>(ctx, rows, cols, Y, tau, batch, st)))
+        rqr_kernel<T><<<batch, RQR_THREADS, 0, ctx->stream>>>(rows, cols, Y, tau);
+    if (st) return st;
     IA_LAUNCH_CHECK(ctx);
     const size_t fsm = sizeof(T) * (size_t)(FQ_COLS + 1) * rows;
     if (fsm <= 200 * 1024) {
