@@ -166,6 +166,23 @@ def test_solve_batch_matches_oracle(cuda, ctx, mode):
         assert relerr(x[f, 0].cpu().numpy(), xo) < (TOL if mode == "standard" else 1e-6)
 
 
+def test_solve_batch_cluster_jacobi_is_bitwise_the_one_cta_kernel(cuda, ctx):
+    """The FP64 one-sided Jacobi runs over a 4-CTA cluster per bin when the
+    clusters fit on the SMs (8 bins) and one CTA per bin otherwise (80 bins):
+    the same rotations in the same order, so the first 8 bins of the 80-bin
+    call equal the 8-bin call bit for bit (x, lambda, s)."""
+    from inverseacoustics_gb300 import api
+    import torch
+    _, _, _, Hs, bs = _gcv_problem(23, 64, 162, 80)
+    Hc = T(np.stack([h.T for h in Hs]), cuda)
+    b = T(np.stack([bb[None, :] for bb in bs]), cuda)
+    x, lam, s, info = api.solve_batch(ctx, Hc, 64, 162, b)
+    x8, lam8, s8, info8 = api.solve_batch(ctx, Hc[:8].contiguous(), 64, 162, b[:8].contiguous())
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0 and int(info8.abs().sum()) == 0
+    assert torch.equal(x[:8], x8) and torch.equal(lam[:8], lam8) and torch.equal(s[:8], s8)
+
+
 def test_esm_pipeline_single_frequency(cuda, ctx):
     """Config 'ESM plain, single frequency' end to end: monopole G, SVD,
     GCV over 200 log-spaced lambda in [1e-8, 1e2], Tikhonov."""
