@@ -738,10 +738,9 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
         // over a cluster per bin: FP32 for batches that leave most of the GPU
         // idle and for the last part of a staggered pipeline (4x the SMs for
         // ~0.7x the time per bin); FP64 whenever 2 or 4 CTAs per bin fit on
-        // the SMs (the FP64 pipe of more SMs per bin).  Systems of 129-192 rows
-        // (12 rows per lane) take 8-CTA clusters in as many waves as needed:
-        // their alternative is the one-CTA kernel on global memory.  Bitwise
-        // the one-CTA result either way.
+        // the SMs (the FP64 pipe of more SMs per bin).  Systems of 129-272 rows
+        // (12 or 17 rows per lane) take 8-CTA clusters in as many waves as
+        // needed: their alternative is a one-CTA kernel on global memory.
         const int np = (N + (N & 1)) / 2;
         int cs = 0, kpl = 8;
         if (!V && M <= 128 && N <= 128) {
@@ -751,9 +750,9 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
                 for (int c : {4, 2})
                     if (!cs && np % c == 0 && np / c >= 2 && c * batch <= ctx->sm_count) cs = c;
             }
-        } else if (!V && M <= 192 && N <= 192 && M > 128 && np % 8 == 0 && np / 8 >= 2) {
+        } else if (!V && M <= 272 && N <= 272 && M > 128 && np % 8 == 0 && np / 8 >= 2) {
             cs = 8;
-            kpl = 12;
+            kpl = M <= 192 ? 12 : 17;
         }
         if (cs) {
             const int P = np / cs;
@@ -771,8 +770,9 @@ int jacobi_rows_batched(ia_context *ctx, int M, int Mdot, int N, T *Y, T *V, int
             at[0].val.clusterDim.z = 1;
             lc.attrs = at;
             lc.numAttrs = 1;
-            auto kern = kpl == 12 ? jacobi_cluster_kernel<T, 8, 12>
-                                  : (cs == 4 ? jacobi_cluster_kernel<T, 4> : jacobi_cluster_kernel<T, 2>);
+            auto kern = kpl == 17   ? jacobi_cluster_kernel<T, 8, 17>
+                        : kpl == 12 ? jacobi_cluster_kernel<T, 8, 12>
+                        : (cs == 4 ? jacobi_cluster_kernel<T, 4> : jacobi_cluster_kernel<T, 2>);
             if (csm > 48 * 1024)
                 IA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
             IA_CUDA_TRY(cudaLaunchKernelEx(&lc, kern, M, Mdot, N, Y, sY, max_sweeps, tol, info));
