@@ -517,12 +517,18 @@ template <int RB, int NT, bool FULL>
 __device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int lda, long long text, float2 *X, int xs,
                                              int k0, int nb, int lo, int hi)
 {
-    constexpr int TH = LU_NB / 2;   // the row's entries in two halves (register budget: two CTAs per SM)
-    for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
+    // the row's entries in two halves (register budget: two CTAs per SM);
+    // two threads per row, each with half of the right-hand sides (twice the
+    // warps to hide the row loads' L2 latency: 25.9 -> 25.75 ms per pass)
+    constexpr int TH = LU_NB / 2;
+    constexpr int SPLIT = 2, RBT = RB / SPLIT, NR = NT / SPLIT;
+    const int cbase = ((int)threadIdx.x / NR) * RBT;
+    X += (size_t)cbase * xs;
+    for (int i = lo + (int)threadIdx.x % NR; i < hi; i += NR) {
         const float2 *tp = T + i;
-        float2 acc[RB];
+        float2 acc[RBT];
 #pragma unroll
-        for (int c = 0; c < RB; ++c) acc[c] = X[i + (size_t)c * xs];
+        for (int c = 0; c < RBT; ++c) acc[c] = X[i + (size_t)c * xs];
 #pragma unroll
         for (int h = 0; h < LU_NB; h += TH) {
             float2 trow[TH];
@@ -535,7 +541,7 @@ __device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int l
             for (int t = 0; t < TH; t += 2) {
                 if (FULL || h + t < nb) {
 #pragma unroll
-                    for (int c = 0; c < RB; ++c) {
+                    for (int c = 0; c < RBT; ++c) {
                         // X(k0 + h + t, c) and the entry below: k0, h, t and xs even
                         const float4 x2 = *reinterpret_cast<const float4 *>(X + k0 + h + t + (size_t)c * xs);
                         zfms(acc[c], trow[t], make_float2(x2.x, x2.y));
@@ -545,7 +551,7 @@ __device__ __forceinline__ void getrs_update(const float2 *__restrict__ T, int l
             }
         }
 #pragma unroll
-        for (int c = 0; c < RB; ++c) X[i + (size_t)c * xs] = acc[c];
+        for (int c = 0; c < RBT; ++c) X[i + (size_t)c * xs] = acc[c];
     }
 }
 
@@ -672,9 +678,9 @@ int getrs_batched(ia_context *ctx, int n, int nrhs, const T *LU, int lda, long l
         // 64-bin pass 28.4 against 28.0 ms)
         constexpr int rb = 8;
         const size_t smem = getrs_fused_smem(n, rb);
-        // a warp per right-hand side (512 threads, the rows split further,
-        // measured slower: 29.1 vs 28.2 ms per 64-bin pass)
-        constexpr int nt = 32 * rb;
+        // 512 threads: a warp per right-hand side in the diagonal solves, two
+        // threads per row in the updates
+        constexpr int nt = 64 * rb;
         if (smem <= 200 * 1024) {
             auto kern = getrs_fused_kernel<rb, nt>;
             if (smem > 48 * 1024)
