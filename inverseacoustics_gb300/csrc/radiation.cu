@@ -636,6 +636,179 @@ __global__ void eye_c_kernel(int b, double2 *__restrict__ X, int batch)
     }
 }
 
+// Two-sided Jacobi eigensolver of the real symmetric b x b Rayleigh-Ritz
+// matrix B (symmetrised), one CTA per bin: herm_jacobi_kernel's sweeps
+// (every pair checked at once, only rounds holding a pair above tol = 2 N eps
+// max|S_ii| run, pairs with both diagonal entries below the floor N eps
+// max|S_ii| skipped, Rutishauser's stable rotation, a round's rotations
+// applied to columns then rows over the whole CTA) in real arithmetic, with S
+// in shared memory and the eigenvectors accumulated into X (global) from the
+// identity; LAM <- diag(S), unsorted.
+constexpr int RJ_THREADS = 512;
+
+// round-robin (circle) ordering: pair k of round `round` over N2 (even) slots
+__device__ __forceinline__ void rr_pair_r(int N2, int round, int k, int &i, int &j)
+{
+    if (k == 0) {
+        i = round;
+        j = N2 - 1;
+    } else {
+        i = round + k;
+        if (i >= N2 - 1) i -= N2 - 1;
+        j = round - k + N2 - 1;
+        if (j >= N2 - 1) j -= N2 - 1;
+    }
+    if (i > j) {
+        const int t = i;
+        i = j;
+        j = t;
+    }
+}
+
+__global__ void __launch_bounds__(RJ_THREADS) rsym_jacobi_kernel(int N, const double *__restrict__ B,
+                                                                 double *__restrict__ X, double *__restrict__ LAM,
+                                                                 int max_sweeps, int *__restrict__ info)
+{
+    extern __shared__ __align__(16) double rj_sm[];
+    const int N2 = N + (N & 1), P = N2 / 2;
+    double *S = rj_sm;                                   // N x N
+    double *cs = S + (size_t)N * N;                      // P
+    double *sp = cs + P;                                 // P
+    double *dg = sp + P;                                 // N: diag(S) at the sweep's start
+    int *pi = reinterpret_cast<int *>(dg + N);           // P
+    int *pj = pi + P;                                    // P
+    int *rflag = pj + P;                                 // N2 - 1
+    __shared__ double red[RJ_THREADS / 32];
+    __shared__ int s_rot, s_nact;
+    const int f = blockIdx.x;
+    B += (size_t)f * N * N;
+    X += (size_t)f * N * N;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    for (int e = tid; e < N * N; e += blockDim.x) {
+        const int i = e % N, j = e / N;
+        S[e] = 0.5 * (B[e] + B[j + (size_t)i * N]);
+        X[e] = i == j ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    double lm = 0.0;
+    for (int i = tid; i < N; i += blockDim.x) lm = fmax(lm, fabs(S[i + (size_t)i * N]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    if (lane == 0) red[wid] = lm;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t = fmax(t, red[w]);
+        red[0] = t;
+    }
+    __syncthreads();
+    const double tol = 2.0 * (double)N * 2.220446049250313e-16 * red[0], floor2 = 0.5 * tol;
+    int sweep = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        for (int r = tid; r < N2 - 1; r += blockDim.x) rflag[r] = 0;
+        for (int i = tid; i < N; i += blockDim.x) dg[i] = S[i + (size_t)i * N];
+        if (tid == 0) {
+            s_rot = 0;
+            s_nact = 0;
+        }
+        __syncthreads();
+        for (int e = tid; e < (N2 - 1) * P; e += blockDim.x) {
+            const int round = e / P, k = e - round * P;
+            int i, j;
+            rr_pair_r(N2, round, k, i, j);
+            if (j >= N || (dg[i] < floor2 && dg[j] < floor2)) continue;
+            if (fabs(S[i + (size_t)j * N]) > tol) rflag[round] = 1;
+        }
+        __syncthreads();
+        for (int round = 0; round < N2 - 1; ++round) {
+            if (!rflag[round]) continue;
+            int mine = 0;
+            for (int k = tid; k < P; k += blockDim.x) {
+                int i, j;
+                rr_pair_r(N2, round, k, i, j);
+                if (j >= N) continue;
+                const double g0 = S[i + (size_t)j * N], g = fabs(g0);
+                if (!(g > tol)) continue;
+                const double a = S[i + (size_t)i * N], b = S[j + (size_t)j * N];
+                if (a < floor2 && b < floor2) continue;
+                const double zeta = (b - a) / (2.0 * g);
+                const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t);
+                const int slot = atomicAdd(&s_nact, 1);
+                cs[slot] = c;
+                sp[slot] = t * c * g0 / g;
+                pi[slot] = i;
+                pj[slot] = j;
+                ++mine;
+            }
+            if (mine) atomicAdd(&s_rot, mine);
+            if (!__syncthreads_or(mine)) continue;
+            const int nact = s_nact;
+            // columns of S and X: [u v] <- [u v] G
+            for (int e = tid; e < nact * 2 * N; e += blockDim.x) {
+                const int q = e / (2 * N), rem = e - q * 2 * N, mat = rem / N, r = rem - mat * N;
+                const int i = pi[q], j = pj[q];
+                const double c = cs[q], w = sp[q];
+                double *M = mat == 0 ? S : X;
+                double *ci = M + (size_t)i * N, *cj = M + (size_t)j * N;
+                const double u = ci[r], v = cj[r];
+                ci[r] = c * u - w * v;
+                cj[r] = c * v + w * u;
+            }
+            __syncthreads();
+            if (tid == 0) s_nact = 0;
+            // rows of S: [u; v] <- G^T [u; v]
+            for (int e = tid; e < nact * N; e += blockDim.x) {
+                const int q = e / N, col = e - q * N;
+                const int i = pi[q], j = pj[q];
+                const double c = cs[q], w = sp[q];
+                double *a = S + i + (size_t)col * N, *b = S + j + (size_t)col * N;
+                const double u = *a, v = *b;
+                *a = c * u - w * v;
+                *b = c * v + w * u;
+            }
+            __syncthreads();
+        }
+        const int total = s_rot;
+        __syncthreads();
+        if (total == 0) break;
+    }
+    if (tid == 0 && sweep >= max_sweeps && info) atomicOr(&info[f], IA_INFO_NOCONV);
+    for (int i = tid; i < N; i += blockDim.x) LAM[(size_t)f * N + i] = S[i + (size_t)i * N];
+}
+
+static size_t rsym_jacobi_smem(int N)
+{
+    const int N2 = N + (N & 1), P = N2 / 2;
+    return sizeof(double) * ((size_t)N * N + 2 * (size_t)P + N) + sizeof(int) * (2 * (size_t)P + N2);
+}
+
+// V (complex, zero imaginary parts) <- the columns of the real X ordered by
+// decreasing eigenvalue lam (ties by index), one CTA per bin
+__global__ void sort_eig_real_kernel(int b, const double *__restrict__ lam, const double *__restrict__ X,
+                                     double2 *__restrict__ V)
+{
+    extern __shared__ int ser_rank[];
+    const int f = blockIdx.x;
+    lam += (size_t)f * b;
+    X += (size_t)f * b * b;
+    V += (size_t)f * b * b;
+    for (int i = threadIdx.x; i < b; i += blockDim.x) {
+        const double li = lam[i];
+        int rk = 0;
+        for (int j = 0; j < b; ++j) {
+            const double lj = lam[j];
+            if (lj > li || (lj == li && j < i)) ++rk;
+        }
+        ser_rank[i] = rk;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+        const int i = e / b, r = e - i * b;
+        V[r + (size_t)ser_rank[i] * b] = make_double2(X[e], 0.0);
+    }
+}
+
 // V <- the columns of X ordered by decreasing eigenvalue lam (ties by index),
 // one CTA per bin
 __global__ void sort_eig_kernel(int b, const double *__restrict__ lam, const double2 *__restrict__ X,
@@ -795,17 +968,30 @@ int radiation_modes_batched(ia_context *ctx, int n, int F, const double *R, int 
     // Rayleigh-Ritz: B = Q^T op Q, eigenpairs of B, modes = Q W
     if ((st = apply64(Q, Y2))) return st;
     if ((st = prod64(ctx, mixed, OP_T, b, b, n, Q, n, nb, Y2, n, nb, B, b, bb, F))) return st;
-    sym_complex_kernel<<<blocks, 256, 0, ctx->stream>>>(b, B, Bc, F);
-    IA_LAUNCH_CHECK(ctx);
     // eigenpairs of the symmetric (positive semidefinite) B by the two-sided
     // FP64 Jacobi, eigenvectors accumulated from the identity, then ordered by
     // decreasing eigenvalue (was: a one-sided complex Jacobi SVD with a
-    // rotation accumulator, 28.8 of 55.8 ms for the 16-bin BEM modes)
-    eye_c_kernel<<<blocks, 256, 0, ctx->stream>>>(b, Ysvd, F);
-    IA_LAUNCH_CHECK(ctx);
-    if ((st = herm_jacobi_batched(ctx, b, Bc, Ysvd, s, 16, F, info))) return st;
-    sort_eig_kernel<<<F, 256, sizeof(int) * (size_t)b, ctx->stream>>>(b, s, Ysvd, Vc);
-    IA_LAUNCH_CHECK(ctx);
+    // rotation accumulator, 28.8 of 55.8 ms for the 16-bin BEM modes): in real
+    // arithmetic with B in shared memory when it fits, else the complex
+    // Hermitian kernel on a copy
+    const size_t rjs = rsym_jacobi_smem(b);
+    if (rjs <= 200 * 1024) {
+        double *Xr = reinterpret_cast<double *>(Ysvd);
+        if (rjs > 48 * 1024)
+            IA_CUDA_TRY(cudaFuncSetAttribute(rsym_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rjs));
+        rsym_jacobi_kernel<<<F, RJ_THREADS, rjs, ctx->stream>>>(b, B, Xr, s, 16, info);
+        IA_LAUNCH_CHECK(ctx);
+        sort_eig_real_kernel<<<F, 256, sizeof(int) * (size_t)b, ctx->stream>>>(b, s, Xr, Vc);
+        IA_LAUNCH_CHECK(ctx);
+    } else {
+        sym_complex_kernel<<<blocks, 256, 0, ctx->stream>>>(b, B, Bc, F);
+        IA_LAUNCH_CHECK(ctx);
+        eye_c_kernel<<<blocks, 256, 0, ctx->stream>>>(b, Ysvd, F);
+        IA_LAUNCH_CHECK(ctx);
+        if ((st = herm_jacobi_batched(ctx, b, Bc, Ysvd, s, 16, F, info))) return st;
+        sort_eig_kernel<<<F, 256, sizeof(int) * (size_t)b, ctx->stream>>>(b, s, Ysvd, Vc);
+        IA_LAUNCH_CHECK(ctx);
+    }
     (void)Vacc;
     ritz_kernel<<<F, 256, 0, ctx->stream>>>(b, nm, B, Vc, lambda, Wr);
     IA_LAUNCH_CHECK(ctx);
