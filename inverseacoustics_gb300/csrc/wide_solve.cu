@@ -894,23 +894,36 @@ __device__ __forceinline__ void hj_pair(int N2, int round, int k, int &i, int &j
     if (i > j) { int t = i; i = j; j = t; }
 }
 
-__global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 *S, double2 *X, double *LAM,
+// SM: S (N <= 120) held in shared memory for the whole run, read from
+// global memory once (its final state is not needed: LAM and X are the
+// results); the pair slots and round flags then take 16- and 8-bit types and
+// the diagonal is read from S directly, so that S fits beside them.
+template <bool SM>
+__global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 *Sg, double2 *X, double *LAM,
                                                                   int max_sweeps, int *info)
 {
+    typedef typename std::conditional<SM, unsigned short, int>::type PIdx;
+    typedef typename std::conditional<SM, unsigned char, int>::type RFlag;
     extern __shared__ __align__(16) double hj_sm[];
     const int N2 = N + (N & 1), P = N2 / 2;
-    double *cs = hj_sm;                                   // P
-    double2 *se = reinterpret_cast<double2 *>(hj_sm + P + (P & 1));   // P, 16-byte aligned
-    int *pi = reinterpret_cast<int *>(se + P);            // P
-    int *pj = pi + P;                                     // P
-    int *rflag = pj + P;                                  // N2 - 1: rounds with a coupled pair
+    double2 *S = SM ? reinterpret_cast<double2 *>(hj_sm) : Sg;          // SM: N x N
+    double *cs = hj_sm + (SM ? 2 * (size_t)N * N : 0);   // P
+    double2 *se = reinterpret_cast<double2 *>(cs + P + (P & 1));   // P, 16-byte aligned
+    PIdx *pi = reinterpret_cast<PIdx *>(se + P);          // P
+    PIdx *pj = pi + P;                                    // P
+    RFlag *rflag = reinterpret_cast<RFlag *>(pj + P);     // N2 - 1: rounds with a coupled pair
     __shared__ double red[HJ_THREADS / 32];
     __shared__ int s_rot;
     __shared__ int s_nact;   // rotating pairs of the current round (cs, se, pi, pj slots)
     const int f = blockIdx.x;
-    S += (size_t)f * N * N;
+    Sg += (size_t)f * N * N;
+    if (!SM) S = Sg;
     X += (size_t)f * N * N;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    if (SM) {
+        for (int e = tid; e < N * N; e += blockDim.x) S[e] = Sg[e];
+        __syncthreads();
+    }
     double lm = 0.0;
     for (int i = tid; i < N; i += blockDim.x) lm = fmax(lm, fabs(S[i + (size_t)i * N].x));
 #pragma unroll
@@ -925,8 +938,10 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
     __syncthreads();
     const double tol = 2.0 * (double)N * 2.220446049250313e-16 * red[0];
     const double floor2 = 0.5 * tol;
-    // N: diag(S) at the sweep's start, after rflag's N2 ints (N2 even: 8-byte aligned)
-    double *dg = reinterpret_cast<double *>(rflag + N2);
+    // N: diag(S) at the sweep's start, after rflag's N2 ints (N2 even: 8-byte
+    // aligned); with S in shared memory the diagonal is read from S
+    double *dg = SM ? nullptr : reinterpret_cast<double *>(rflag + N2);
+    auto diag = [&](int i) { return SM ? S[i + (size_t)i * N].x : dg[i]; };
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         // every pair of the sweep checked at once (independent loads): only
@@ -934,7 +949,8 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
         // this sweep raise in skipped rounds are met by the next sweep's check,
         // and a converged S costs one pass instead of N2 - 1 serial rounds
         for (int r = tid; r < N2 - 1; r += blockDim.x) rflag[r] = 0;
-        for (int i = tid; i < N; i += blockDim.x) dg[i] = S[i + (size_t)i * N].x;
+        if (!SM)
+            for (int i = tid; i < N; i += blockDim.x) dg[i] = S[i + (size_t)i * N].x;
         if (tid == 0) {
             s_rot = 0;
             s_nact = 0;
@@ -945,7 +961,7 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
             int i, j;
             hj_pair(N2, round, k, i, j);
             if (j >= N) continue;
-            if (dg[i] < floor2 && dg[j] < floor2) continue;
+            if (diag(i) < floor2 && diag(j) < floor2) continue;
             const double2 s = S[i + (size_t)j * N];
             if (sqrt(s.x * s.x + s.y * s.y) > tol) rflag[round] = 1;
         }
@@ -969,8 +985,8 @@ __global__ void __launch_bounds__(HJ_THREADS) herm_jacobi_kernel(int N, double2 
                 const int slot = atomicAdd(&s_nact, 1);
                 cs[slot] = c;
                 se[slot] = make_double2(sn * s.x / g, sn * s.y / g);   // s e
-                pi[slot] = i;
-                pj[slot] = j;
+                pi[slot] = (PIdx)i;
+                pj[slot] = (PIdx)j;
                 ++mine;
             }
             if (mine) atomicAdd(&s_rot, mine);
@@ -1489,13 +1505,36 @@ __global__ void precision_guard_kernel(int F, const double *__restrict__ fro2, i
 int herm_jacobi_batched(ia_context *ctx, int N, double2 *S, double2 *X, double *LAM, int max_sweeps, int batch,
                         int *info)
 {
-    const int P = (N + (N & 1)) / 2;
+    const int P = (N + (N & 1)) / 2, N2 = 2 * P;
+    // S in shared memory when it fits beside the pair slots (N <= 120 with
+    // 16-bit slot indices and 8-bit round flags): the device's per-CTA limit
+    // less the kernel's static shared memory
+    const size_t smem_s = sizeof(double2) * (size_t)N * N + sizeof(double) * (size_t)(P + (P & 1)) +
+                          sizeof(double2) * P + 2 * sizeof(unsigned short) * P + (size_t)N2;
+    static size_t smem_cap = 0;   // per process: one device type
+    if (!smem_cap) {
+        int optin = 0;
+        cudaFuncAttributes fa{};
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) == cudaSuccess &&
+            cudaFuncGetAttributes(&fa, herm_jacobi_kernel<true>) == cudaSuccess && (size_t)optin > fa.sharedSizeBytes)
+            smem_cap = (size_t)optin - fa.sharedSizeBytes;
+        else
+            smem_cap = 1;
+    }
+    if (smem_s <= smem_cap && N < 65536) {
+        IA_CUDA_TRY(cudaFuncSetAttribute(herm_jacobi_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_s));
+        herm_jacobi_kernel<true><<<batch, HJ_THREADS, smem_s, ctx->stream>>>(N, S, X, LAM, max_sweeps, info);
+        IA_LAUNCH_CHECK(ctx);
+        return IA_OK;
+    }
     const size_t smem = sizeof(double) * (size_t)(P + (P & 1)) + sizeof(double2) * P + 2 * sizeof(int) * P +
-                        sizeof(int) * (size_t)(2 * P) + sizeof(double) * (size_t)N;
+                        sizeof(int) * (size_t)N2 + sizeof(double) * (size_t)N;
     if (smem > 227 * 1024 - 512) return IA_ERR_TOO_LARGE;
     if (smem > 48 * 1024)
-        IA_CUDA_TRY(cudaFuncSetAttribute(herm_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    herm_jacobi_kernel<<<batch, HJ_THREADS, smem, ctx->stream>>>(N, S, X, LAM, max_sweeps, info);
+        IA_CUDA_TRY(cudaFuncSetAttribute(herm_jacobi_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+    herm_jacobi_kernel<false><<<batch, HJ_THREADS, smem, ctx->stream>>>(N, S, X, LAM, max_sweeps, info);
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
 }
