@@ -104,6 +104,77 @@ __global__ void __launch_bounds__(256) gemm_kernel(int opa, int opb, int M, int 
     }
 }
 
+// Rank-K update for K <= GP_K with both operands untransposed (the blocked
+// LU's A22 -= L21 U12 and the blocked solves' B -= L X): the whole A and B
+// panels are staged once (one barrier instead of two per 8-wide K step, and
+// every thread's global loads in flight together), B's rows padded by one
+// element so the column-major panel stores are conflict free.  Same thread
+// layout and the same k order per output as gemm_kernel: bitwise the same
+// results.
+constexpr int GP_K = 32;
+
+template <class T, int BM, int BN, int TM, int TN>
+__global__ void __launch_bounds__(256) gemm_nn_panel_kernel(int M, int N, int K, T alpha,
+                                                            const T *__restrict__ A, int lda, long long sA,
+                                                            const T *__restrict__ B, int ldb, long long sB, T beta,
+                                                            T *__restrict__ C, int ldc, long long sC)
+{
+    constexpr int NTX = BN / TN, NTY = BM / TM;
+    static_assert(NTX * NTY == 256, "256 threads per tile");
+    __shared__ T As[GP_K][BM];
+    __shared__ T Bs[GP_K][BN + 1];
+    const int f = blockIdx.z;
+    A += f * sA;
+    B += f * sB;
+    C += f * sC;
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const T zero = ctraits<T>::make(0, 0);
+#pragma unroll
+    for (int e = threadIdx.x; e < GP_K * BM; e += 256) {
+        const int r = e % BM, kk = e / BM;
+        As[kk][r] = (m0 + r < M && kk < K) ? A[(m0 + r) + (size_t)kk * lda] : zero;
+    }
+#pragma unroll
+    for (int e = threadIdx.x; e < GP_K * BN; e += 256) {
+        const int kk = e % GP_K, c = e / GP_K;
+        Bs[kk][c] = (n0 + c < N && kk < K) ? B[kk + (size_t)(n0 + c) * ldb] : zero;
+    }
+    __syncthreads();
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = zero;
+#pragma unroll 8
+    for (int kk = 0; kk < K; ++kk) {
+        T a[TM], b[TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + NTY * i];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + NTX * j];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) zfma(acc[i][j], a[i], b[j]);
+    }
+    const bool beta0 = (beta.x == 0 && beta.y == 0);
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        int r = m0 + ty + NTY * i;
+        if (r >= M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            int c = n0 + tx + NTX * j;
+            if (c >= N) continue;
+            T v = zmul(alpha, acc[i][j]);
+            T *p = C + r + (size_t)c * ldc;
+            if (!beta0) v = zadd(v, zmul(beta, *p));
+            *p = v;
+        }
+    }
+}
+
 template <class T, int BM, int BN, int TM, int TN>
 static int gemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda,
                        long long sA, const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch)
@@ -115,8 +186,22 @@ static int gemm_launch(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T a
     return IA_OK;
 }
 
-// tile variants: 64x64 (4x4 per thread), 32x32 (2x2), 128x64 (8x4)
+template <class T, int BM, int BN, int TM, int TN>
+static int gemm_panel_launch(ia_context *ctx, int M, int N, int K, T alpha, const T *A, int lda, long long sA,
+                             const T *B, int ldb, long long sB, T beta, T *C, int ldc, long long sC, int batch)
+{
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+    gemm_nn_panel_kernel<T, BM, BN, TM, TN>
+        <<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    IA_LAUNCH_CHECK(ctx);
+    return IA_OK;
+}
+
+// tile variants: 64x64 (4x4 per thread), 32x32 (2x2), 128x64 (8x4); for
+// untransposed operands with K <= GP_K also the staged-panel forms 32x32
+// (2x2) and, FP32 only, 64x64 (4x4)
 constexpr int GEMM_VARIANTS = 3;
+constexpr int GEMM_VARIANTS_PANEL = 5;
 
 template <class T>
 int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, const T *A, int lda, long long sA,
@@ -129,6 +214,14 @@ int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, 
                                                     ldc, sC, batch);
         case 2: return gemm_launch<T, 128, 64, 8, 4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta,
                                                      Cout, ldc, sC, batch);
+        case 3: return gemm_panel_launch<T, 32, 32, 2, 2>(ctx, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cout,
+                                                          ldc, sC, batch);
+        case 4:
+            // 64x64 panels of double2 would take 66 KB, above the static shared-memory limit
+            if constexpr (std::is_same<T, float2>::value)
+                return gemm_panel_launch<T, 64, 64, 4, 4>(ctx, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cout,
+                                                          ldc, sC, batch);
+            return IA_ERR_ARG;
         default: return gemm_launch<T, 64, 64, 4, 4>(ctx, opa, opb, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta,
                                                      Cout, ldc, sC, batch);
         }
@@ -143,7 +236,11 @@ int gemm_batched(ia_context *ctx, Op opa, Op opb, int M, int N, int K, T alpha, 
     key.v[5] = batch;
     const size_t cbytes = sizeof(T) * ((size_t)(batch - 1) * sC + (size_t)ldc * (N - 1) + M);
     TuneScratch scratch{ctx};
-    const int v = tune_select(ctx, key, GEMM_VARIANTS, [&](int vv) -> int {
+    const bool panel = opa == OP_N && opb == OP_N && K <= GP_K;
+    const int nvar = !panel                               ? GEMM_VARIANTS
+                     : std::is_same<T, float2>::value ? GEMM_VARIANTS_PANEL
+                                                      : GEMM_VARIANTS_PANEL - 1;
+    const int v = tune_select(ctx, key, nvar, [&](int vv) -> int {
         if (!scratch.p) {
             int st = scratch.init(C, cbytes);
             if (st) return st;
