@@ -292,7 +292,10 @@ int ia_monopole_batch(ia_context *ctx, int l, int m, int F, const double *d_mics
  *   d_At, d_Bt : F x (m x mt)  columns = surface rows 0..m-1 then CHIEF rows
  *   d_Ahs_t, d_Bhs_t : F x (m x l)  columns = field rows
  * B terms scaled by i rho c k.  Any of the outputs may be NULL only together
- * with its partner. */
+ * with its partner.  IA_PREC_MIXED keeps a per-call table of the
+ * frequency-independent point geometry (8 x 3 x rows x nq x elements bytes,
+ * used up to 1 GiB) in the context's workspace, so it may return
+ * IA_ERR_CAPTURE like the solvers. */
 int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int n_ch,
                            const double *d_cp, int F, const double *d_k, const ia_config *cfg, ia_complex *d_At,
                            ia_complex *d_Bt, ia_complex *d_Ahs_t, ia_complex *d_Bhs_t);

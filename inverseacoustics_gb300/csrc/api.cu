@@ -662,8 +662,17 @@ int ia_ibem_assemble_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
 {
     if (!ctx || !mesh || !cfg || F < 1 || l < 0 || n_ch < 0 || !d_k) return IA_ERR_ARG;
     if ((l > 0 && !d_mics) || (n_ch > 0 && !d_cp)) return IA_ERR_ARG;
+    const bool mixed = cfg->precision == IA_PREC_MIXED;
+    // the double-float assembly's geometry table lives in the workspace
+    float2 *G = nullptr;
+    const size_t gbytes = mixed ? ibem_geom_bytes(mesh, mesh->m + n_ch + l) : 0;
+    if (gbytes) {
+        const int st = ws_reserve(ctx, gbytes);
+        if (st) return st;
+        G = reinterpret_cast<float2 *>(ctx->ws);
+    }
     return ibem_rows(ctx, mesh, l, d_mics, n_ch, d_cp, F, d_k, cfg->c, cfg->rho, (double2 *)d_At, (double2 *)d_Bt,
-                     (double2 *)d_Ahs_t, (double2 *)d_Bhs_t, cfg->precision == IA_PREC_MIXED);
+                     (double2 *)d_Ahs_t, (double2 *)d_Bhs_t, mixed, false, G);
 }
 
 // H^T (m x l per frequency) into Ht, given workspace for A^T, B^T, pivots.
@@ -694,9 +703,11 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
 // the FP64-level products of the mixed transfer run on the tensor cores
 static bool tc_products(const ia_config *cfg, int m) { return tc_products_ok(cfg->gemm_slices, m); }
 
-static size_t transfer_mixed_ws_bytes(int m, int l, int F, const ia_config *cfg)
+static size_t transfer_mixed_ws_bytes(const ia_mesh *mesh, int l, int F, const ia_config *cfg)
 {
-    size_t b = ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F);
+    const int m = mesh->m;
+    size_t b = ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F) +
+               ws_round(ibem_geom_bytes(mesh, m + l));
     if (tc_products(cfg, m))
         b += tc_planes_bytes(m, m, cfg->gemm_slices, false, F) + tc_planes_bytes(l, m, cfg->gemm_slices, true, F) +
              1024;
@@ -719,12 +730,15 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     double2 *Y = cur.take<double2>((size_t)m * l * F);
     double2 *R = cur.take<double2>((size_t)m * l * F);
     float4 *Y4 = cur.take<float4>((size_t)m * l * F);
+    const size_t gbytes = ibem_geom_bytes(mesh, m + l);
+    float2 *G = gbytes ? cur.take<float2>(gbytes / sizeof(float2)) : nullptr;
+    if (cur.off > cur.cap) return IA_ERR_ALLOC;
     // A^T and B^T arrive as double-float pairs (float4, the size of double2)
     float4 *At4 = reinterpret_cast<float4 *>(At), *Bt4 = reinterpret_cast<float4 *>(Bt);
     int st;
     {
         NvtxRange r("ia.assembly");
-        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true);
+        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true, G);
     }
     if (st) return st;
     if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
@@ -783,7 +797,7 @@ int ia_ibem_transfer_batch(ia_context *ctx, const ia_mesh *mesh, int l, const do
     const int m = mesh->m;
     const bool mixed = cfg->precision == IA_PREC_MIXED;
     size_t need = ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
-                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + (mixed ? transfer_mixed_ws_bytes(m, l, F, cfg) : 0);
+                  ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + (mixed ? transfer_mixed_ws_bytes(mesh, l, F, cfg) : 0);
     int st = ws_reserve(ctx, need);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
@@ -1025,12 +1039,13 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
         });
 }
 
-static size_t ibem_solve_ws_bytes(int m, int l, int F, int nrhs, const ia_config *cfg)
+static size_t ibem_solve_ws_bytes(const ia_mesh *mesh, int l, int F, int nrhs, const ia_config *cfg)
 {
     const bool mixed = cfg->precision == IA_PREC_MIXED;
+    const int m = mesh->m;
     return ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
            ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
-           (mixed ? transfer_mixed_ws_bytes(m, l, F, cfg) : 0);
+           (mixed ? transfer_mixed_ws_bytes(mesh, l, F, cfg) : 0);
 }
 
 // the whole IBEM pipeline for F bins on ctx->stream; ev_rows (if given) is
@@ -1076,7 +1091,7 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         if (parts < 1 || parts > IA_SPLIT_PARTS || F % parts || (parts > 1 && (F / parts) % 4)) return IA_ERR_ARG;
     }
     const int Fp = F / parts;
-    const size_t need = ibem_solve_ws_bytes(m, l, Fp, nrhs, cfg);
+    const size_t need = ibem_solve_ws_bytes(mesh, l, Fp, nrhs, cfg);
     int st = ws_reserve(ctx, need * parts);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;

@@ -107,25 +107,46 @@ struct FreqBlock {
     bool uniform;
 };
 
+// Frequency-independent geometry of one quadrature point p (x, y, z at
+// stride n) against x_o: r, 1/r and ft = n.(x_q - x_o) / r^2.
+template <class R>
+__device__ __forceinline__ void point_geometry(const R *__restrict__ p, int n, R nx, R ny, R nz, R xo, R yo, R zo,
+                                               R &r, R &invr, R &ft)
+{
+    const R dx = r_sub(p[0], xo), dy = r_sub(p[(size_t)n], yo), dz = r_sub(p[2 * (size_t)n], zo);
+    const R r2 = r_add(r_add(r_mul(dx, dx), r_mul(dy, dy)), r_mul(dz, dz));
+    invr = r_rsqrt(r2);
+    r = r_mul(r2, invr);
+    const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
+    ft = r_mul(nd, r_mul(invr, invr));
+}
+
 // Regular-rule integral of one element against x_o for the block's
 // frequencies.  qd: precomputed (x, y, z, wa0..2, wb0..2) for each point,
-// structure of arrays with stride n (elements) and 9 * n per point.
-template <class R, int FB, bool CT>
+// structure of arrays with stride n (elements) and 9 * n per point.  GT: the
+// point geometry (r, 1/r, ft) is read from this row's geometry table gq
+// (ibem_geom_kernel; planes of stride n, 3 n per point) instead of computed.
+template <class R, int FB, bool CT, bool GT>
 __device__ __forceinline__ void regular_element(const R *__restrict__ qd, int n, int e, int nq, R nx, R ny, R nz,
-                                                R xo, R yo, R zo, const FreqBlock &fb, const R (&kf)[FB], R dkf,
+                                                R xo, R yo, R zo, const float2 *__restrict__ gq,
+                                                const FreqBlock &fb, const R (&kf)[FB], R dkf,
                                                 const float4 *tab, const DfTrigRed &P, const DfTrigCoef &C,
                                                 const R *cw, cx<R> (&a)[FB][3], cx<R> (&b)[FB][3], R &ct)
 {
     for (int q = 0; q < nq; ++q) {
         const R *p = qd + (size_t)q * 9 * n + e;
-        const R dx = r_sub(p[0], xo), dy = r_sub(p[(size_t)n], yo), dz = r_sub(p[2 * (size_t)n], zo);
         const R wa[3] = {p[3 * (size_t)n], p[4 * (size_t)n], p[5 * (size_t)n]};
         const R wb[3] = {p[6 * (size_t)n], p[7 * (size_t)n], p[8 * (size_t)n]};
-        const R r2 = r_add(r_add(r_mul(dx, dx), r_mul(dy, dy)), r_mul(dz, dz));
-        const R invr = r_rsqrt(r2);
-        const R r = r_mul(r2, invr);
-        const R nd = r_add(r_add(r_mul(nx, dx), r_mul(ny, dy)), r_mul(nz, dz));
-        const R ft = r_mul(nd, r_mul(invr, invr));
+        R r, invr, ft;
+        if constexpr (GT) {
+            const float2 *g = gq + (size_t)q * 3 * n;
+            const float2 g0 = g[0], g1 = g[(size_t)n], g2 = g[2 * (size_t)n];
+            r = R{g0.x, g0.y};
+            invr = R{g1.x, g1.y};
+            ft = R{g2.x, g2.y};
+        } else {
+            point_geometry(p, n, nx, ny, nz, xo, yo, zo, r, invr, ft);
+        }
         if (CT) r_mac(ct, r_mul(cw[q], ft), r_sub(r_zero(R()), invr));   // C term: w_q / 4pi (-ft / r)
         cx<R> ph, step;
         r_sincos(r_mul(kf[0], r), tab, P, C, ph.im, ph.re);
@@ -225,16 +246,16 @@ __device__ __forceinline__ void write_split_rows(int m, int tid, const cx<dfl> *
     }
 }
 
-template <class R>
-__global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
+template <class R, bool GT>
+__global__ void __launch_bounds__(IBEM_THREADS, GT ? 5 : 1) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
     const double *__restrict__ reg,
     const double *__restrict__ sing, int nqs, const double *__restrict__ mics, const double *__restrict__ cp,
     const double *__restrict__ kv, double c, double rho, DfTrigCoef C, DfTrigRed P, const float4 *__restrict__ dftab,
-    int split_ab, const double *__restrict__ creg, double2 *__restrict__ At, double2 *__restrict__ Bt,
-    double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
+    int split_ab, const double *__restrict__ creg, const float2 *__restrict__ gtab, double2 *__restrict__ At,
+    double2 *__restrict__ Bt, double2 *__restrict__ Ahs_t, double2 *__restrict__ Bhs_t)
 {
     constexpr int FB = AsmBlock<R>::FB;
     extern __shared__ __align__(16) unsigned char ibem_smem[];
@@ -244,8 +265,11 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
     __shared__ double ct_red[IBEM_THREADS / 32];
     __shared__ R cw[IBEM_MAX_NQ];   // regular-rule weights w_q / 4pi (the C term)
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int row = blockIdx.x;
-    const int f0 = blockIdx.y * FB;
+    // with the geometry table the frequency blocks of one row are consecutive
+    // CTAs (one 1-D grid), so they read the row's table from L2 together
+    const int nfb = (F + FB - 1) / FB;
+    const int row = GT ? (int)(blockIdx.x / nfb) : (int)blockIdx.x;
+    const int f0 = (GT ? (int)(blockIdx.x % nfb) : (int)blockIdx.y) * FB;
     const int mt = m + n_ch;
     FreqBlock fb;
     fb.nf = F - f0 < FB ? F - f0 : FB;
@@ -289,8 +313,9 @@ __global__ void __launch_bounds__(IBEM_THREADS) ibem_rows_kernel(
             for (int f = 0; f < FB; ++f)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) { a[f][v] = cx_zero<R>(); b[f][v] = cx_zero<R>(); }
-            regular_element<R, FB, !DF>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr, zr, fb,
-                                        kf, dkf, tab, P, C, cw, a, b, ctr);
+            const float2 *gq = GT ? gtab + (size_t)row * nq * 3 * n + e : nullptr;
+            regular_element<R, FB, !DF, GT>(qdat, n, e, nq, qnrm[e], qnrm[e + n], qnrm[e + 2 * (size_t)n], xr, yr,
+                                            zr, gq, fb, kf, dkf, tab, P, C, cw, a, b, ctr);
             if (!DF) ctr = r_norm(ctr);
             const int cols[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
@@ -449,9 +474,59 @@ int mesh_creg(ia_context *ctx, ia_mesh *mesh)
     return IA_OK;
 }
 
+// Geometry table of the double-float assembly: for every row (collocation or
+// field point), regular-rule point q and element e, the frequency-independent
+// r, 1/r and ft (point_geometry, the same arithmetic the rows kernel does
+// inline), stored as (hi, lo) pairs at G[((row nq + q) 3 + c) n + e] so a
+// warp's threads (consecutive elements) load each value coalesced.  The rows
+// kernel then spends its issue slots on the per-frequency work only.  One
+// thread per (row, element).
+__global__ void __launch_bounds__(128) ibem_geom_kernel(int m, int n, int l, int n_ch, int nq, int nblk,
+                                                        const double *__restrict__ nodes, const double *__restrict__ cp,
+                                                        const double *__restrict__ mics, const dfl *__restrict__ qdat,
+                                                        const dfl *__restrict__ qnrm, float2 *__restrict__ G)
+{
+    const int row = (int)(blockIdx.x / nblk);
+    const int e = (int)(blockIdx.x % nblk) * 128 + (int)threadIdx.x;
+    const int mt = m + n_ch;
+    if (e >= n || row >= mt + l) return;
+    double xo, yo, zo;
+    if (row < m) {
+        xo = nodes[row]; yo = nodes[row + m]; zo = nodes[row + 2 * m];
+    } else if (row < mt) {
+        const int i = row - m;
+        xo = cp[i]; yo = cp[i + n_ch]; zo = cp[i + 2 * n_ch];
+    } else {
+        const int i = row - mt;
+        xo = mics[i]; yo = mics[i + l]; zo = mics[i + 2 * l];
+    }
+    const dfl xr = df_from_double(xo), yr = df_from_double(yo), zr = df_from_double(zo);
+    const dfl nx = qnrm[e], ny = qnrm[e + n], nz = qnrm[e + 2 * (size_t)n];
+    const long long gext = (long long)(mt + l) * nq * 3 * n;
+    for (int q = 0; q < nq; ++q) {
+        dfl r, invr, ft;
+        point_geometry(qdat + (size_t)q * 9 * n + e, n, nx, ny, nz, xr, yr, zr, r, invr, ft);
+        const long long o = ((long long)row * nq + q) * 3 * n + e;
+        if (!IA_IDX_OK(o + 2 * (long long)n, gext)) continue;
+        G[o] = make_float2(r.hi, r.lo);
+        G[o + n] = make_float2(invr.hi, invr.lo);
+        G[o + 2 * (size_t)n] = make_float2(ft.hi, ft.lo);
+    }
+}
+
+// Largest geometry table the double-float assembly uses (per call, in the
+// caller's workspace); above it the rows kernel computes the geometry inline.
+constexpr size_t IBEM_GEOM_MAX_BYTES = size_t(1) << 30;
+
+size_t ibem_geom_bytes(const ia_mesh *mesh, int rows)
+{
+    const size_t b = sizeof(float2) * 3 * (size_t)rows * mesh->nq * mesh->n;
+    return b <= IBEM_GEOM_MAX_BYTES ? b : 0;
+}
+
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
-              bool df32, bool split_ab)
+              bool df32, bool split_ab, float2 *gtab)
 {
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
@@ -461,21 +536,38 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
     static const DfTrigCoef coef = df_trig_coefficients();
     static const DfTrigRed red = df_trig_reduction_constants();
-    dim3 g(rows, (F + FB - 1) / FB);
-    if (df32) {
-        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        ibem_rows_kernel<dfl><<<g, IBEM_THREADS, smem, ctx->stream>>>(
+    const int nfb = (F + FB - 1) / FB;
+    dim3 g(rows, nfb);
+    if (df32 && gtab) {
+        // the geometry table (ibem_geom_bytes(mesh, rows) bytes), then the rows
+        // kernel reading it, the frequency blocks of a row in consecutive CTAs
+        const int nblk = (mesh->n + 127) / 128;
+        ibem_geom_kernel<<<(unsigned)rows * nblk, 128, 0, ctx->stream>>>(
+            m, mesh->n, l, n_ch, mesh->nq, nblk, mesh->d_nodes, cp, mics, (const dfl *)mesh->d_qdat_f,
+            (const dfl *)mesh->d_qnrm_f, gtab);
+        IA_LAUNCH_CHECK(ctx);
+        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         220 * 1024));
+        ibem_rows_kernel<dfl, true><<<(unsigned)rows * nfb, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
             (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
             mesh->d_reg, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0,
-            mesh->d_creg, At, Bt, Ahs_t, Bhs_t);
-    } else {
-        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            mesh->d_creg, gtab, At, Bt, Ahs_t, Bhs_t);
+    } else if (df32) {
+        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
-        ibem_rows_kernel<double><<<g, IBEM_THREADS, smem, ctx->stream>>>(
+        ibem_rows_kernel<dfl, false><<<g, IBEM_THREADS, smem, ctx->stream>>>(
+            m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, (const dfl *)mesh->d_qdat_f,
+            (const dfl *)mesh->d_qnrm_f, mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq,
+            mesh->d_reg, mesh->d_sing, mesh->nqs, mics, cp, k, c, rho, coef, red, mesh->d_dftab, split_ab ? 1 : 0,
+            mesh->d_creg, nullptr, At, Bt, Ahs_t, Bhs_t);
+    } else {
+        IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         220 * 1024));
+        ibem_rows_kernel<double, false><<<g, IBEM_THREADS, smem, ctx->stream>>>(
             m, mesh->n, l, n_ch, mesh->ncolors, F, mesh->d_nodes, mesh->d_egeo, mesh->d_qdat, mesh->d_qnrm,
             mesh->d_evert, mesh->d_color_ptr, mesh->d_adj_ptr, mesh->d_adj, mesh->nq, mesh->d_reg, mesh->d_sing,
-            mesh->nqs, mics, cp, k, c, rho, coef, red, nullptr, 0, nullptr, At, Bt, Ahs_t, Bhs_t);
+            mesh->nqs, mics, cp, k, c, rho, coef, red, nullptr, 0, nullptr, nullptr, At, Bt, Ahs_t, Bhs_t);
     }
     IA_LAUNCH_CHECK(ctx);
     return IA_OK;
