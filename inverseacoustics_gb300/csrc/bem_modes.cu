@@ -349,6 +349,7 @@ size_t bem_modes_ws_bytes(const ia_mesh *mesh, int l, int n_ch, int F, int nm, c
                  radiation_modes_ws_bytes(2 * mesh->m, F, c.nr, &c.cfg, true);
         }
     } else b += ws_round(8 * M * M * FF) + ws_round(8 * nm * FF) + radiation_modes_ws_bytes(mesh->m, F, nm, cfg, true);
+    if (cfg->precision == IA_PREC_MIXED) b += ws_round(ibem_geom_bytes(mesh, (int)(MT + L)));   // assembly geometry
     if (bem_mixed_solve(cfg, n_ch)) {
         b += 2 * ws_round(8 * M * M * FF) + ws_round(16 * M * M * FF);
         if (tc_products_ok(bem_slices(cfg), mesh->m))
@@ -373,7 +374,10 @@ static int bem_mixed_z(ia_context *ctx, const ia_mesh *mesh, int l, const double
     const int m = mesh->m;
     const long long mm = (long long)m * m, ml = (long long)m * l;
     int st;
-    if ((st = ibem_rows(ctx, mesh, l, mics, 0, nullptr, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t, true, true)))
+    const size_t gbytes = ibem_geom_bytes(mesh, m + l);
+    float2 *G = gbytes ? cur.take<float2>(gbytes / sizeof(float2)) : nullptr;
+    if (cur.off > cur.cap) return IA_ERR_ALLOC;
+    if ((st = ibem_rows(ctx, mesh, l, mics, 0, nullptr, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t, true, true, G)))
         return st;
     // A, B column-major as float4 pairs (16-byte moves through the double2 view)
     if ((st = ztranspose_batched(ctx, m, m, At, m, mm, A, m, mm, false, F))) return st;
@@ -457,8 +461,11 @@ int bem_modes_batched(ia_context *ctx, const ia_mesh *mesh, int l, const double 
             return st;
     } else {
         // collocation rows, then A, B (mt x m), A_hs, B_hs (l x m) column-major
-        if ((st = ibem_rows(ctx, mesh, l, mics, n_ch, cp, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t,
-                            cfg->precision == IA_PREC_MIXED)))
+        const bool df = cfg->precision == IA_PREC_MIXED;
+        const size_t gbytes = df ? ibem_geom_bytes(mesh, mt + l) : 0;
+        float2 *G = gbytes ? cur.take<float2>(gbytes / sizeof(float2)) : nullptr;
+        if (cur.off > cur.cap) return IA_ERR_ALLOC;
+        if ((st = ibem_rows(ctx, mesh, l, mics, n_ch, cp, F, k, cfg->c, cfg->rho, At, Bt, Ahs_t, Bhs_t, df, false, G)))
             return st;
         if ((st = ztranspose_batched(ctx, m, mt, At, m, tm, A, mt, tm, false, F))) return st;
         if ((st = ztranspose_batched(ctx, m, mt, Bt, m, tm, B, mt, tm, false, F))) return st;

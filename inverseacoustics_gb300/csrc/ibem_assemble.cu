@@ -247,7 +247,7 @@ __device__ __forceinline__ void write_split_rows(int m, int tid, const cx<dfl> *
 }
 
 template <class R, bool GT>
-__global__ void __launch_bounds__(IBEM_THREADS, GT ? 5 : 1) ibem_rows_kernel(
+__global__ void __launch_bounds__(IBEM_THREADS, GT ? 6 : 1) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
