@@ -16,7 +16,10 @@
 // colour share no vertex, so the three column updates of all threads never
 // collide and need no atomics; colours are separated by __syncthreads().  The
 // per-(element, quadrature point) geometry -- x_q, w N_v / 4pi,
-// w N_v |n| / 4pi -- is precomputed at mesh creation.  Within a block,
+// w N_v |n| / 4pi -- is precomputed at mesh creation; the double-float
+// kernel also reads the per-(row, element, point) r, 1/r and n.(x_q - x_o)/r^2
+// from a table computed once per call (ibem_geom_kernel), where the caller
+// gives it workspace for one.  Within a block,
 // exp(i k_f r) advances by one complex multiply per frequency when the k_f are
 // evenly spaced (exp(i k_{f+1} r) = exp(i k_f r) exp(i dk r)), and is
 // evaluated directly otherwise.  For a surface row, the elements incident to
@@ -41,10 +44,12 @@ namespace ia {
 // work of the slow FP64 pipe serve four frequencies.  Double-float: 1 -- the
 // accumulators of a block dominate the registers (244 at 4, 146 at 2, 96 at
 // 1) and the row buffers the shared memory, so one frequency per CTA runs 5
-// CTAs per SM instead of 2, which outweighs recomputing the geometry per
+// CTAs per SM instead of 2, which outweighed recomputing the geometry per
 // frequency (measured per 64-bin launch: 13.1 ms at 4, 11.7 at 2, 11.0 at 1;
-// with the table-driven sin/cos the whole 64-bin pass still runs 28.2 ms at 2
-// against 27.9 at 1).
+// with the table-driven sin/cos the whole 64-bin pass still ran 28.2 ms at 2
+// against 27.9 at 1).  With the geometry table the frequencies of a row share
+// the geometry through L2 instead, and the kernel runs 6 CTAs per SM (80
+// registers): 10.3 -> 7.5 ms per 64-bin assembly.
 constexpr int IBEM_FB_MAX = 4;
 template <class R> struct AsmBlock { static constexpr int FB = 4; };
 template <> struct AsmBlock<dfl> { static constexpr int FB = 1; };
