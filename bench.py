@@ -636,19 +636,22 @@ def run_ours(args):
         del a64
     except Exception:
         pass
-    # The dominant kernel of the pass (44 % of its SM time, 20 % of the
+    # The dominant kernel of the pass (37 % of its SM time, 16 % of the
     # serialised launch list, profiles/ibem_pipeline_mixed_launches_F64.txt)
-    # is the mixed-path assembly, ibem_rows_kernel<dfl>.  Its bound is FP32
+    # is the mixed-path assembly, ibem_rows_kernel<dfl, 1> (reading the
+    # per-call geometry table ibem_geom_kernel writes).  Its bound is FP32
     # instruction issue, not HBM: warp instructions per 64-frequency launch
     # scaled from the ncu capture of the same kernel in
     # profiles/ibem_rows_kernel_dfl_F16.txt
-    # (smsp__inst_executed.sum 1.1914e9 for an 8-frequency launch; the work
+    # (smsp__inst_executed.sum 9.0503e8 for an 8-frequency launch; the work
     # per (row, frequency) CTA is fixed, so 64 frequencies issue 8x that),
     # against one warp instruction per SM sub-partition per clock at the
-    # sampled SM clock; its DRAM bytes (read + write, 767.9 MB per 64
-    # frequencies) come from the launch list's capture.
-    asm_warp_instr = 8 * 1.19142e9
-    asm_traffic = 767.9e6
+    # sampled SM clock.  Its DRAM bytes from the same capture: the rows
+    # written (100.6 MB per 8 frequencies, 8x for 64) and the geometry table
+    # read once per launch (165.2 MB: the frequencies of a row run in
+    # consecutive CTAs and share it through L2).
+    asm_warp_instr = 8 * 9.0503e8
+    asm_traffic = 8 * 100.6e6 + 165.2e6
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.summary().get("sm_mhz") or 2070.0
     issue_peak = props.multi_processor_count * 4 * sm_mhz * 1e6
@@ -658,7 +661,8 @@ def run_ours(args):
     # FP64 path's dense work: LU + solves + transfer GEMM, and the SVD of
     # the 120 x 642 transfer matrices (4 (6 M N^2 + 20 N^3), M = 642, N = 120)
     svd_flops = N_FREQ * 4.0 * (6.0 * m * l * l + 20.0 * l ** 3)
-    roofline = {"kernel": "ibem_rows_kernel<dfl> (mixed-path assembly; the largest share of the pass)",
+    roofline = {"kernel": "ibem_rows_kernel<dfl, 1> (mixed-path assembly; the largest share of the pass; timed "
+                          "with the geometry-table kernel ibem_geom_kernel before it)",
                 "bound": "issue", "achieved": issue_achieved / 1e9, "peak": issue_peak / 1e9,
                 "unit": "G warp-instructions/s", "frac": issue_achieved / issue_peak, "traffic": asm_traffic,
                 "sm_mhz": sm_mhz,
@@ -667,7 +671,7 @@ def run_ours(args):
                 "hbm": {"achieved": asm_bytes / (t_asm / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                         "frac": asm_bytes / (t_asm / 1000.0) / 1e9 / hbm_peak, "peak_kind": peak_kind,
                         "algorithmic_bytes": asm_bytes},
-                "note": "FP32-issue bound (ncu: issue 73 %, FMA pipe 64 %, 698 FP32 lane instructions per "
+                "note": "FP32-issue bound (ncu: issue 75 %, FMA pipe 61 %, 530 FP32 lane instructions per "
                         "quadrature-point evaluation); HBM is not its bound"}
     roofline_tensor = {"kernel": "tc_slice_kernel x2 + tc_gemm_kernel<7> (the transfer's FP64-level products, "
                                  "642 x 120 x 642 complex, 64 bins)",
