@@ -33,6 +33,7 @@
 // the FP64 path, double-float (dfl, df32.cuh) for the mixed path, which moves
 // the dominant work from GB300's FP64 pipe to its FP32 pipe at ~1e-14
 // relative accuracy.  The singular elements stay FP64 in both.
+#include <cstdlib>
 #include <type_traits>
 #include "df32.cuh"
 #include "ia_common.cuh"
@@ -521,10 +522,13 @@ __global__ void __launch_bounds__(128) ibem_geom_kernel(int m, int n, int l, int
 
 // Largest geometry table the double-float assembly uses (per call, in the
 // caller's workspace); above it the rows kernel computes the geometry inline.
+// IA_ASM_GEOM_TABLE=0 selects the inline form at every size.
 constexpr size_t IBEM_GEOM_MAX_BYTES = size_t(1) << 30;
 
 size_t ibem_geom_bytes(const ia_mesh *mesh, int rows)
 {
+    const char *e = getenv("IA_ASM_GEOM_TABLE");
+    if (e && e[0] == '0') return 0;
     const size_t b = sizeof(float2) * 3 * (size_t)rows * mesh->nq * mesh->n;
     return b <= IBEM_GEOM_MAX_BYTES ? b : 0;
 }

@@ -18,7 +18,19 @@ def T(a, dev):
     return torch.as_tensor(np.ascontiguousarray(a), device=dev)
 
 
-def test_mixed_assembly_matches_fp64(cuda, ctx):
+@pytest.fixture(params=["table", "inline"])
+def geom_form(request, monkeypatch):
+    """The double-float assembly with its per-call geometry table (the default
+    wherever the table fits the size limit) and with the geometry computed
+    inline (IA_ASM_GEOM_TABLE=0, the form above the limit)."""
+    if request.param == "inline":
+        monkeypatch.setenv("IA_ASM_GEOM_TABLE", "0")
+    else:
+        monkeypatch.delenv("IA_ASM_GEOM_TABLE", raising=False)
+    return request.param
+
+
+def test_mixed_assembly_matches_fp64(cuda, ctx, geom_form):
     """The mixed path assembles in double-float (FP32 pairs, own sin/cos by
     Cody-Waite reduction + Taylor series): rows agree with the FP64 kernel
     (CUDA sincos/rsqrt) to 1e-13, element by element to 1e-12."""
@@ -38,7 +50,7 @@ def test_mixed_assembly_matches_fp64(cuda, ctx):
         assert np.max(np.abs(b - a)) < 1e-12 * np.max(np.abs(a))
 
 
-def test_mixed_assembly_large_arguments(cuda, ctx):
+def test_mixed_assembly_large_arguments(cuda, ctx, geom_form):
     """kr up to ~150: the table-driven double-float sin/cos reduces by pi/512
     exactly for kr < 100 and hands larger arguments to the FP64-reduced series;
     both regimes (and the switch between them inside one row) agree with the
@@ -56,6 +68,33 @@ def test_mixed_assembly_large_arguments(cuda, ctx):
         a, b = a.cpu().numpy(), b.cpu().numpy()
         for f in range(len(ks)):
             assert relerr(b[f], a[f]) < 1e-12, f
+
+
+def test_mixed_assembly_geometry_table_equals_inline(cuda, ctx, monkeypatch):
+    """The geometry table holds the r, 1/r and n.(x_q - x_o)/r^2 the rows
+    kernel otherwise computes inline, by the same double-float operations:
+    the two forms agree to double-float rounding (1e-13 of each row's largest
+    entry), surface, CHIEF and field rows, evenly and unevenly spaced
+    frequencies."""
+    from inverseacoustics_gb300 import api
+    import torch
+    w = g.ibem_sphere(n_freq=64)
+    nodes, elems, mics = w.arrays["nodes"], w.arrays["elems"], w.arrays["mics"]
+    ks = w.k[[0, 1, 2, 3, 17, 40, 63]]
+    cp = np.array([[0.01, -0.02, 0.015], [-0.03, 0.0, 0.02]]).T.copy()
+    mesh = api.Mesh(ctx, nodes, elems)
+    cfg = api.default_config(precision=1)
+    args = (ctx, mesh, T(mics, cuda), T(ks, cuda), cfg)
+    monkeypatch.delenv("IA_ASM_GEOM_TABLE", raising=False)
+    tab = api.ibem_assemble_batch(*args, cp=T(cp, cuda))
+    monkeypatch.setenv("IA_ASM_GEOM_TABLE", "0")
+    inl = api.ibem_assemble_batch(*args, cp=T(cp, cuda))
+    torch.cuda.synchronize()
+    for a, b in zip(tab, inl):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        scale = np.max(np.abs(b), axis=-1, keepdims=True)
+        assert np.max(np.abs(a - b) / scale) < 1e-13
+    mesh.close()
 
 
 # FP64-level products of the refinement and the transfer GEMM: the
