@@ -703,11 +703,20 @@ static int ibem_transfer_t(ia_context *ctx, const ia_mesh *mesh, int l, const do
 // the FP64-level products of the mixed transfer run on the tensor cores
 static bool tc_products(const ia_config *cfg, int m) { return tc_products_ok(cfg->gemm_slices, m); }
 
-static size_t transfer_mixed_ws_bytes(const ia_mesh *mesh, int l, int F, const ia_config *cfg)
+// The assembly's geometry table: in the transfer's own workspace, or (the
+// staggered parts of one solve) one table that the first part writes and
+// the later parts, which start after the first part's assembly, read.
+struct GeomTable {
+    float2 *p;
+    bool build;
+};
+
+// with_table: the transfer's workspace holds its own geometry table
+static size_t transfer_mixed_ws_bytes(const ia_mesh *mesh, int l, int F, const ia_config *cfg, bool with_table = true)
 {
     const int m = mesh->m;
     size_t b = ws_round(8 * (size_t)m * m * F) + ws_round(8 * (size_t)m * l * F) + 3 * ws_round(16 * (size_t)m * l * F) +
-               ws_round(ibem_geom_bytes(mesh, m + l));
+               (with_table ? ws_round(ibem_geom_bytes(mesh, m + l)) : 0);
     if (tc_products(cfg, m))
         b += tc_planes_bytes(m, m, cfg->gemm_slices, false, F) + tc_planes_bytes(l, m, cfg->gemm_slices, true, F) +
              1024;
@@ -722,7 +731,7 @@ static size_t transfer_mixed_ws_bytes(const ia_mesh *mesh, int l, int F, const i
 static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                                  const double *d_k, const ia_config *cfg, double2 *At, double2 *Bt, int *ipiv,
                                  double2 *Ahs_t, double2 *Ht, int *d_info, WsCursor &cur,
-                                 cudaEvent_t ev_rows = nullptr)
+                                 cudaEvent_t ev_rows = nullptr, const GeomTable *shared_geom = nullptr)
 {
     const int m = mesh->m;
     float2 *M32 = cur.take<float2>((size_t)m * m * F);
@@ -731,14 +740,22 @@ static int ibem_transfer_t_mixed(ia_context *ctx, const ia_mesh *mesh, int l, co
     double2 *R = cur.take<double2>((size_t)m * l * F);
     float4 *Y4 = cur.take<float4>((size_t)m * l * F);
     const size_t gbytes = ibem_geom_bytes(mesh, m + l);
-    float2 *G = gbytes ? cur.take<float2>(gbytes / sizeof(float2)) : nullptr;
+    float2 *G = nullptr;
+    bool build_geom = true;
+    if (shared_geom) {
+        G = gbytes ? shared_geom->p : nullptr;
+        build_geom = shared_geom->build;
+    } else if (gbytes) {
+        G = cur.take<float2>(gbytes / sizeof(float2));
+    }
     if (cur.off > cur.cap) return IA_ERR_ALLOC;
     // A^T and B^T arrive as double-float pairs (float4, the size of double2)
     float4 *At4 = reinterpret_cast<float4 *>(At), *Bt4 = reinterpret_cast<float4 *>(Bt);
     int st;
     {
         NvtxRange r("ia.assembly");
-        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true, G);
+        st = ibem_rows(ctx, mesh, l, d_mics, 0, nullptr, F, d_k, cfg->c, cfg->rho, At, Bt, Ahs_t, Ht, true, true, G,
+                       build_geom);
     }
     if (st) return st;
     if (ev_rows) IA_CUDA_TRY(cudaEventRecord(ev_rows, ctx->stream));
@@ -1039,20 +1056,22 @@ int ia_solve_batch(ia_context *ctx, int m, int n, int F, const ia_complex *d_H, 
         });
 }
 
-static size_t ibem_solve_ws_bytes(const ia_mesh *mesh, int l, int F, int nrhs, const ia_config *cfg)
+static size_t ibem_solve_ws_bytes(const ia_mesh *mesh, int l, int F, int nrhs, const ia_config *cfg,
+                                  bool with_table = true)
 {
     const bool mixed = cfg->precision == IA_PREC_MIXED;
     const int m = mesh->m;
     return ws_round(sizeof(double2) * (size_t)m * m * F) * 2 + ws_round(sizeof(int) * (size_t)m * F) +
            ws_round(sizeof(double2) * (size_t)m * l * F) * 2 + solve_ws_bytes(l, m, F, nrhs, cfg) +
-           (mixed ? transfer_mixed_ws_bytes(mesh, l, F, cfg) : 0);
+           (mixed ? transfer_mixed_ws_bytes(mesh, l, F, cfg, with_table) : 0);
 }
 
 // the whole IBEM pipeline for F bins on ctx->stream; ev_rows (if given) is
 // recorded when the assembly has been issued
 static int ibem_solve_part(ia_context *ctx, const ia_mesh *mesh, int l, const double *d_mics, int F,
                            const double *d_k, int nrhs, const double2 *p, const ia_config *cfg, double2 *x,
-                           double *lambda, double *s, int *info, WsCursor &cur, cudaEvent_t ev_rows)
+                           double *lambda, double *s, int *info, WsCursor &cur, cudaEvent_t ev_rows,
+                           const GeomTable *shared_geom = nullptr)
 {
     const int m = mesh->m;
     double2 *At = cur.take<double2>((size_t)m * m * F);
@@ -1062,7 +1081,8 @@ static int ibem_solve_part(ia_context *ctx, const ia_mesh *mesh, int l, const do
     double2 *Ht = cur.take<double2>((size_t)m * l * F);
     int st;
     if (cfg->precision == IA_PREC_MIXED)
-        st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, info, cur, ev_rows);
+        st = ibem_transfer_t_mixed(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, info, cur, ev_rows,
+                                   shared_geom);
     else st = ibem_transfer_t(ctx, mesh, l, d_mics, F, d_k, cfg, At, Bt, ipiv, Ahs, Ht, info, ev_rows);
     if (st) return st;
     return solve_core(ctx, l, m, F, Ht, true, nrhs, p, cfg, x, lambda, s, info, cur);
@@ -1081,7 +1101,9 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
     // the latency-bound stages of one part (LU panels, Jacobi, QR: one CTA
     // per frequency) run beside the throughput-bound stages of the others,
     // and only the last part's chain is left exposed at the end.  Each part
-    // has its own workspace region.  Frequencies stay in the assembly's
+    // has its own workspace region; the mixed assembly's geometry table is
+    // one region after them, written by the first part and read by all (a
+    // part starts after the previous part's assembly).  Frequencies stay in the assembly's
     // blocks (4 bins in FP64, 1 in double-float; parts are multiples of 4)
     // and every later kernel works per frequency, so the results are bitwise
     // those of one F-bin pass.
@@ -1091,8 +1113,10 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         if (parts < 1 || parts > IA_SPLIT_PARTS || F % parts || (parts > 1 && (F / parts) % 4)) return IA_ERR_ARG;
     }
     const int Fp = F / parts;
-    const size_t need = ibem_solve_ws_bytes(mesh, l, Fp, nrhs, cfg);
-    int st = ws_reserve(ctx, need * parts);
+    const size_t need = ibem_solve_ws_bytes(mesh, l, Fp, nrhs, cfg, parts == 1);
+    const size_t gshared = parts > 1 && cfg->precision == IA_PREC_MIXED ? ibem_geom_bytes(mesh, m + l) : 0;
+    const size_t goff = ws_round(need * parts);
+    int st = ws_reserve(ctx, goff + gshared);
     if (!st) st = clear_info(ctx, d_info, F);
     if (st) return st;
     const int p = l < m ? l : m;
@@ -1125,10 +1149,11 @@ int ia_ibem_solve_batch(ia_context *ctx, const ia_mesh *mesh, int l, const doubl
         ctx->stream = sq;
         ctx->tail_part = q + 1 == parts;
         WsCursor cur{(char *)ctx->ws + need * q, 0, need};
+        const GeomTable geom{reinterpret_cast<float2 *>((char *)ctx->ws + goff), q == 0};
         st = ibem_solve_part(ctx, mesh, l, d_mics, Fp, d_k + f0, nrhs, (const double2 *)d_p + (size_t)f0 * nrhs * l,
                              cfg, (double2 *)d_x + (size_t)f0 * nrhs * m,
                              d_lambda ? d_lambda + (size_t)f0 * nrhs : nullptr, d_s ? d_s + (size_t)f0 * p : nullptr,
-                             d_info + f0, cur, q + 1 < parts ? ctx->ev_rows[q] : nullptr);
+                             d_info + f0, cur, q + 1 < parts ? ctx->ev_rows[q] : nullptr, &geom);
         ctx->stream = main;
         ctx->tail_part = 0;
         if (!st && cur.off > need) st = IA_ERR_ALLOC;   // workspace accounting broken: the parts would overlap

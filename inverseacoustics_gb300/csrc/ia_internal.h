@@ -283,10 +283,11 @@ int bounds_read_svd(IaBoundsSite *out);
 int bounds_read_wide(IaBoundsSite *out);
 int bounds_read_asm(IaBoundsSite *out);
 // gtab (double-float only): scratch of ibem_geom_bytes(mesh, m + n_ch + l)
-// bytes for the per-call geometry table, or null to compute it inline
+// bytes for the per-call geometry table, or null to compute it inline;
+// build_gtab false: the table already holds these rows' geometry
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
-              bool df32 = false, bool split_ab = false, float2 *gtab = nullptr);
+              bool df32 = false, bool split_ab = false, float2 *gtab = nullptr, bool build_gtab = true);
 // bytes of the double-float assembly's geometry table for `rows` rows; 0
 // when it is above the size the assembly uses a table for
 size_t ibem_geom_bytes(const ia_mesh *mesh, int rows);

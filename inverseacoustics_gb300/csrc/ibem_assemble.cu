@@ -408,8 +408,9 @@ __global__ void __launch_bounds__(IBEM_THREADS, GT ? 6 : 1) ibem_rows_kernel(
         const cx<R> *Ar = rowbuf + (size_t)f * 2 * m, *Br = Ar + m;
         double2 *arow, *brow;
         // the row's offset in its output (F x mt x m surface rows or F x l x m field rows)
-        const long long roff = row < mt ? ((long long)fg * mt + row) * m : ((long long)fg * l + (row - mt)) * m;
-        const long long rext = row < mt ? (long long)F * mt * m : (long long)F * l * m;
+        [[maybe_unused]] const long long roff =
+            row < mt ? ((long long)fg * mt + row) * m : ((long long)fg * l + (row - mt)) * m;
+        [[maybe_unused]] const long long rext = row < mt ? (long long)F * mt * m : (long long)F * l * m;
         if (!IA_IDX_OK(roff + m - 1, rext)) continue;
         if (row < mt) {
             arow = At ? At + ((size_t)fg * mt + row) * m : nullptr;
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(128) ibem_geom_kernel(int m, int n, int l, int
     }
     const dfl xr = df_from_double(xo), yr = df_from_double(yo), zr = df_from_double(zo);
     const dfl nx = qnrm[e], ny = qnrm[e + n], nz = qnrm[e + 2 * (size_t)n];
-    const long long gext = (long long)(mt + l) * nq * 3 * n;
+    [[maybe_unused]] const long long gext = (long long)(mt + l) * nq * 3 * n;
     for (int q = 0; q < nq; ++q) {
         dfl r, invr, ft;
         point_geometry(qdat + (size_t)q * 9 * n + e, n, nx, ny, nz, xr, yr, zr, r, invr, ft);
@@ -535,7 +536,7 @@ size_t ibem_geom_bytes(const ia_mesh *mesh, int rows)
 
 int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, int n_ch, const double *cp, int F,
               const double *k, double c, double rho, double2 *At, double2 *Bt, double2 *Ahs_t, double2 *Bhs_t,
-              bool df32, bool split_ab, float2 *gtab)
+              bool df32, bool split_ab, float2 *gtab, bool build_gtab)
 {
     if (mesh->nq > IBEM_MAX_NQ) return IA_ERR_RULE;
     const int m = mesh->m;
@@ -551,10 +552,12 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
         // the geometry table (ibem_geom_bytes(mesh, rows) bytes), then the rows
         // kernel reading it, the frequency blocks of a row in consecutive CTAs
         const int nblk = (mesh->n + 127) / 128;
-        ibem_geom_kernel<<<(unsigned)rows * nblk, 128, 0, ctx->stream>>>(
-            m, mesh->n, l, n_ch, mesh->nq, nblk, mesh->d_nodes, cp, mics, (const dfl *)mesh->d_qdat_f,
-            (const dfl *)mesh->d_qnrm_f, gtab);
-        IA_LAUNCH_CHECK(ctx);
+        if (build_gtab) {
+            ibem_geom_kernel<<<(unsigned)rows * nblk, 128, 0, ctx->stream>>>(
+                m, mesh->n, l, n_ch, mesh->nq, nblk, mesh->d_nodes, cp, mics, (const dfl *)mesh->d_qdat_f,
+                (const dfl *)mesh->d_qnrm_f, gtab);
+            IA_LAUNCH_CHECK(ctx);
+        }
         IA_CUDA_TRY(cudaFuncSetAttribute(ibem_rows_kernel<dfl, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024));
         ibem_rows_kernel<dfl, true><<<(unsigned)rows * nfb, IBEM_THREADS, smem, ctx->stream>>>(
