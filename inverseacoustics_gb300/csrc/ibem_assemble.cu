@@ -49,8 +49,10 @@ namespace ia {
 // frequency (measured per 64-bin launch: 13.1 ms at 4, 11.7 at 2, 11.0 at 1;
 // with the table-driven sin/cos the whole 64-bin pass still ran 28.2 ms at 2
 // against 27.9 at 1).  With the geometry table the frequencies of a row share
-// the geometry through L2 instead, and the kernel runs 6 CTAs per SM (80
-// registers): 10.3 -> 7.5 ms per 64-bin assembly.
+// the geometry through L2 instead, and the kernel runs 7 CTAs per SM (72
+// registers, the sin/cos table read through L1): 10.3 -> 7.3 ms per 64-bin
+// assembly.  The launch bounds keep the inline double-float kernel at 5 CTAs
+// per SM (96 registers) and the FP64 kernel at 3 (168).
 constexpr int IBEM_FB_MAX = 4;
 template <class R> struct AsmBlock { static constexpr int FB = 4; };
 template <> struct AsmBlock<dfl> { static constexpr int FB = 1; };
@@ -253,7 +255,7 @@ __device__ __forceinline__ void write_split_rows(int m, int tid, const cx<dfl> *
 }
 
 template <class R, bool GT>
-__global__ void __launch_bounds__(IBEM_THREADS, GT ? 6 : 1) ibem_rows_kernel(
+__global__ void __launch_bounds__(IBEM_THREADS, GT ? 7 : std::is_same<R, dfl>::value ? 5 : 3) ibem_rows_kernel(
     int m, int n, int l, int n_ch, int ncolors, int F, const double *__restrict__ nodes, const double *__restrict__ egeo,
     const R *__restrict__ qdat, const R *__restrict__ qnrm, const int *__restrict__ evert,
     const int *__restrict__ color_ptr, const int *__restrict__ adj_ptr, const int *__restrict__ adj, int nq,
@@ -267,7 +269,11 @@ __global__ void __launch_bounds__(IBEM_THREADS, GT ? 6 : 1) ibem_rows_kernel(
     extern __shared__ __align__(16) unsigned char ibem_smem[];
     cx<R> *rowbuf = reinterpret_cast<cx<R> *>(ibem_smem);   // FB x (A row, B row), m each
     constexpr bool DF = std::is_same<R, dfl>::value;
-    float4 *tab = DF ? reinterpret_cast<float4 *>(rowbuf + 2 * FB * (size_t)m) : nullptr;   // sin/cos table
+    // sin/cos table: staged in shared memory, except in the table-reading
+    // kernel, which reads it through L1 (its 16 KB make room for a seventh
+    // CTA per SM)
+    float4 *tab_s = DF && !GT ? reinterpret_cast<float4 *>(rowbuf + 2 * FB * (size_t)m) : nullptr;
+    const float4 *tab = DF ? (GT ? dftab : tab_s) : nullptr;
     __shared__ double ct_red[IBEM_THREADS / 32];
     __shared__ R cw[IBEM_MAX_NQ];   // regular-rule weights w_q / 4pi (the C term)
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -291,8 +297,8 @@ __global__ void __launch_bounds__(IBEM_THREADS, GT ? 6 : 1) ibem_rows_kernel(
     for (int f = 0; f < FB; ++f) kf[f] = r_of_double<R>(fb.k[f]);
     const R dkf = r_of_double<R>(fb.dk);
     for (int j = tid; j < 2 * FB * m; j += blockDim.x) rowbuf[j] = cx_zero<R>();
-    if (DF)
-        for (int j = tid; j < DF_TRIG_TABLE; j += blockDim.x) tab[j] = dftab[j];
+    if (tab_s)
+        for (int j = tid; j < DF_TRIG_TABLE; j += blockDim.x) tab_s[j] = dftab[j];
     for (int q = tid; q < nq; q += blockDim.x) cw[q] = r_of_double<R>(reg[q + 2 * nq] * IA_INV4PI);
     double xo, yo, zo;
     int self = -1;
@@ -542,7 +548,8 @@ int ibem_rows(ia_context *ctx, const ia_mesh *mesh, int l, const double *mics, i
     const int m = mesh->m;
     const int rows = m + n_ch + l;
     const int FB = df32 ? AsmBlock<dfl>::FB : AsmBlock<double>::FB;
-    const size_t smem = sizeof(double2) * 2 * (size_t)m * FB + (df32 ? DF_TRIG_TABLE * sizeof(float4) : 0);
+    // the table-reading kernel reads the sin/cos table through L1
+    const size_t smem = sizeof(double2) * 2 * (size_t)m * FB + (df32 && !gtab ? DF_TRIG_TABLE * sizeof(float4) : 0);
     if (smem > 220 * 1024) return IA_ERR_TOO_LARGE;
     static const DfTrigCoef coef = df_trig_coefficients();
     static const DfTrigRed red = df_trig_reduction_constants();
