@@ -643,8 +643,9 @@ def run_ours(args):
     # instruction issue, not HBM: warp instructions per 64-frequency launch
     # scaled from the ncu capture of the same kernel in
     # profiles/ibem_rows_kernel_dfl_F16.txt
-    # (smsp__inst_executed.sum 9.0503e8 for an 8-frequency launch; the work
-    # per (row, frequency) CTA is fixed, so 64 frequencies issue 8x that),
+    # (smsp__inst_executed.sum 9.0503e8 for an 8-frequency launch of the
+    # 6-CTA-per-SM build, the last one captured; the work per (row,
+    # frequency) CTA is fixed, so 64 frequencies issue 8x that),
     # against one warp instruction per SM sub-partition per clock at the
     # sampled SM clock.  Its DRAM bytes from the same capture: the rows
     # written (100.6 MB per 8 frequencies, 8x for 64) and the geometry table
